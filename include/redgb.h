@@ -1,0 +1,202 @@
+/*
+ * redgb.h -- C ABI of the GB300 (sm_103a) implementation of red.cuda's hot path:
+ * direct-summation gravity, Runge-Kutta stage combination with the embedded error
+ * norm (RK4, RKF5, RKF7(8)) and close-encounter / collision-merge / ejection /
+ * hit-star event detection.
+ *
+ * The reference has no FFI layer: the path sits behind two C++ classes,
+ * `pp_disk` (red.cuda/src/red.cuda/pp_disk.h:14-195) and `integrator`
+ * (red.cuda/src/red.cuda/integrator.h:17-88), built by `options::create_pp_disk` /
+ * `options::create_integrator` (red.cuda/src/red.cuda/options.cpp:197-274) and driven by
+ * the time loop in red.cuda/src/red.cuda/main.cu:176-263.  Every entry point below
+ * names the reference member function it replaces.
+ *
+ * Conventions
+ *  - plain pointers and sizes, no C++ or torch types; every call returns an int status
+ *    (RG_OK == 0, negative on error) instead of throwing, and rg_last_error() gives the
+ *    message of the calling thread's last failure;
+ *  - records use the reference's own layouts (red.cuda/red.type/red_type.h, as compiled
+ *    on Linux: natural alignment, no forced 16-byte alignment); sizes are asserted in
+ *    redgb_types.h;
+ *  - caller-facing units are the reference's file units: AU, solar masses, days and
+ *    AU/day; internally time runs in units of 1/k days (k = Gauss' constant) exactly as
+ *    in the reference (pp_disk.cu:1512-1551, integrator.cu:29) so that G = 1;
+ *  - one context drives one GPU (the device current at rg_create) on its own stream.
+ */
+#ifndef REDGB_H
+#define REDGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "redgb_types.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+enum {
+    RG_OK                  = 0,
+    RG_ERR_ARG             = -1,  /* bad argument (null pointer, size, enum value)       */
+    RG_ERR_CUDA            = -2,  /* a CUDA runtime call or kernel launch failed          */
+    RG_ERR_EVENT_OVERFLOW  = -3,  /* more events in one step than the event buffer holds  */
+    RG_ERR_DT_NONFINITE    = -4,  /* the step-size controller produced inf/nan or 0       */
+    RG_ERR_STATE           = -5,  /* call out of order (e.g. rg_step before an integrator) */
+    RG_ERR_NOT_IMPLEMENTED = -6,  /* reference refuses it too (super-planetesimal merge)  */
+    RG_ERR_NOMEM           = -7,  /* device or host allocation failed                     */
+    RG_ERR_NO_DEVICE       = -8   /* no CUDA device / the library was built without one   */
+};
+
+/* gravity kernels */
+enum {
+    RG_GRAVITY_FP64  = 0, /* FP64, reference operation order, bit-identical to the CPU path */
+    RG_GRAVITY_MIXED = 1  /* FP64 displacements, FP32 rsqrt + FP64 Newton, compensated FP32 */
+};
+
+/* semantics switches (both default to the reference's CPU path, the oracle) */
+enum {
+    RG_EVENT_TIME_CPU   = 0, /* NSI/NI sinks stamp events with the step-start time
+                                (pp_disk.cu:576,581)                                        */
+    RG_EVENT_TIME_STAGE = 1  /* every sink stamps its stage time (GPU path, pp_disk.cu:279)  */
+};
+
+/* ------------------------------------------------------------------ library */
+
+/* Message of the calling thread's most recent failed call ("" if none). */
+const char* rg_last_error(void);
+
+/* Library version string and the device architecture it was compiled for. */
+const char* rg_version(void);
+
+/* Number of CUDA devices visible to the library (0 if none).  Never fails. */
+int rg_device_count(void);
+
+/* ------------------------------------------------------------------ one disk */
+
+typedef struct rg_ctx rg_ctx;
+
+/*
+ * Replaces pp_disk::pp_disk + pp_disk::load (pp_disk.cu:1204-1235,1614-1683) and the
+ * set-up in options::create_pp_disk (options.cpp:197-235): bodies are given in the
+ * reference's storage order (stars, giants, rocky, proto, super-planetesimals,
+ * planetesimals, test particles -- the counts in `n`), in AU and AU/day.  As in the
+ * reference the system is moved to its barycentre if body 0 sits at rest in the origin,
+ * velocities and epochs are rescaled to internal time units, and `thr` (the five
+ * threshold_t values, red_type.h:46-54) is copied as by pp_disk::copy_threshold
+ * (pp_disk.cu:1441-1452).  `epoch` may be NULL.  `event_capacity` bounds the number
+ * of raw event records one step may produce (0 -> max(n_total, 1024)); the reference
+ * sizes this buffer to n_total and never checks it (pp_disk.cu:1262,1267).
+ */
+int rg_create(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v,
+              const rg_param_t* p, const rg_body_metadata_t* md, const double* epoch,
+              const double thr[RG_THRESHOLD_N], int event_capacity, rg_ctx** out);
+
+/* Frees every host and device buffer of the context (pp_disk::~pp_disk, pp_disk.cu:1237). */
+int rg_destroy(rg_ctx* ctx);
+
+/*
+ * Replaces options::create_integrator (options.cpp:237-274) and the integrator
+ * constructors (integrator.cu:27-52, int_rungekutta4.cu:102, int_rungekutta8.cu:463).
+ * `type` is an integrator_type_t: RG_INT_EULER, RG_INT_RK4, RG_INT_RK5 (Cash-Karp,
+ * restated from int_rungekutta5.cu, which does not build in the reference) or
+ * RG_INT_RKF78.  `dt_day` is the first trial step in days (main.cu:141 uses 0.001).
+ */
+int rg_set_integrator(rg_ctx* ctx, int type, double dt_day, int adaptive, double tolerance,
+                      int error_check_for_tp);
+
+/*
+ * The reference's event switches: `close_encounter` and `inner_steps`
+ * (parameter.cpp:36-37,160-190; pp_disk.h:126-127).  `hill_factor` > 0 additionally
+ * logs a CLOSE_ENCOUNTER for every interacting pair closer than hill_factor mutual
+ * Hill radii (not in the reference; 3 for the planetesimal-disk workloads).
+ * `event_time_mode` is RG_EVENT_TIME_CPU (default) or RG_EVENT_TIME_STAGE.
+ */
+int rg_set_event_options(rg_ctx* ctx, int close_encounter, int inner_steps,
+                         double hill_factor, int event_time_mode);
+
+/* Selects the gravity kernel (RG_GRAVITY_FP64 default, RG_GRAVITY_MIXED). */
+int rg_set_gravity_mode(rg_ctx* ctx, int mode);
+
+/* Sets the simulation clock in days (pp_disk::t = parameter::start_time). */
+int rg_set_time(rg_ctx* ctx, double t_day);
+
+/*
+ * One integration step with the reference's step-size control: replaces
+ * rungekutta4::step (int_rungekutta4.cu:189-273), rungekutta5::step
+ * (int_rungekutta5.cu:202-282), rungekutta8::step (int_rungekutta8.cu:704-797) and
+ * euler::step.  Collision / close-encounter records found in the stages are kept for
+ * rg_check_for_collision exactly as the reference keeps them in d_events.
+ */
+int rg_step(rg_ctx* ctx, double* dt_did_day);
+
+/* pp_disk::check_for_ejection_hit_centrum (pp_disk.cu:683-715) with its handler
+ * (pp_disk.cu:1091-1109): `n_handled` receives the number of events. */
+int rg_check_for_ejection_hit_centrum(rg_ctx* ctx, int* n_handled);
+
+/* pp_disk::check_for_collision (pp_disk.cu:717-738): dedup per pair keeping the
+ * earliest record (pp_disk.cu:1111-1149) and merge (pp_disk.cu:1151-1202). */
+int rg_check_for_collision(rg_ctx* ctx, int* n_handled);
+
+/* pp_disk::check_for_close_encounter(true) (pp_disk.cu:742-770): moves the recorded
+ * close encounters into the event log. */
+int rg_check_for_close_encounter(rg_ctx* ctx, int* n_handled);
+
+/* pp_disk::check_for_rebuild_vectors (pp_disk.cu:893-907): compacts the storage once
+ * at least `n` events have been handled since the last compaction. */
+int rg_check_for_rebuild_vectors(rg_ctx* ctx, int n, int* rebuilt);
+
+/*
+ * The time loop of main.cu:176-263 without file output: ejection / hit-star check,
+ * step, collision or close-encounter handling and compaction, repeated while
+ * t <= t_stop_day (main.cu:176) and fewer than `max_steps` steps were taken
+ * (max_steps <= 0: no limit).  `n_steps` (may be NULL) receives the steps taken.
+ */
+int rg_advance(rg_ctx* ctx, double t_stop_day, int64_t max_steps, int64_t* n_steps);
+
+/*
+ * Drains the event log: the records pp_disk::print_event_data writes
+ * (pp_disk.cu:1772-1848), in the order it writes them, with the reference's internal
+ * units (t in 1/k days, velocities in AU per 1/k days).  Copies at most `cap`
+ * records, returns the number copied in *n and removes them from the log.
+ */
+int rg_events(rg_ctx* ctx, rg_event_t* out, int cap, int* n);
+int rg_event_count(rg_ctx* ctx, int* n);
+
+/* Current body count (active + inactive until the next compaction). */
+int rg_get_n_total(rg_ctx* ctx, rg_counts_t* n, int* n_total);
+
+/*
+ * Copies the state out in the reference's record layouts and file units (AU, AU/day,
+ * days), like pp_disk::copy_to_host + print_result_ascii (pp_disk.cu:1426,1685).
+ * Any output pointer may be NULL.  Arrays must hold n_total records.
+ */
+int rg_get_state(rg_ctx* ctx, rg_vec_t* r, rg_vec_t* v, rg_param_t* p,
+                 rg_body_metadata_t* md, double* t_day);
+
+/* Same, in internal units (velocities in AU per 1/k days), bit-exact device contents. */
+int rg_get_state_internal(rg_ctx* ctx, rg_vec_t* r, rg_vec_t* v, rg_param_t* p,
+                          rg_body_metadata_t* md, double* t_internal);
+
+/* Replaces the positions and velocities (file units) of all n_total bodies. */
+int rg_set_state(rg_ctx* ctx, const rg_vec_t* r, const rg_vec_t* v);
+
+/* One force evaluation at the current state (pp_disk::calc_dydx(1, ...),
+ * pp_disk.cu:998-1041) in internal units; events it finds are discarded. */
+int rg_calc_accel(rg_ctx* ctx, rg_vec_t* a);
+
+/* Integrator and event counters (integrator.cu:258-278, pp_disk.h:129-133). */
+int rg_get_counters(rg_ctx* ctx, rg_counters_t* c);
+
+/* Total energy and angular momentum over the force model's pair set (internal units,
+ * G = 1), FP64 with compensated sums.  Not in the reference. */
+int rg_energy(rg_ctx* ctx, double* energy, double angmom[3]);
+
+/* Last step-size values in days: the step that was taken and the next trial step. */
+int rg_get_dt(rg_ctx* ctx, double* dt_did_day, double* dt_try_day);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* REDGB_H */

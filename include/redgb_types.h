@@ -1,0 +1,127 @@
+/*
+ * redgb_types.h -- record layouts and enumerations shared by the C ABI (redgb.h), the
+ * CUDA library and the CPU oracle.  They are the reference's own types
+ * (red.cuda/red.type/red_type.h) as laid out by gcc on Linux, where __BUILTIN_ALIGN__
+ * is empty (red_type.h:117-121): natural alignment, so a body file written by the
+ * reference, or a record array handed over by reference-side code, can be passed in
+ * unchanged.
+ */
+#ifndef REDGB_TYPES_H
+#define REDGB_TYPES_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* red_type.h:136-143 vec_t (w is always 0; it only pads the record to 32 bytes) */
+typedef struct rg_vec { double x, y, z, w; } rg_vec_t;
+
+/* red_type.h:146-152 param_t */
+typedef struct rg_param { double mass, radius, density, cd; } rg_param_t;
+
+/* red_type.h:155-161 body_metadata_t (24 bytes: 3 int32 + 4 pad + double) */
+typedef struct rg_body_metadata {
+    int32_t id;
+    int32_t body_type;
+    int32_t mig_type;
+    double  mig_stop_at;
+} rg_body_metadata_t;
+
+/* red_type.h:101-115 orbelem_t */
+typedef struct rg_orbelem { double sma, ecc, inc, peri, node, mean; } rg_orbelem_t;
+
+/* red_type.h:230-277 event_data_t, 472 bytes */
+typedef struct rg_event {
+    int32_t      event_name;   /* event_name_t                                */
+    double       t;            /* time of the event (internal units)          */
+    double       d;            /* distance of the bodies                      */
+    int32_t      id1, idx1;    /* survivor                                    */
+    rg_param_t   p1;
+    rg_vec_t     r1, v1;
+    rg_orbelem_t oe1;
+    int32_t      id2, idx2;    /* merger                                      */
+    rg_param_t   p2;
+    rg_vec_t     r2, v2;
+    rg_orbelem_t oe2;
+    rg_param_t   ps;           /* survivor after the event                    */
+    rg_vec_t     rs, vs;
+    rg_orbelem_t oes;
+} rg_event_t;
+
+/* number_of_bodies constructor arguments (number_of_bodies.h:7) */
+typedef struct rg_counts {
+    int32_t n_s, n_gp, n_rp, n_pp, n_spl, n_pl, n_tp;
+} rg_counts_t;
+
+/* integrator counters (integrator.h:65-67) and event counters (pp_disk.h:129-133) */
+typedef struct rg_counters {
+    int64_t n_failed_step, n_passed_step, n_tried_step;
+    int64_t n_hit_centrum[3], n_ejection[3], n_collision[3], n_close_encounter[3], n_event[3];
+    int64_t n_gravity_evals;   /* force evaluations (not in the reference) */
+    int64_t n_pairs;           /* interacting pairs evaluated              */
+} rg_counters_t;
+
+/* red_type.h:46-54 threshold_t */
+enum {
+    RG_THRESHOLD_HIT_CENTRUM_DISTANCE = 0,
+    RG_THRESHOLD_EJECTION_DISTANCE = 1,
+    RG_THRESHOLD_RADII_ENHANCE_FACTOR = 2,
+    RG_THRESHOLD_HIT_CENTRUM_DISTANCE_SQUARED = 3,
+    RG_THRESHOLD_EJECTION_DISTANCE_SQUARED = 4,
+    RG_THRESHOLD_N = 5
+};
+
+/* red_type.h:56-64 integrator_type_t */
+enum {
+    RG_INT_EULER = 0,
+    RG_INT_RK2 = 1,
+    RG_INT_RK4 = 2,
+    RG_INT_RK5 = 3,
+    RG_INT_RKF78 = 4
+};
+
+/* red_type.h:66-74 event_name_t */
+enum {
+    RG_EVENT_NONE = 0,
+    RG_EVENT_HIT_CENTRUM = 1,
+    RG_EVENT_EJECTION = 2,
+    RG_EVENT_CLOSE_ENCOUNTER = 3,
+    RG_EVENT_COLLISION = 4
+};
+
+/* red_type.h:90-99 body_type_t */
+enum {
+    RG_BODY_STAR = 0,
+    RG_BODY_GIANTPLANET = 1,
+    RG_BODY_ROCKYPLANET = 2,
+    RG_BODY_PROTOPLANET = 3,
+    RG_BODY_SUPERPLANETESIMAL = 4,
+    RG_BODY_PLANETESIMAL = 5,
+    RG_BODY_TESTPARTICLE = 6,
+    RG_BODY_PADDINGPARTICLE = 7
+};
+
+/* red_type.h:76-82 event_counter_name_t */
+enum { RG_COUNTER_TOTAL = 0, RG_COUNTER_LAST_CLEAR = 1, RG_COUNTER_LAST_STEP = 2 };
+
+#ifdef __cplusplus
+}
+#endif
+
+#if defined(__cplusplus)
+static_assert(sizeof(rg_vec_t) == 32, "vec_t is 32 bytes");
+static_assert(sizeof(rg_param_t) == 32, "param_t is 32 bytes");
+static_assert(sizeof(rg_body_metadata_t) == 24, "body_metadata_t is 24 bytes");
+static_assert(sizeof(rg_orbelem_t) == 48, "orbelem_t is 48 bytes");
+static_assert(sizeof(rg_event_t) == 472, "event_data_t is 472 bytes");
+#elif defined(__STDC_VERSION__) && __STDC_VERSION__ >= 201112L
+_Static_assert(sizeof(rg_vec_t) == 32, "vec_t is 32 bytes");
+_Static_assert(sizeof(rg_param_t) == 32, "param_t is 32 bytes");
+_Static_assert(sizeof(rg_body_metadata_t) == 24, "body_metadata_t is 24 bytes");
+_Static_assert(sizeof(rg_orbelem_t) == 48, "orbelem_t is 48 bytes");
+_Static_assert(sizeof(rg_event_t) == 472, "event_data_t is 472 bytes");
+#endif
+
+#endif /* REDGB_TYPES_H */
