@@ -1,0 +1,308 @@
+"""Benchmark of the gravity + Runge-Kutta hot path on GB300 (one JSON line).
+
+Workload (default): 16384 self-gravitating planetesimals (m log-uniform 1e-9..1e-7 Msun,
+Sigma ~ r^-1.5 on 1..4 AU) around a 1 Msun star, RK4 with a fixed 0.1-day step.  A
+bench step is one RK4 step: 4 force evaluations of 16385 x 16384 pairs plus the stage
+combinations.  Metric: simulated years per second (and interacting pairs per second).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl ours|reference] [--mode mixed|fp64]
+
+--impl reference times the FP64 CPU path (the oracle port of the reference's CPU code,
+one core, the reference is single threaded) on the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "red.cuda.closeencounter_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from redgb import bodies, types as T  # noqa: E402
+
+WORKLOADS = {
+    # name: (config, n, integrator, dt_day, adaptive)
+    "self_gravitating_16384_rk4": ("self_gravitating", 16384, T.INT_RK4, 0.1, False),
+    "planetesimal_disk_rkf78": ("planetesimal_disk", 1024, T.INT_RKF78, 0.001, True),
+}
+FLOP_PER_PAIR = 36  # the reference's own count (pp_disk.cu:170-184,293)
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return rank, ws, dist
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if f[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def flush_l2(buf):
+    """Writes a buffer larger than the 129 MB L2 between timed steps."""
+    buf.zero_()
+
+
+def run_ours(args, rank, ws, dist):
+    import torch
+
+    from redgb import lib
+
+    cfg, n, int_type, dt_day, adaptive = WORKLOADS[args.workload]
+    dev = torch.cuda.current_device()
+    disk = bodies.config_disk(cfg, n=n, seed=rank)
+    thr = bodies.thresholds(collision_factor=0.0)
+    mode = T.GRAVITY_MIXED if args.mode == "mixed" else T.GRAVITY_FP64
+    pairs = disk.pairs_per_eval()
+    evals_per_step = {T.INT_RK4: 4 + (1 if adaptive else 0), T.INT_RKF78: 13 if adaptive else 11,
+                      T.INT_RK5: 6}[int_type]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def make(mode_):
+        s = lib.System(disk, thr)
+        s.set_integrator(int_type, dt_day, adaptive, 1e-10)
+        s.set_gravity_mode(mode_)
+        return s
+
+    def timed_steps(s, k, prof=False):
+        """Per-step CUDA-event time on the library's stream, L2 flushed between steps."""
+        ext = torch.cuda.ExternalStream(s.stream())
+        tot = 0.0
+        days = 0.0
+        if prof:
+            s.set_profiling(True)
+            s.profile()
+        for _ in range(k):
+            flush_l2(flush)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            days += s.step()
+            e1.record(ext)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+        p = s.profile() if prof else None
+        if prof:
+            s.set_profiling(False)
+        return tot / 1e3, days, p
+
+    sysm = make(mode)
+    for _ in range(args.warmup):
+        sysm.step()
+    E0, _ = sysm.energy()
+    k0 = sysm.counters()["n_kernels"]
+    clocks = ClockSampler(dev)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    secs, days, prof = timed_steps(sysm, args.steps, prof=True)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if dist:
+        t = torch.tensor([secs], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dist.barrier()
+        secs = float(t.item())
+    launches = sysm.counters()["n_kernels"] - k0
+    E1, _ = sysm.energy()
+    years = days / T.YEAR
+    value = ws * years / secs
+    pairs_per_s = ws * args.steps * evals_per_step * pairs / secs
+
+    # e2e: the public API with host buffers every step (state in, step, state out)
+    r_h, v_h = sysm.state()[:2]
+    nbytes = disk.n_total * 6 * 8
+    t_e2e = 0.0
+    e2e_days = 0.0
+    for _ in range(args.steps):
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sysm.set_state(r_h, v_h)
+        e2e_days += sysm.step()
+        r_h, v_h = sysm.state()[:2]
+        t_e2e += time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([t_e2e], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_e2e = float(t.item())
+    e2e = {"value": ws * (e2e_days / T.YEAR) / t_e2e, "unit": "sim-years/s", "h2d_bytes_per_step": nbytes,
+           "d2h_bytes_per_step": nbytes}
+
+    out = None
+    if rank == 0:
+        from redgb import lib as L
+        kind = 0 if mode == T.GRAVITY_MIXED else 1
+        peak = L.measure_pipe_peak(kind)
+        avg_ms = prof["gravity_ms"] / max(prof["gravity_launches"], 1)
+        achieved = pairs * FLOP_PER_PAIR / (avg_ms * 1e-3) / 1e12
+        # the FP64 form of the same step, for the mixed/FP64 comparison
+        fp = make(T.GRAVITY_FP64)
+        for _ in range(min(args.warmup, 3)):
+            fp.step()
+        k_fp = max(2, min(args.steps, 5))
+        s_fp, d_fp, _ = timed_steps(fp, k_fp)
+        ae = fp.calc_accel()
+        fp.set_gravity_mode(T.GRAVITY_MIXED)
+        am = fp.calc_accel()
+        a_e = np.stack([ae[f] for f in "xyz"], 1)
+        a_m = np.stack([am[f] for f in "xyz"], 1)
+        rel = np.linalg.norm(a_m - a_e, axis=1) / np.linalg.norm(a_e, axis=1)
+        out = {
+            "metric": "sim-years/s", "value": value, "unit": "sim-years/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32" if mode == T.GRAVITY_MIXED else "f64",
+            "data": "synthetic seeded disk (no public dataset exists)",
+            "config": {"workload": args.workload, "bodies": disk.n_total, "integrator": "RK4 fixed 0.1 day",
+                       "gravity": args.mode, "pairs_per_eval": pairs, "evals_per_step": evals_per_step,
+                       "l2": "flushed between timed steps (256 MB write)", "parallelism": f"replicas x{ws}"},
+            "pairs_per_s": pairs_per_s,
+            "dE_over_E": abs((E1 - E0) / E0),
+            "e2e": e2e,
+            "gpu_launches": int(launches),
+            "roofline": {"bound": "fp32" if kind == 0 else "fp64", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                         "kernel": "grav_mixed_kernel" if kind == 0 else "grav_fp64_pairpar",
+                         "peak_source": "measured FMA-chain microbenchmark on this GPU (rg_measure_pipe_peak)",
+                         "flop_per_pair": FLOP_PER_PAIR, "avg_launch_ms": avg_ms},
+            "fp64_form": {"value": (d_fp / T.YEAR) / s_fp, "ms_per_step": 1e3 * s_fp / k_fp,
+                          "pairs_per_s": k_fp * evals_per_step * pairs / s_fp,
+                          "fp64_peak_tflops": L.measure_pipe_peak(1),
+                          "achieved_tflops": k_fp * evals_per_step * pairs * FLOP_PER_PAIR / s_fp / 1e12},
+            "mixed_force_error": {"max_rel": float(rel.max()), "rms_rel": float(np.sqrt(np.mean(rel ** 2)))},
+            "clocks": clk,
+        }
+        if ws == 1 and not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(args, disk, int_type, dt_day, adaptive, samples=args.cpu_steps)
+    return out
+
+
+def cpu_baseline(args, disk, int_type, dt_day, adaptive, samples):
+    """The oracle (the reference's CPU path restated in C, single thread) on the same disk."""
+    import pyoracle
+    o = pyoracle.OracleSystem(disk, bodies.thresholds(collision_factor=0.0))
+    o.set_integrator(int_type, dt_day, adaptive, 1e-10)
+    t0 = time.perf_counter()
+    days = 0.0
+    for _ in range(samples):
+        days += o.step()
+    secs = time.perf_counter() - t0
+    return {"value": (days / T.YEAR) / secs, "unit": "sim-years/s", "cores": 1, "kind": "port",
+            "sample": f"{samples} integrator steps of the same {disk.n_total}-body workload",
+            "seconds": secs}
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return None
+    cfg, n, int_type, dt_day, adaptive = WORKLOADS[args.workload]
+    disk = bodies.config_disk(cfg, n=n, seed=0)
+    import pyoracle
+    o = pyoracle.OracleSystem(disk, bodies.thresholds(collision_factor=0.0))
+    o.set_integrator(int_type, dt_day, adaptive, 1e-10)
+    for _ in range(args.warmup):
+        o.step()
+    t0 = time.perf_counter()
+    days = 0.0
+    for _ in range(args.steps):
+        days += o.step()
+    secs = time.perf_counter() - t0
+    value = (days / T.YEAR) / secs
+    return {"metric": "sim-years/s", "value": value, "unit": "sim-years/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "impl": "reference",
+            "data": "synthetic seeded disk (no public dataset exists)",
+            "config": {"workload": args.workload, "bodies": disk.n_total, "integrator": "RK4 fixed 0.1 day"},
+            "cpu_baseline": {"value": value, "unit": "sim-years/s", "cores": 1, "kind": "port",
+                             "sample": f"{args.steps} full integrator steps, single thread (the reference's "
+                                       "CPU path is serial)"},
+            "e2e": {"value": value, "unit": "sim-years/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--workload", default="self_gravitating_16384_rk4", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        rank, ws = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+        out = run_reference(args, rank, ws)
+    else:
+        rank, ws, dist = dist_init()
+        out = run_ours(args, rank, ws, dist)
+        if dist:
+            dist.destroy_process_group()
+    if out is not None:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

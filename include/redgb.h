@@ -31,6 +31,12 @@
 
 #include "redgb_types.h"
 
+#if defined(__GNUC__)
+#define RG_API __attribute__((visibility("default")))
+#else
+#define RG_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -64,13 +70,13 @@ enum {
 /* ------------------------------------------------------------------ library */
 
 /* Message of the calling thread's most recent failed call ("" if none). */
-const char* rg_last_error(void);
+RG_API const char* rg_last_error(void);
 
 /* Library version string and the device architecture it was compiled for. */
-const char* rg_version(void);
+RG_API const char* rg_version(void);
 
 /* Number of CUDA devices visible to the library (0 if none).  Never fails. */
-int rg_device_count(void);
+RG_API int rg_device_count(void);
 
 /* ------------------------------------------------------------------ one disk */
 
@@ -88,12 +94,12 @@ typedef struct rg_ctx rg_ctx;
  * of raw event records one step may produce (0 -> max(n_total, 1024)); the reference
  * sizes this buffer to n_total and never checks it (pp_disk.cu:1262,1267).
  */
-int rg_create(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v,
+RG_API int rg_create(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v,
               const rg_param_t* p, const rg_body_metadata_t* md, const double* epoch,
               const double thr[RG_THRESHOLD_N], int event_capacity, rg_ctx** out);
 
 /* Frees every host and device buffer of the context (pp_disk::~pp_disk, pp_disk.cu:1237). */
-int rg_destroy(rg_ctx* ctx);
+RG_API int rg_destroy(rg_ctx* ctx);
 
 /*
  * Replaces options::create_integrator (options.cpp:237-274) and the integrator
@@ -102,7 +108,7 @@ int rg_destroy(rg_ctx* ctx);
  * restated from int_rungekutta5.cu, which does not build in the reference) or
  * RG_INT_RKF78.  `dt_day` is the first trial step in days (main.cu:141 uses 0.001).
  */
-int rg_set_integrator(rg_ctx* ctx, int type, double dt_day, int adaptive, double tolerance,
+RG_API int rg_set_integrator(rg_ctx* ctx, int type, double dt_day, int adaptive, double tolerance,
                       int error_check_for_tp);
 
 /*
@@ -112,14 +118,14 @@ int rg_set_integrator(rg_ctx* ctx, int type, double dt_day, int adaptive, double
  * Hill radii (not in the reference; 3 for the planetesimal-disk workloads).
  * `event_time_mode` is RG_EVENT_TIME_CPU (default) or RG_EVENT_TIME_STAGE.
  */
-int rg_set_event_options(rg_ctx* ctx, int close_encounter, int inner_steps,
+RG_API int rg_set_event_options(rg_ctx* ctx, int close_encounter, int inner_steps,
                          double hill_factor, int event_time_mode);
 
 /* Selects the gravity kernel (RG_GRAVITY_FP64 default, RG_GRAVITY_MIXED). */
-int rg_set_gravity_mode(rg_ctx* ctx, int mode);
+RG_API int rg_set_gravity_mode(rg_ctx* ctx, int mode);
 
 /* Sets the simulation clock in days (pp_disk::t = parameter::start_time). */
-int rg_set_time(rg_ctx* ctx, double t_day);
+RG_API int rg_set_time(rg_ctx* ctx, double t_day);
 
 /*
  * One integration step with the reference's step-size control: replaces
@@ -128,23 +134,23 @@ int rg_set_time(rg_ctx* ctx, double t_day);
  * euler::step.  Collision / close-encounter records found in the stages are kept for
  * rg_check_for_collision exactly as the reference keeps them in d_events.
  */
-int rg_step(rg_ctx* ctx, double* dt_did_day);
+RG_API int rg_step(rg_ctx* ctx, double* dt_did_day);
 
 /* pp_disk::check_for_ejection_hit_centrum (pp_disk.cu:683-715) with its handler
  * (pp_disk.cu:1091-1109): `n_handled` receives the number of events. */
-int rg_check_for_ejection_hit_centrum(rg_ctx* ctx, int* n_handled);
+RG_API int rg_check_for_ejection_hit_centrum(rg_ctx* ctx, int* n_handled);
 
 /* pp_disk::check_for_collision (pp_disk.cu:717-738): dedup per pair keeping the
  * earliest record (pp_disk.cu:1111-1149) and merge (pp_disk.cu:1151-1202). */
-int rg_check_for_collision(rg_ctx* ctx, int* n_handled);
+RG_API int rg_check_for_collision(rg_ctx* ctx, int* n_handled);
 
 /* pp_disk::check_for_close_encounter(true) (pp_disk.cu:742-770): moves the recorded
  * close encounters into the event log. */
-int rg_check_for_close_encounter(rg_ctx* ctx, int* n_handled);
+RG_API int rg_check_for_close_encounter(rg_ctx* ctx, int* n_handled);
 
 /* pp_disk::check_for_rebuild_vectors (pp_disk.cu:893-907): compacts the storage once
  * at least `n` events have been handled since the last compaction. */
-int rg_check_for_rebuild_vectors(rg_ctx* ctx, int n, int* rebuilt);
+RG_API int rg_check_for_rebuild_vectors(rg_ctx* ctx, int n, int* rebuilt);
 
 /*
  * The time loop of main.cu:176-263 without file output: ejection / hit-star check,
@@ -152,7 +158,7 @@ int rg_check_for_rebuild_vectors(rg_ctx* ctx, int n, int* rebuilt);
  * t <= t_stop_day (main.cu:176) and fewer than `max_steps` steps were taken
  * (max_steps <= 0: no limit).  `n_steps` (may be NULL) receives the steps taken.
  */
-int rg_advance(rg_ctx* ctx, double t_stop_day, int64_t max_steps, int64_t* n_steps);
+RG_API int rg_advance(rg_ctx* ctx, double t_stop_day, int64_t max_steps, int64_t* n_steps);
 
 /*
  * Drains the event log: the records pp_disk::print_event_data writes
@@ -160,40 +166,56 @@ int rg_advance(rg_ctx* ctx, double t_stop_day, int64_t max_steps, int64_t* n_ste
  * units (t in 1/k days, velocities in AU per 1/k days).  Copies at most `cap`
  * records, returns the number copied in *n and removes them from the log.
  */
-int rg_events(rg_ctx* ctx, rg_event_t* out, int cap, int* n);
-int rg_event_count(rg_ctx* ctx, int* n);
+RG_API int rg_events(rg_ctx* ctx, rg_event_t* out, int cap, int* n);
+RG_API int rg_event_count(rg_ctx* ctx, int* n);
 
 /* Current body count (active + inactive until the next compaction). */
-int rg_get_n_total(rg_ctx* ctx, rg_counts_t* n, int* n_total);
+RG_API int rg_get_n_total(rg_ctx* ctx, rg_counts_t* n, int* n_total);
 
 /*
  * Copies the state out in the reference's record layouts and file units (AU, AU/day,
  * days), like pp_disk::copy_to_host + print_result_ascii (pp_disk.cu:1426,1685).
  * Any output pointer may be NULL.  Arrays must hold n_total records.
  */
-int rg_get_state(rg_ctx* ctx, rg_vec_t* r, rg_vec_t* v, rg_param_t* p,
+RG_API int rg_get_state(rg_ctx* ctx, rg_vec_t* r, rg_vec_t* v, rg_param_t* p,
                  rg_body_metadata_t* md, double* t_day);
 
 /* Same, in internal units (velocities in AU per 1/k days), bit-exact device contents. */
-int rg_get_state_internal(rg_ctx* ctx, rg_vec_t* r, rg_vec_t* v, rg_param_t* p,
+RG_API int rg_get_state_internal(rg_ctx* ctx, rg_vec_t* r, rg_vec_t* v, rg_param_t* p,
                           rg_body_metadata_t* md, double* t_internal);
 
 /* Replaces the positions and velocities (file units) of all n_total bodies. */
-int rg_set_state(rg_ctx* ctx, const rg_vec_t* r, const rg_vec_t* v);
+RG_API int rg_set_state(rg_ctx* ctx, const rg_vec_t* r, const rg_vec_t* v);
 
 /* One force evaluation at the current state (pp_disk::calc_dydx(1, ...),
  * pp_disk.cu:998-1041) in internal units; events it finds are discarded. */
-int rg_calc_accel(rg_ctx* ctx, rg_vec_t* a);
+RG_API int rg_calc_accel(rg_ctx* ctx, rg_vec_t* a);
 
 /* Integrator and event counters (integrator.cu:258-278, pp_disk.h:129-133). */
-int rg_get_counters(rg_ctx* ctx, rg_counters_t* c);
+RG_API int rg_get_counters(rg_ctx* ctx, rg_counters_t* c);
 
 /* Total energy and angular momentum over the force model's pair set (internal units,
  * G = 1), FP64 with compensated sums.  Not in the reference. */
-int rg_energy(rg_ctx* ctx, double* energy, double angmom[3]);
+RG_API int rg_energy(rg_ctx* ctx, double* energy, double angmom[3]);
 
 /* Last step-size values in days: the step that was taken and the next trial step. */
-int rg_get_dt(rg_ctx* ctx, double* dt_did_day, double* dt_try_day);
+RG_API int rg_get_dt(rg_ctx* ctx, double* dt_did_day, double* dt_try_day);
+
+/* ------------------------------------------------------------------ measurement */
+
+/* The CUDA stream (cudaStream_t) the context launches on, for callers that time or
+ * order their own work against it. */
+RG_API int rg_get_stream(rg_ctx* ctx, void** stream);
+
+/* Records CUDA events around every force evaluation and stage kernel of the context
+ * (on its stream) when `on` is non-zero; rg_get_profile sums their device times. */
+RG_API int rg_set_profiling(rg_ctx* ctx, int on);
+RG_API int rg_get_profile(rg_ctx* ctx, rg_profile_t* prof);
+
+/* Measured throughput of one arithmetic pipe of the current device, in TFLOP/s
+ * (an FMA counts 2): kind 0 = FP32 FMA, 1 = FP64 FMA.  A chain of independent FMAs
+ * per thread on every SM, timed with CUDA events. */
+RG_API int rg_measure_pipe_peak(int kind, double* tflops);
 
 #ifdef __cplusplus
 }

@@ -61,7 +61,16 @@ typedef struct rg_counters {
     int64_t n_hit_centrum[3], n_ejection[3], n_collision[3], n_close_encounter[3], n_event[3];
     int64_t n_gravity_evals;   /* force evaluations (not in the reference) */
     int64_t n_pairs;           /* interacting pairs evaluated              */
+    int64_t n_kernels;         /* CUDA kernels launched by the library     */
 } rg_counters_t;
+
+/* kernel timing of a context (rg_set_profiling): CUDA events around every launch */
+typedef struct rg_profile {
+    int64_t gravity_launches;  /* force evaluations timed            */
+    double  gravity_ms;        /* their summed device time           */
+    int64_t stage_launches;    /* stage-combine / error kernels timed */
+    double  stage_ms;
+} rg_profile_t;
 
 /* red_type.h:46-54 threshold_t */
 enum {

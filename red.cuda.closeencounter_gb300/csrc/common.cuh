@@ -1,0 +1,80 @@
+// common.cuh -- device data layout and records shared by the kernels and the host driver.
+//
+// HBM layout of one force evaluation (all FP64, structure of arrays so every kernel reads
+// and writes unit-stride, coalesced rows):
+//   state y  : 6 rows of n doubles  [rx | ry | rz | vx | vy | vz]
+//   stage k_r: 6 rows of n doubles  [v_r (dr/dt) | a_r (dv/dt)]
+//   stage positions P: 3 rows of n doubles
+//   body data: mass[n], radius[n], id[n] (int32), rho[n] (distance from body 0, Hill test)
+// The reference's 4-component vec_t w slot is always 0 and never stored here.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace redgb {
+
+// One rectangular block of the interaction matrix: sinks [sink_begin, sink_end) feel the
+// sources [src_begin, src_end) (number_of_bodies::get_bound_SI/NSI/NI,
+// number_of_bodies.cpp:196-258).  `sys` is the disk of an ensemble (0 for one disk);
+// `base` is the disk's first body.  `block` is 0 for SI, 1 for NSI, 2 for NI sinks.
+struct Tile {
+    int sink_begin, sink_end;
+    int src_begin, src_end;
+    int sys, base, block, pad;
+};
+
+// A collision / close-encounter / Hill-sphere candidate found by a gravity kernel.
+// The host turns it into the reference's 472-byte event_data_t.
+struct DevEvent {
+    uint32_t seq;   // (attempt << 8) | stage
+    int32_t kind;   // 0: radius criterion (pp_disk.cu:265), 1: mutual Hill sphere
+    int32_t i, j;   // sink, source (body indices of the whole batch)
+    int32_t sys, pad;
+    double d;
+    double ri[3], vi[3], rj[3], vj[3], r0[3], v0[3];
+};
+
+struct EventBuf {
+    DevEvent* rec;
+    unsigned int* count;  // may exceed cap: the host reports RG_ERR_EVENT_OVERFLOW
+    unsigned int cap;
+};
+
+// Arguments of one force evaluation over a tile list.
+struct GravArgs {
+    const double* __restrict__ px;  // stage positions, rows of n
+    const double* __restrict__ py;
+    const double* __restrict__ pz;
+    const double* __restrict__ vx;  // stage velocities (event records only)
+    const double* __restrict__ vy;
+    const double* __restrict__ vz;
+    const double* __restrict__ mass;
+    const double* __restrict__ radius;
+    const int* __restrict__ id;
+    const double* __restrict__ rho;  // |r_i - r_0| of the step-start state (Hill test)
+    double* ax;  // output rows
+    double* ay;
+    double* az;
+    const Tile* tiles;
+    int n_tiles;
+    double f_rad;      // THRESHOLD_RADII_ENHANCE_FACTOR
+    double hill_f3;    // hill_factor^3
+    int record;        // record radius-criterion candidates
+    int hill;          // record Hill candidates
+    uint32_t seq;
+    EventBuf ev;  // radius-criterion records
+    EventBuf hv;  // Hill-sphere records
+};
+
+}  // namespace redgb
+
+#define RG_CUDA_CHECK(expr)                                                   \
+    do {                                                                      \
+        cudaError_t _e = (expr);                                              \
+        if (_e != cudaSuccess) return ::redgb::cuda_fail(_e, #expr, __FILE__, __LINE__); \
+    } while (0)
+
+namespace redgb {
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+}

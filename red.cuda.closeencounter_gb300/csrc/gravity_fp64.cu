@@ -1,0 +1,233 @@
+// gravity_fp64.cu -- FP64 direct-summation gravity with collision / close-encounter
+// screening, bit-identical to the reference's FP64 path.
+//
+// Reference: kernel_pp_disk::calc_grav_accel (pp_disk.cu:217-296) and its CPU twin
+// pp_disk::cpu_calc_grav_accel_SI (pp_disk.cu:404-572).  For every sink i the reference
+// adds the source terms m_j (r_j - r_i) / (|r_j - r_i| * |r_j - r_i|^2) one after the
+// other in ascending j.  This file is compiled with -fmad=false and keeps that operation
+// order, so the accelerations equal the CPU path's bit for bit.
+//
+// GB300 design.  The serial sum is only 3 FP64 adds per pair; the sqrt, the division and
+// the multiplies (~35 FP64 operations) do not depend on the order.  The pair-parallel
+// kernel therefore lets all 256 threads of a CTA compute the S x J pair terms of a tile
+// (S sinks x J sources) into shared memory, and 3 S threads then add them in source
+// order.  That keeps every SM's FP64 pipe busy however few sinks a block has (3 sinks x
+// 1027 sources in the planetesimal disk), which thread-per-sink scheduling cannot.
+// The row-serial kernel (thread per sink) serves blocks with few sources per sink
+// (planetesimals x 3 massive bodies).  Sources are staged through shared memory in both.
+#include "common.cuh"
+
+namespace redgb {
+
+struct PairOut {
+    double tx, ty, tz;
+};
+
+// One (sink, source) pair: the term added to a_i and the event tests of pp_disk.cu:265
+// (radius criterion) and of the mutual Hill sphere (cube form, no cube root).
+__device__ __forceinline__ void pair_term(const GravArgs& g, const Tile& tile, int i, int j, double xi, double yi,
+                                          double zi, double Ri, double mi, double rhoi, double xj, double yj,
+                                          double zj, double mj, double Rj, double rhoj, PairOut& o)
+{
+    const double dx = xj - xi;
+    const double dy = yj - yi;
+    const double dz = zj - zi;
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    const double d = sqrt(r2);
+    const double w = mj / (d * r2);
+    o.tx = w * dx;
+    o.ty = w * dy;
+    o.tz = w * dz;
+    const int li = i - tile.base, lj = j - tile.base;
+    bool rad = g.record && li > 0 && li > lj && d < g.f_rad * (Ri + Rj);
+    bool hill = false;
+    if (g.hill && tile.block != 2 && li > 0 && li > lj && lj > 0) {
+        const double h = 0.5 * (rhoi + rhoj);
+        const double lhs = d * d * d;
+        const double rhs = ((g.hill_f3 * (mi + mj)) / (3.0 * g.mass[tile.base])) * (h * h * h);
+        hill = lhs < rhs;
+    }
+    if (rad || hill) {
+        for (int kind = 0; kind < 2; kind++) {
+            if (!(kind == 0 ? rad : hill)) continue;
+            const EventBuf& eb = kind == 0 ? g.ev : g.hv;
+            unsigned int slot = atomicAdd(eb.count, 1u);
+            if (slot < eb.cap) {
+                DevEvent* e = &eb.rec[slot];
+                e->seq = g.seq;
+                e->kind = kind;
+                e->i = i;
+                e->j = j;
+                e->sys = tile.sys;
+                e->pad = 0;
+                e->d = d;
+                const int b0 = tile.base;
+                e->ri[0] = xi; e->ri[1] = yi; e->ri[2] = zi;
+                e->rj[0] = xj; e->rj[1] = yj; e->rj[2] = zj;
+                e->vi[0] = g.vx[i]; e->vi[1] = g.vy[i]; e->vi[2] = g.vz[i];
+                e->vj[0] = g.vx[j]; e->vj[1] = g.vy[j]; e->vj[2] = g.vz[j];
+                e->r0[0] = g.px[b0]; e->r0[1] = g.py[b0]; e->r0[2] = g.pz[b0];
+                e->v0[0] = g.vx[b0]; e->v0[1] = g.vy[b0]; e->v0[2] = g.vz[b0];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Pair-parallel kernel: CTA = S sinks, source tiles of J = 1024 / S.
+template <int S>
+__global__ void __launch_bounds__(256) grav_fp64_pairpar(GravArgs g)
+{
+    constexpr int NT = 256;
+    constexpr int J = 1024 / S;
+    constexpr int STRIDE = NT / S;  // source offset between a thread's terms
+    constexpr int JPT = J / STRIDE;  // terms per thread per tile
+    __shared__ double tx[J * S], ty[J * S], tz[J * S];
+    __shared__ double sx[J], sy[J], sz[J], sm[J], sR[J], srho[J];
+    __shared__ int sid[J];
+
+    const Tile tile = g.tiles[blockIdx.x];
+    const int t = threadIdx.x;
+    const int s = t % S;
+    const int q0 = t / S;
+    const int i = tile.sink_begin + s;
+    const bool sink_ok = i < tile.sink_end;
+    double xi = 0, yi = 0, zi = 0, Ri = 0, mi = 0, rhoi = 0;
+    bool active = false;
+    if (sink_ok) {
+        xi = g.px[i]; yi = g.py[i]; zi = g.pz[i];
+        Ri = g.radius[i]; mi = g.mass[i];
+        rhoi = g.hill ? g.rho[i] : 0.0;
+        active = 0 < g.id[i];
+    }
+    const int bc = t / S;  // phase-B component (0, 1, 2) for t < 3 S
+    const double* Tb = bc == 0 ? tx : (bc == 1 ? ty : tz);
+    double acc = 0.0;
+
+    for (int j0 = tile.src_begin; j0 < tile.src_end; j0 += J) {
+        const int nj = min(J, tile.src_end - j0);
+        for (int q = t; q < nj; q += NT) {
+            const int j = j0 + q;
+            sx[q] = g.px[j]; sy[q] = g.py[j]; sz[q] = g.pz[j];
+            sm[q] = g.mass[j]; sR[q] = g.radius[j]; sid[q] = g.id[j];
+            srho[q] = g.hill ? g.rho[j] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < JPT; k++) {
+            const int q = q0 + k * STRIDE;
+            const int j = j0 + q;
+            PairOut o{0.0, 0.0, 0.0};
+            if (active && q < nj && j != i && 0 <= sid[q])
+                pair_term(g, tile, i, j, xi, yi, zi, Ri, mi, rhoi, sx[q], sy[q], sz[q], sm[q], sR[q], srho[q], o);
+            tx[q * S + s] = o.tx;
+            ty[q * S + s] = o.ty;
+            tz[q * S + s] = o.tz;
+        }
+        __syncthreads();
+        if (t < 3 * S) {
+            for (int q = 0; q < nj; q++) acc = acc + Tb[q * S + s];
+        }
+        __syncthreads();
+    }
+    if (t < 3 * S && sink_ok) {
+        double* out = bc == 0 ? g.ax : (bc == 1 ? g.ay : g.az);
+        out[i] = acc;
+    }
+}
+
+// ---------------------------------------------------------------------------------------
+// Row-serial kernel: one thread per sink, sources staged through shared memory.
+__global__ void __launch_bounds__(128) grav_fp64_rowseq(GravArgs g)
+{
+    constexpr int NT = 128;
+    __shared__ double sx[NT], sy[NT], sz[NT], sm[NT], sR[NT], srho[NT];
+    __shared__ int sid[NT];
+    const Tile tile = g.tiles[blockIdx.x];
+    const int t = threadIdx.x;
+    const int i = tile.sink_begin + t;
+    const bool sink_ok = i < tile.sink_end;
+    double xi = 0, yi = 0, zi = 0, Ri = 0, mi = 0, rhoi = 0;
+    bool active = false;
+    if (sink_ok) {
+        xi = g.px[i]; yi = g.py[i]; zi = g.pz[i];
+        Ri = g.radius[i]; mi = g.mass[i];
+        rhoi = g.hill ? g.rho[i] : 0.0;
+        active = 0 < g.id[i];
+    }
+    double ax = 0.0, ay = 0.0, az = 0.0;
+    for (int j0 = tile.src_begin; j0 < tile.src_end; j0 += NT) {
+        const int nj = min(NT, tile.src_end - j0);
+        if (t < nj) {
+            const int j = j0 + t;
+            sx[t] = g.px[j]; sy[t] = g.py[j]; sz[t] = g.pz[j];
+            sm[t] = g.mass[j]; sR[t] = g.radius[j]; sid[t] = g.id[j];
+            srho[t] = g.hill ? g.rho[j] : 0.0;
+        }
+        __syncthreads();
+        if (active) {
+            for (int q = 0; q < nj; q++) {
+                const int j = j0 + q;
+                if (j == i || 0 > sid[q]) continue;
+                PairOut o;
+                pair_term(g, tile, i, j, xi, yi, zi, Ri, mi, rhoi, sx[q], sy[q], sz[q], sm[q], sR[q], srho[q], o);
+                ax = ax + o.tx;
+                ay = ay + o.ty;
+                az = az + o.tz;
+            }
+        }
+        __syncthreads();
+    }
+    if (sink_ok) {
+        g.ax[i] = ax;
+        g.ay[i] = ay;
+        g.az[i] = az;
+    }
+}
+
+// Distance of every body from its disk's body 0 (the star), for the Hill test:
+// sqrt(SQR(x_i - x_0) + SQR(y_i - y_0) + SQR(z_i - z_0)).
+__global__ void star_distance(const double* __restrict__ x, const double* __restrict__ y,
+                              const double* __restrict__ z, const int* __restrict__ base_of, int n,
+                              double* __restrict__ rho)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int b = base_of ? base_of[i] : 0;
+    const double dx = x[i] - x[b], dy = y[i] - y[b], dz = z[i] - z[b];
+    rho[i] = sqrt(dx * dx + dy * dy + dz * dz);
+}
+
+// ---------------------------------------------------------------------------------------
+// Host launchers
+int launch_grav_fp64_pairpar(const GravArgs& g, int S, cudaStream_t st)
+{
+    if (g.n_tiles <= 0) return 0;
+    if (S == 16)
+        grav_fp64_pairpar<16><<<g.n_tiles, 256, 0, st>>>(g);
+    else if (S == 32)
+        grav_fp64_pairpar<32><<<g.n_tiles, 256, 0, st>>>(g);
+    else
+        grav_fp64_pairpar<8><<<g.n_tiles, 256, 0, st>>>(g);
+    RG_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int launch_grav_fp64_rowseq(const GravArgs& g, cudaStream_t st)
+{
+    if (g.n_tiles <= 0) return 0;
+    grav_fp64_rowseq<<<g.n_tiles, 128, 0, st>>>(g);
+    RG_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int launch_star_distance(const double* x, const double* y, const double* z, const int* base_of, int n, double* rho,
+                         cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    star_distance<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, base_of, n, rho);
+    RG_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+}  // namespace redgb

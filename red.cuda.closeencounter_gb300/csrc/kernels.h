@@ -1,0 +1,82 @@
+// kernels.h -- launch arguments of the stage, error, ejection and energy kernels
+// (stages.cu) and of the gravity kernels (gravity_fp64.cu, gravity_mixed.cu).
+#pragma once
+
+#include "common.cuh"
+
+namespace redgb {
+
+constexpr int MAXT = 9;  // longest stage row (RKF7(8) stage 12)
+
+// Forms of a stage sum; each is the exact expression of one reference kernel.
+enum CombineForm {
+    FORM_SUM = 0,     // y + dt * (c0 k0 + c1 k1 + ...)           rk8_kernel::calc_ytemp_for_f*, euler sum_vector
+    FORM_SCALED = 1,  // y + (c0 * dt) * k0                        rk4_kernel::sum_vector (int_rungekutta4.cu:37-48)
+    FORM_ACC = 2,     // acc = y; acc += dt * c_q * k_q (c_q != 0)  rk5_kernel::calc_ytemp / calc_y_np1
+    FORM_RK4_NP1 = 3, // y + (b0 dt)(k0 + k3) + (b1 dt)(k1 + k2)    rk4_kernel::calc_y_np1 (int_rungekutta4.cu:50-61)
+    FORM_RK8_NP1 = 4  // y + dt (b0 k0 + b5 k5 + b6 (k6 + k7) + b8 (k8 + k9) + b10 k10)  int_rungekutta8.cu:322-333
+};
+
+struct CombineArgs {
+    const double* y;           // 6 rows
+    const double* k[MAXT];     // stage derivatives used by this row (6 rows each)
+    double c[MAXT];            // coefficients
+    int nterm;
+    int form;
+    int n;                     // bodies
+    int stride;                // row stride of every buffer (>= n)
+    const double* dt;          // device scalar: the trial step (internal units)
+    double* out_lo;            // rows 0..2 of the result (positions)
+    double* out_hi;            // rows 3..5 of the result (velocities)
+};
+
+int launch_combine(const CombineArgs& a, cudaStream_t st);
+
+enum ErrForm { ERR_RK4 = 0, ERR_RK5 = 1, ERR_RK8 = 2 };
+
+struct ErrArgs {
+    const double* k[6];
+    double c[6];
+    int form;
+    int stride;  // row stride
+    int n_err;   // bodies checked per row
+    unsigned long long* max_bits;  // device scalar, zeroed before the launch
+};
+
+int launch_error_max(const ErrArgs& a, cudaStream_t st);
+
+// Ejection / hit-star candidate (index, kind, r^2).
+struct EjectRec {
+    int i;
+    int kind;  // RG_EVENT_EJECTION or RG_EVENT_HIT_CENTRUM
+    double r2;
+};
+
+int launch_ejection(const double* x, const double* y, const double* z, const int* id, const int* type, int n,
+                    const double* thr, EjectRec* rec, unsigned int* count, unsigned int cap, cudaStream_t st);
+
+struct EnergyArgs {
+    const double* y;  // 6 rows of stride
+    const double* mass;
+    const int* id;
+    int n, n_si, n_massive, stride;
+    double* part;  // 5 rows of n: T, U, Lx, Ly, Lz
+};
+
+int launch_energy(const EnergyArgs& a, cudaStream_t st);
+
+int launch_grav_fp64_pairpar(const GravArgs& g, int S, cudaStream_t st);
+int launch_grav_fp64_rowseq(const GravArgs& g, cudaStream_t st);
+// mixed precision (gravity_mixed.cu): positions split into FP32 (hi, lo) once per evaluation
+constexpr int MIXED_SINKS_PER_TILE = 64;
+constexpr size_t SPLIT_POS_BYTES = 32;  // per body
+int launch_split_positions(const double* x, const double* y, const double* z, const double* m, int n,
+                           struct SplitPos* out, cudaStream_t st);
+int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* heavy_end, float near_ratio,
+                            cudaStream_t st);
+int launch_star_distance(const double* x, const double* y, const double* z, const int* base_of, int n, double* rho,
+                         cudaStream_t st);
+
+int measure_pipe_peak(int kind, double* tflops);
+
+}  // namespace redgb

@@ -80,7 +80,7 @@ class Counters(ctypes.Structure):
                 ("n_hit_centrum", ctypes.c_int64 * 3), ("n_ejection", ctypes.c_int64 * 3),
                 ("n_collision", ctypes.c_int64 * 3), ("n_close_encounter", ctypes.c_int64 * 3),
                 ("n_event", ctypes.c_int64 * 3), ("n_gravity_evals", ctypes.c_int64),
-                ("n_pairs", ctypes.c_int64)]
+                ("n_pairs", ctypes.c_int64), ("n_kernels", ctypes.c_int64)]
 
     def as_dict(self):
         out = {}
@@ -88,6 +88,12 @@ class Counters(ctypes.Structure):
             val = getattr(self, f)
             out[f] = list(val) if not isinstance(val, int) else val
         return out
+
+
+class Profile(ctypes.Structure):
+    """rg_profile_t: summed device time of timed launches."""
+    _fields_ = [("gravity_launches", ctypes.c_int64), ("gravity_ms", ctypes.c_double),
+                ("stage_launches", ctypes.c_int64), ("stage_ms", ctypes.c_double)]
 
 
 def ptr(a):

@@ -15,6 +15,7 @@ for p in (PKG, os.path.join(ROOT, "oracle")):
 
 from redgb import bodies, types as T  # noqa: E402
 from redgb.driver import run_main_loop  # noqa: E402
+from redgb.types import event_key  # noqa: E402,F401
 
 GOLDEN = os.path.join(ROOT, "tests", "golden")
 INT_TYPES = {"e": T.INT_EULER, "rk4": T.INT_RK4, "rk5": T.INT_RK5, "rkf8": T.INT_RKF78}

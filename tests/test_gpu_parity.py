@@ -1,0 +1,174 @@
+"""CUDA library vs the reference's FP64 path: bit-exact parity through the C ABI.
+
+Every comparison here is exact (NaN == NaN): the FP64 kernels keep the reference's
+operation order and build without FMA contraction, so states, accelerations and event
+records must equal the oracle's and the reference's own outputs bit for bit.
+"""
+import numpy as np
+import pytest
+
+import helpers as H
+import pyoracle
+from redgb import bodies, lib, types as T
+from redgb.api import RedError
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_system(disk, thr, **kw):
+    return lib.System(disk, thr, **kw)
+
+
+@pytest.mark.parametrize("name", H.FIXTURES[1:])
+def test_reference_runs_bit_exact(gpulib, name):
+    """Whole reference runs: RKF7(8) with merges and compactions, close-encounter
+    records with orbital elements, ejection / hit-star, RK4 fixed and adaptive."""
+    disk, params, result, events = H.load_fixture(name)
+    s = gpu_system(disk, H.thresholds_of(params))
+    snaps, evs, _ = H.run_fixture(s, params)
+    assert H.compare_result(H.snapshots_as_result(snaps), result) == []
+    assert H.compare_events(evs, events) == []
+
+
+def test_twobody_golden(gpulib):
+    disk, params, result, _ = H.load_fixture("twobody_euler")
+    s = gpu_system(disk, H.thresholds_of(params))
+    snaps, _, n = H.run_fixture(s, params, max_steps=36526)
+    rows = H.snapshots_as_result(snaps)
+    for row, ref in zip(rows[:4], result[:4]):
+        assert H.same(row[9], ref["r"])
+
+
+def _pair(disk, thr, setup):
+    g = gpu_system(disk, thr)
+    o = pyoracle.OracleSystem(disk, thr)
+    for s in (g, o):
+        setup(s)
+    return g, o
+
+
+def _assert_same_state(g, o):
+    rg, vg, pg, mg, tg = g.state(internal=True)
+    ro, vo, po, mo, to = o.state(internal=True)
+    assert tg == to
+    for f in "xyz":
+        assert H.same(rg[f], ro[f]), f
+        assert H.same(vg[f], vo[f]), f
+    assert np.array_equal(mg["id"], mo["id"])
+    for f in ("mass", "radius", "density"):
+        assert H.same(pg[f], po[f])
+
+
+DISKS = {
+    "nsi": lambda: bodies.make_disk(n_pl=300, seed=21),
+    "si": lambda: bodies.make_disk(n_pl=200, pl_type=T.BODY_PROTOPLANET, seed=22, m_range=(1e-8, 1e-6)),
+    "mixed_types": lambda: bodies.make_disk(n_pl=150, seed=23, n_tp=40, embryos=((1e-6, 1.5, 0.05), (2e-6, 2.2, 0.02))),
+}
+INTEGRATORS = [(T.INT_EULER, False, 0.5), (T.INT_RK4, False, 2.0), (T.INT_RK4, True, 2.0), (T.INT_RK5, False, 2.0),
+               (T.INT_RK5, True, 2.0), (T.INT_RKF78, False, 4.0), (T.INT_RKF78, True, 4.0)]
+
+
+@pytest.mark.parametrize("kind", sorted(DISKS))
+@pytest.mark.parametrize("int_type,adaptive,dt", INTEGRATORS)
+def test_steps_bit_exact(gpulib, kind, int_type, adaptive, dt):
+    disk = DISKS[kind]()
+    thr = bodies.thresholds(collision_factor=0.0)
+
+    def setup(s):
+        s.set_integrator(int_type, dt, adaptive, 1e-12, error_check_for_tp=(kind == "mixed_types"))
+
+    g, o = _pair(disk, thr, setup)
+    for _ in range(6):
+        assert g.step() == o.step()
+        _assert_same_state(g, o)
+    assert g.counters()["n_tried_step"] == o.counters()["n_tried_step"]
+    assert g.dt() == o.dt()
+
+
+@pytest.mark.parametrize("n", [2, 3, 33, 1000, 4097])
+def test_acceleration_bit_exact(gpulib, n):
+    """Both FP64 kernels (pair-parallel for the many-source blocks, row-serial for the
+    rest) against the oracle, all-self-interacting and planetesimal disks."""
+    for disk in (bodies.make_disk(n_pl=max(n - 1, 0), pl_type=T.BODY_PROTOPLANET, giants=(), seed=n),
+                 bodies.make_disk(n_pl=max(n - 3, 0), seed=n, n_tp=5)):
+        g = gpu_system(disk, bodies.thresholds())
+        o = pyoracle.OracleSystem(disk, bodies.thresholds())
+        ag, ao = g.calc_accel(), o.calc_accel()
+        for f in "xyzw":
+            assert H.same(ag[f], ao[f]), (n, f)
+
+
+def test_acceleration_full_size_sampled(gpulib):
+    """16384 self-gravitating bodies + star: sampled rows against the oracle."""
+    disk = bodies.config_disk("self_gravitating")
+    g = gpu_system(disk, bodies.thresholds())
+    ag = g.calc_accel()
+    r = g.state(internal=True)[0]
+    rows = np.r_[0:3, 4000:4003, disk.n_total - 3:disk.n_total]
+    for i in rows:
+        ao = pyoracle.grav_accel_rows(disk, r, int(i), int(i) + 1)
+        for f in "xyz":
+            assert H.same(ag[f][i], ao[f][0]), (i, f)
+
+
+def test_inactive_and_zero_mass_bodies(gpulib):
+    disk = bodies.make_disk(n_pl=60, pl_type=T.BODY_PROTOPLANET, seed=5, n_tp=4)
+    disk.md["id"][[5, 17, 40]] *= -1
+    disk.p["mass"][[7, 8]] = 0.0
+    g, o = _pair(disk, bodies.thresholds(), lambda s: s.set_integrator(T.INT_RKF78, 3.0, True, 1e-10))
+    for _ in range(3):
+        g.step()
+        o.step()
+    _assert_same_state(g, o)
+
+
+def test_hill_close_encounters_match_oracle(gpulib):
+    disk = bodies.make_disk(n_pl=120, pl_type=T.BODY_PROTOPLANET, seed=5, m_range=(1e-7, 1e-5),
+                            giants=((9.55e-4, 5.2, 0.05),), a_range=(1.0, 1.3), sigma_e=0.05, sigma_i=0.02)
+    thr = bodies.thresholds(collision_factor=1.0)
+
+    def setup(s):
+        s.set_integrator(T.INT_RKF78, 0.001, True, 1e-10)
+        s.set_event_options(hill_factor=3.0)
+
+    g, o = _pair(disk, thr, setup)
+    g.advance(120.0)
+    o.advance(120.0)
+    eg, eo = g.events(), o.events()
+    assert len(eo) > 0
+    assert [H.event_key(e) for e in eg] == [H.event_key(e) for e in eo]
+    assert H.same(eg["d"], eo["d"]) and H.same(eg["t"], eo["t"])
+    _assert_same_state(g, o)
+
+
+def test_energy_matches_oracle(gpulib):
+    disk = bodies.make_disk(n_pl=500, seed=3, n_tp=10, embryos=((1e-6, 1.5, 0.0),))
+    g = gpu_system(disk, bodies.thresholds())
+    o = pyoracle.OracleSystem(disk, bodies.thresholds())
+    (eg, lg), (eo, lo) = g.energy(), o.energy()
+    assert abs(eg - eo) <= 1e-14 * abs(eo)
+    assert np.allclose(lg, lo, rtol=1e-13, atol=0)
+
+
+def test_event_overflow_is_reported(gpulib):
+    disk, params, _, _ = H.load_fixture("disk_si_rkf78_collide")
+    thr = H.thresholds_of(params)
+    thr[T.THRESHOLD_RADII_ENHANCE_FACTOR] = 5000.0
+    s = gpu_system(disk, thr, event_capacity=4)
+    s.set_integrator(T.INT_RKF78, 0.001, True, 1e-10)
+    with pytest.raises(RedError) as ei:
+        for _ in range(20):
+            s.step()
+    assert ei.value.status == -3
+
+
+def test_bad_arguments_are_rejected(gpulib):
+    disk = bodies.make_disk(n_pl=4, seed=1)
+    s = gpu_system(disk, bodies.thresholds())
+    with pytest.raises(RedError) as ei:
+        s.step()  # no integrator yet
+    assert ei.value.status == -5
+    with pytest.raises(RedError):
+        s.set_integrator(99, 1.0)
+    with pytest.raises(RedError):
+        s.set_event_options(hill_factor=-1.0)
