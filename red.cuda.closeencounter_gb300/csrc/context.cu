@@ -110,8 +110,29 @@ struct rg_ctx {
     std::vector<int> ev_kind;  // per recorded pair
     size_t ev_used = 0;
     // tiles for the current body counts
-    std::vector<Tile> tiles_pp, tiles_hp, tiles_mx, tiles_rs;  // FP64 pair-parallel, heavy rows, mixed, row-serial
-    std::vector<int> heavy_mx;
+    // launch plan of one force evaluation, per gravity mode (build_plan)
+    struct Group {
+        int kind;       // GROUP_*
+        size_t off;     // first tile in d_tiles
+        int n;          // tiles
+        int row_base;   // few-sink groups: first row in the terms buffer
+        int rows;       // few-sink groups: rows
+    };
+    std::vector<Group> plan[2];
+    std::vector<Tile> tiles;       // all groups' tiles, uploaded to d_tiles
+    std::vector<int> heavy_mx;     // per tile (mixed groups): end of the heavy sources
+    std::vector<int> few_row0, few_nsrc;  // per tile (few-sink groups)
+    std::vector<int> row_sink, row_nsrc;  // per terms-buffer row
+    int few_rows = 0;
+    long long few_pitch = 0;
+    double* d_terms = nullptr;
+    size_t terms_cap = 0;
+    double* d_partial = nullptr;  // mixed kernel: per source chunk partial sums
+    size_t partial_cap = 0;
+    int n_sm = 152;
+    int* d_row_sink = nullptr;
+    int* d_row_nsrc = nullptr;
+    int rows_cap = 0;
     int64_t pairs_per_eval = 0;
     bool tiles_dirty = true;
 
@@ -154,6 +175,10 @@ void free_all(rg_ctx* c)
     cudaFree(c->d_tiles);
     cudaFree(c->d_heavy);
     cudaFree(c->d_split);
+    cudaFree(c->d_terms);
+    cudaFree(c->d_partial);
+    cudaFree(c->d_row_sink);
+    cudaFree(c->d_row_nsrc);
     cudaFree(c->d_ev);
     cudaFree(c->d_ev_count);
     cudaFree(c->d_hill);
@@ -265,38 +290,74 @@ int set_param_dev(rg_ctx* c, int i)
     return RG_OK;
 }
 
-// --------------------------------------------------------------------- tiles
+// --------------------------------------------------------------------- launch plan
+enum { GROUP_PAIRPAR = 0, GROUP_ROWSEQ = 1, GROUP_FEW_SERIAL = 2, GROUP_FEW_TREE = 3, GROUP_MIXED = 4 };
+constexpr int FEW_BLOCK_SINKS = 32;  // blocks with at most this many sinks use the few-sink path
+
 // CTA tiles of the interaction matrix (number_of_bodies::get_bound_SI/NSI/NI,
-// number_of_bodies.cpp:196-258, barycentric frame).
+// number_of_bodies.cpp:196-258, barycentric frame) for both gravity modes.
 void build_tiles(rg_ctx* c)
 {
-    c->tiles_pp.clear();
-    c->tiles_hp.clear();
-    c->tiles_mx.clear();
-    c->tiles_rs.clear();
+    c->tiles.clear();
     c->heavy_mx.clear();
+    c->few_row0.clear();
+    c->few_nsrc.clear();
+    c->row_sink.clear();
+    c->row_nsrc.clear();
+    c->few_rows = 0;
+    c->few_pitch = 0;
     const int nsi = c->n_si(), nm = c->n_massive(), nt = c->n_total();
     // heavy bodies of the mixed kernel: the leading stars, giant and rocky planets.  As
-    // sources their terms are exact FP64; as sinks (few rows) they use the FP64 kernel.
+    // sources their terms are exact FP64; as sinks (few rows) they use the FP64 path.
     const int n_heavy = std::min(nsi, c->cnt[0] + c->cnt[1] + c->cnt[2]);
     struct Blk {
         int s0, s1, src1, block;
     } blks[3] = {{0, nsi, nm, 0}, {nsi, nm, nsi, 1}, {nm, nt, nm, 2}};
     c->pairs_per_eval = (int64_t)nsi * (nm > 0 ? nm - 1 : 0) + (int64_t)(nm - nsi) * nsi + (int64_t)(nt - nm) * nm;
-    const int S = c->pairpar_S;
+
+    auto add_group = [&](int mode, int kind, int s0, int s1, int src1, int block, int step) {
+        if (s1 <= s0) return;
+        rg_ctx::Group gr{kind, c->tiles.size(), 0, c->few_rows, 0};
+        for (int s = s0; s < s1; s += step) {
+            c->tiles.push_back(Tile{s, std::min(s + step, s1), 0, src1, 0, 0, block, 0});
+            c->heavy_mx.push_back(kind == GROUP_MIXED ? std::min(n_heavy, src1) : 0);
+            if (kind == GROUP_FEW_SERIAL || kind == GROUP_FEW_TREE) {
+                c->few_row0.push_back(c->few_rows);
+                c->few_nsrc.push_back(src1);
+                for (int i = s; i < std::min(s + step, s1); i++) {
+                    c->row_sink.push_back(i);
+                    c->row_nsrc.push_back(src1);
+                    c->few_rows++;
+                    gr.rows++;
+                }
+                c->few_pitch = std::max<long long>(c->few_pitch, src1);
+            } else {
+                c->few_row0.push_back(0);
+                c->few_nsrc.push_back(0);
+            }
+            gr.n++;
+        }
+        c->plan[mode].push_back(gr);
+    };
+    c->plan[0].clear();
+    c->plan[1].clear();
     for (const auto& b : blks) {
         if (b.s1 <= b.s0) continue;
-        if (b.src1 <= c->rowseq_max_src) {
-            for (int s = b.s0; s < b.s1; s += 128) c->tiles_rs.push_back(Tile{s, std::min(s + 128, b.s1), 0, b.src1, 0, 0, b.block, 0});
+        const int ns = b.s1 - b.s0;
+        if (b.src1 <= c->rowseq_max_src) {  // few sources: thread per sink, both modes
+            add_group(0, GROUP_ROWSEQ, b.s0, b.s1, b.src1, b.block, 128);
+            c->plan[1].push_back(c->plan[0].back());
             continue;
         }
-        for (int s = b.s0; s < b.s1; s += S) c->tiles_pp.push_back(Tile{s, std::min(s + S, b.s1), 0, b.src1, 0, 0, b.block, 0});
-        const int light0 = b.block == 0 ? std::max(b.s0, n_heavy) : b.s0;
-        for (int s = b.s0; s < light0; s += S) c->tiles_hp.push_back(Tile{s, std::min(s + S, light0), 0, b.src1, 0, 0, b.block, 0});
-        for (int s = light0; s < b.s1; s += MIXED_SINKS_PER_TILE) {
-            c->tiles_mx.push_back(Tile{s, std::min(s + MIXED_SINKS_PER_TILE, b.s1), 0, b.src1, 0, 0, b.block, 0});
-            c->heavy_mx.push_back(std::min(n_heavy, b.src1));
+        if (ns <= FEW_BLOCK_SINKS) {  // few sinks, many sources: exact serial row sums, both modes
+            add_group(0, GROUP_FEW_SERIAL, b.s0, b.s1, b.src1, b.block, FEW_SINKS_MAX);
+            c->plan[1].push_back(c->plan[0].back());
+            continue;
         }
+        add_group(0, GROUP_PAIRPAR, b.s0, b.s1, b.src1, b.block, c->pairpar_S);
+        const int light0 = b.block == 0 ? std::max(b.s0, std::min(n_heavy, b.s1)) : b.s0;
+        add_group(1, GROUP_FEW_TREE, b.s0, light0, b.src1, b.block, FEW_SINKS_MAX);
+        add_group(1, GROUP_MIXED, light0, b.s1, b.src1, b.block, MIXED_SINKS_PER_TILE);
     }
     c->tiles_dirty = true;
 }
@@ -304,7 +365,7 @@ void build_tiles(rg_ctx* c)
 int sync_tiles(rg_ctx* c)
 {
     if (!c->tiles_dirty) return RG_OK;
-    const int n = (int)(c->tiles_pp.size() + c->tiles_hp.size() + c->tiles_mx.size() + c->tiles_rs.size());
+    const int n = (int)c->tiles.size();
     if (n > c->tiles_cap) {
         cudaFree(c->d_tiles);
         cudaFree(c->d_heavy);
@@ -315,15 +376,33 @@ int sync_tiles(rg_ctx* c)
         if (rc) return rc;
         c->tiles_cap = n;
     }
-    std::vector<Tile> all(c->tiles_pp);  // device order: pp | hp | mx | rs
-    all.insert(all.end(), c->tiles_hp.begin(), c->tiles_hp.end());
-    all.insert(all.end(), c->tiles_mx.begin(), c->tiles_mx.end());
-    all.insert(all.end(), c->tiles_rs.begin(), c->tiles_rs.end());
-    if (n > 0)
-        RG_CUDA_CHECK(cudaMemcpyAsync(c->d_tiles, all.data(), n * sizeof(Tile), cudaMemcpyHostToDevice, c->st));
-    if (!c->heavy_mx.empty())
-        RG_CUDA_CHECK(cudaMemcpyAsync(c->d_heavy, c->heavy_mx.data(), c->heavy_mx.size() * sizeof(int),
+    const size_t need = (size_t)3 * c->few_rows * (size_t)c->few_pitch;
+    if (need > c->terms_cap) {
+        cudaFree(c->d_terms);
+        c->d_terms = nullptr;
+        int rc = dalloc(&c->d_terms, need);
+        if (rc) return rc;
+        c->terms_cap = need;
+    }
+    if (c->few_rows > c->rows_cap) {
+        cudaFree(c->d_row_sink);
+        cudaFree(c->d_row_nsrc);
+        c->d_row_sink = c->d_row_nsrc = nullptr;
+        int rc = dalloc(&c->d_row_sink, (size_t)c->few_rows);
+        if (!rc) rc = dalloc(&c->d_row_nsrc, (size_t)c->few_rows);
+        if (rc) return rc;
+        c->rows_cap = c->few_rows;
+    }
+    if (n > 0) {
+        RG_CUDA_CHECK(cudaMemcpyAsync(c->d_tiles, c->tiles.data(), n * sizeof(Tile), cudaMemcpyHostToDevice, c->st));
+        RG_CUDA_CHECK(cudaMemcpyAsync(c->d_heavy, c->heavy_mx.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    }
+    if (c->few_rows > 0) {
+        RG_CUDA_CHECK(cudaMemcpyAsync(c->d_row_sink, c->row_sink.data(), c->few_rows * sizeof(int),
                                       cudaMemcpyHostToDevice, c->st));
+        RG_CUDA_CHECK(cudaMemcpyAsync(c->d_row_nsrc, c->row_nsrc.data(), c->few_rows * sizeof(int),
+                                      cudaMemcpyHostToDevice, c->st));
+    }
     RG_CUDA_CHECK(cudaStreamSynchronize(c->st));
     c->tiles_dirty = false;
     return RG_OK;
@@ -368,31 +447,56 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
     c->n_gravity_evals++;
     c->n_pairs += c->pairs_per_eval;
     const long prof = prof_begin(c, 0);
-    const size_t off_hp = c->tiles_pp.size(), off_mx = off_hp + c->tiles_hp.size(),
-                 off_rs = off_mx + c->tiles_mx.size();
-    if (c->gravity_mode == RG_GRAVITY_MIXED) {
-        g.tiles = c->d_tiles + off_hp;
-        g.n_tiles = (int)c->tiles_hp.size();
-        rc = launch_grav_fp64_pairpar(g, c->pairpar_S, c->st);
-        c->n_kernels += g.n_tiles > 0;
-        g.tiles = c->d_tiles + off_mx;
-        g.n_tiles = (int)c->tiles_mx.size();
-        if (!rc && g.n_tiles > 0) {
-            rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->n_total(), (SplitPos*)c->d_split, c->st);
-            if (!rc) rc = launch_grav_mixed_tiles(g, c->d_split, c->d_heavy, c->near_ratio, c->st);
-            c->n_kernels += 2;
+    bool split_done = false;
+    for (const auto& gr : c->plan[c->gravity_mode == RG_GRAVITY_MIXED ? 1 : 0]) {
+        g.tiles = c->d_tiles + gr.off;
+        g.n_tiles = gr.n;
+        switch (gr.kind) {
+        case GROUP_PAIRPAR:
+            rc = launch_grav_fp64_pairpar(g, c->pairpar_S, c->st);
+            c->n_kernels++;
+            break;
+        case GROUP_ROWSEQ:
+            rc = launch_grav_fp64_rowseq(g, c->st);
+            c->n_kernels++;
+            break;
+        case GROUP_FEW_SERIAL:
+        case GROUP_FEW_TREE:
+            rc = launch_grav_fp64_few(g, c->few_row0.data() + gr.off, c->few_nsrc.data() + gr.off, c->d_terms,
+                                      c->few_rows, c->few_pitch, c->d_row_sink, c->d_row_nsrc, gr.row_base, gr.rows,
+                                      gr.kind == GROUP_FEW_SERIAL, c->st);
+            c->n_kernels += gr.n + 1;
+            break;
+        case GROUP_MIXED:
+            if (!split_done) {
+                rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, c->n_total(), (SplitPos*)c->d_split, c->st);
+                split_done = true;
+                c->n_kernels++;
+            }
+            if (!rc) {
+                // split the sources over grid.y so that about 4 CTAs per SM are in flight
+                const int src = c->tiles[gr.off].src_end - c->tiles[gr.off].src_begin;
+                int chunks = std::max(1, std::min((4 * c->n_sm + gr.n - 1) / gr.n, src / (4 * MIXED_SOURCE_TILE)));
+                const int chunk = ((src + chunks - 1) / chunks + MIXED_SOURCE_TILE - 1) / MIXED_SOURCE_TILE *
+                                  MIXED_SOURCE_TILE;
+                chunks = (src + chunk - 1) / chunk;
+                if (chunks > 1 && (size_t)chunks * 3 * c->cap > c->partial_cap) {
+                    cudaFree(c->d_partial);
+                    c->d_partial = nullptr;
+                    c->partial_cap = 0;
+                    rc = dalloc(&c->d_partial, (size_t)chunks * 3 * c->cap);
+                    if (!rc) c->partial_cap = (size_t)chunks * 3 * c->cap;
+                }
+                if (!rc)
+                    rc = launch_grav_mixed_tiles(g, c->d_split, c->d_heavy + gr.off, c->near_ratio, chunks, chunk,
+                                                 c->d_partial, c->cap, c->st);
+                c->n_kernels += chunks > 1;
+            }
+            c->n_kernels++;
+            break;
         }
-    } else {
-        g.tiles = c->d_tiles;
-        g.n_tiles = (int)c->tiles_pp.size();
-        rc = launch_grav_fp64_pairpar(g, c->pairpar_S, c->st);
-        c->n_kernels += g.n_tiles > 0;
+        if (rc) return rc;
     }
-    if (rc) return rc;
-    g.tiles = c->d_tiles + off_rs;
-    g.n_tiles = (int)c->tiles_rs.size();
-    rc = launch_grav_fp64_rowseq(g, c->st);
-    c->n_kernels += g.n_tiles > 0;
     prof_end(c, prof);
     return rc;
 }
@@ -1087,6 +1191,7 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
     const int nt = (int)tot;
     c->cap = nt;
     cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->n_sm, cudaDevAttrMultiProcessorCount, c->device);
     c->ev_cap = (unsigned int)(event_capacity > 0 ? event_capacity : std::max(nt, 1024));
     int rc = RG_OK;
     auto chk = [&](int x) {

@@ -199,6 +199,114 @@ __global__ void star_distance(const double* __restrict__ x, const double* __rest
 }
 
 // ---------------------------------------------------------------------------------------
+// Few-sink path: blocks with a handful of sinks and many sources (the star and giants
+// of a planetesimal disk).  Kernel A spreads the pair terms of up to FEW_MAX sinks over
+// the whole GPU, one thread per source, into a terms buffer (3 x rows x n_src); kernel B
+// adds each row in ascending source order -- one thread per (sink, component), which is
+// the reference's serial sum -- or, for the mixed-precision kernel's heavy rows, as a
+// compensated tree reduction.
+constexpr int FEW_MAX = 8;
+
+struct FewArgs {
+    GravArgs g;
+    int row0;        // first row of this tile in the terms buffer
+    double* terms;   // 3 x rows x pitch
+    int rows;        // rows of the buffer
+    long long pitch; // >= largest source count
+};
+
+__global__ void __launch_bounds__(256) grav_fp64_few_terms(FewArgs a)
+{
+    const GravArgs& g = a.g;
+    const Tile tile = g.tiles[blockIdx.y];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;  // source offset within the tile
+    const int j = tile.src_begin + q;
+    __shared__ double sx[FEW_MAX], sy[FEW_MAX], sz[FEW_MAX], sR[FEW_MAX], sm[FEW_MAX], srho[FEW_MAX];
+    __shared__ int sact[FEW_MAX];
+    const int ns = tile.sink_end - tile.sink_begin;
+    if (threadIdx.x < ns) {
+        const int i = tile.sink_begin + threadIdx.x;
+        sx[threadIdx.x] = g.px[i]; sy[threadIdx.x] = g.py[i]; sz[threadIdx.x] = g.pz[i];
+        sR[threadIdx.x] = g.radius[i]; sm[threadIdx.x] = g.mass[i];
+        srho[threadIdx.x] = g.hill ? g.rho[i] : 0.0;
+        sact[threadIdx.x] = 0 < g.id[i];
+    }
+    __syncthreads();
+    if (j >= tile.src_end) return;
+    const double xj = g.px[j], yj = g.py[j], zj = g.pz[j], mj = g.mass[j], Rj = g.radius[j];
+    const double rhoj = g.hill ? g.rho[j] : 0.0;
+    const bool src_ok = 0 <= g.id[j];
+    const long long plane = (long long)a.rows * a.pitch;
+    for (int s = 0; s < ns; s++) {
+        const int i = tile.sink_begin + s;
+        PairOut o{0.0, 0.0, 0.0};
+        if (sact[s] && src_ok && j != i)
+            pair_term(g, tile, i, j, sx[s], sy[s], sz[s], sR[s], sm[s], srho[s], xj, yj, zj, mj, Rj, rhoj, o);
+        const long long e = (long long)(a.row0 + s) * a.pitch + q;
+        a.terms[e] = o.tx;
+        a.terms[plane + e] = o.ty;
+        a.terms[2 * plane + e] = o.tz;
+    }
+}
+
+struct FewSumArgs {
+    const double* terms;
+    int rows;         // rows of the whole buffer
+    int row0, nrows;  // the rows this launch sums
+    long long pitch;
+    const int* row_sink;   // sink index of each row
+    const int* row_nsrc;   // sources of each row
+    double* ax;
+    double* ay;
+    double* az;
+};
+
+// exact: one thread per (row, component), ascending source order
+__global__ void few_sum_serial(FewSumArgs a)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * a.nrows) return;
+    const int comp = t / a.nrows, row = a.row0 + t % a.nrows;
+    const double* T = a.terms + ((long long)comp * a.rows + row) * a.pitch;
+    const int n = a.row_nsrc[row];
+    double acc = 0.0;
+    int q = 0;
+    for (; q + 8 <= n; q += 8) {
+        const double t0 = T[q], t1 = T[q + 1], t2 = T[q + 2], t3 = T[q + 3];
+        const double t4 = T[q + 4], t5 = T[q + 5], t6 = T[q + 6], t7 = T[q + 7];
+        acc = acc + t0; acc = acc + t1; acc = acc + t2; acc = acc + t3;
+        acc = acc + t4; acc = acc + t5; acc = acc + t6; acc = acc + t7;
+    }
+    for (; q < n; q++) acc = acc + T[q];
+    double* out = comp == 0 ? a.ax : (comp == 1 ? a.ay : a.az);
+    out[a.row_sink[row]] = acc;
+}
+
+// mixed-precision heavy rows: one CTA per (row, component), compensated tree reduction
+__global__ void __launch_bounds__(256) few_sum_tree(FewSumArgs a)
+{
+    const int comp = blockIdx.x / a.nrows, row = a.row0 + blockIdx.x % a.nrows;
+    const double* T = a.terms + ((long long)comp * a.rows + row) * a.pitch;
+    const int n = a.row_nsrc[row];
+    double s = 0.0, c = 0.0;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const double x = T[q];
+        const double t = s + x;
+        c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
+        s = t;
+    }
+    s += c;
+    __shared__ double red[256];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) (comp == 0 ? a.ax : (comp == 1 ? a.ay : a.az))[a.row_sink[row]] = red[0];
+}
+
+// ---------------------------------------------------------------------------------------
 // Host launchers
 int launch_grav_fp64_pairpar(const GravArgs& g, int S, cudaStream_t st)
 {
@@ -217,6 +325,30 @@ int launch_grav_fp64_rowseq(const GravArgs& g, cudaStream_t st)
 {
     if (g.n_tiles <= 0) return 0;
     grav_fp64_rowseq<<<g.n_tiles, 128, 0, st>>>(g);
+    RG_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+// Few-sink tiles (at most FEW_MAX sinks each) -> terms -> row sums.  `tiles` holds
+// n_tiles tiles, rows are numbered tile by tile; host arrays row_sink/row_nsrc are on the
+// device already (dev_row_sink, dev_row_nsrc).
+int launch_grav_fp64_few(const GravArgs& g, const int* tile_row0, const int* tile_nsrc, double* terms, int rows,
+                         long long pitch, const int* dev_row_sink, const int* dev_row_nsrc, int group_row0,
+                         int group_rows, bool serial, cudaStream_t st)
+{
+    if (g.n_tiles <= 0 || rows <= 0 || group_rows <= 0) return 0;
+    for (int k = 0; k < g.n_tiles; k++) {
+        if (tile_nsrc[k] <= 0) continue;
+        FewArgs a{g, tile_row0[k], terms, rows, pitch};
+        a.g.tiles = g.tiles + k;
+        grav_fp64_few_terms<<<(tile_nsrc[k] + 255) / 256, 256, 0, st>>>(a);
+        RG_CUDA_CHECK(cudaGetLastError());
+    }
+    FewSumArgs b{terms, rows, group_row0, group_rows, pitch, dev_row_sink, dev_row_nsrc, g.ax, g.ay, g.az};
+    if (serial)
+        few_sum_serial<<<(3 * group_rows + 127) / 128, 128, 0, st>>>(b);
+    else
+        few_sum_tree<<<3 * group_rows, 256, 0, st>>>(b);
     RG_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

@@ -35,16 +35,25 @@ struct SplitPos {
     float4 zm;  // z_hi, z_lo, m, (unused)
 };
 
+// inactive bodies (id < 0, pp_disk.cu:242) get mass 0 here, so the pair loop needs no
+// per-pair activity test: their terms vanish
 __global__ void split_positions_kernel(const double* __restrict__ x, const double* __restrict__ y,
-                                       const double* __restrict__ z, const double* __restrict__ m, int n,
-                                       SplitPos* __restrict__ out)
+                                       const double* __restrict__ z, const double* __restrict__ m,
+                                       const int* __restrict__ id, int n, SplitPos* __restrict__ out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double xd = x[i], yd = y[i], zd = z[i];
     const float xh = (float)xd, yh = (float)yd, zh = (float)zd;
     out[i].xy = make_float4(xh, (float)(xd - (double)xh), yh, (float)(yd - (double)yh));
-    out[i].zm = make_float4(zh, (float)(zd - (double)zh), (float)m[i], 0.0f);
+    out[i].zm = make_float4(zh, (float)(zd - (double)zh), id[i] < 0 ? 0.0f : (float)m[i], 0.0f);
+}
+
+__device__ __forceinline__ float rsqrt_approx(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 
 // compensated accumulation: s + c tracks the exact sum of the added terms to ~2^-46
@@ -73,14 +82,17 @@ struct MixedArgs {
     const SplitPos* sp;
     const int* heavy_end;  // per tile: sources [src_begin, heavy_end) are heavy
     float near_ratio;
+    int chunk;             // sources per grid.y chunk (multiple of MX_T)
+    double* partial;       // n_chunks x 3 x n_part doubles, or nullptr when grid.y == 1
+    int n_part;            // row length of `partial`
 };
 
 constexpr int MX_WARPS = 8;
-constexpr int MX_R = 2;         // sinks per lane
-constexpr int MX_S = 32 * MX_R; // sinks per CTA
+constexpr int MX_R = 4;          // sinks per lane
+constexpr int MX_S = 32 * MX_R;  // sinks per CTA
 static_assert(MX_S == MIXED_SINKS_PER_TILE, "tile size");
 static_assert(sizeof(SplitPos) == SPLIT_POS_BYTES, "split size");
-constexpr int MX_T = 256;       // sources per shared-memory tile
+constexpr int MX_T = 256;        // sources per shared-memory tile
 
 __device__ __forceinline__ void exact_event_tests(const GravArgs& g, const Tile& tile, int i, int j, double xi,
                                                   double yi, double zi, double Ri, double mi, double rhoi)
@@ -125,195 +137,281 @@ __device__ __forceinline__ void exact_event_tests(const GravArgs& g, const Tile&
     }
 }
 
-__global__ void __launch_bounds__(256) grav_mixed_kernel(MixedArgs a)
+struct SinkD {
+    double x, y, z, R, m, rho;
+};
+
+// FP64 displacement, FP32 rsqrt seed, one FP64 Newton step: a near pair's term
+__device__ __forceinline__ void near_term(const GravArgs& g, const SinkD& sd, int j, double& hx, double& hy,
+                                          double& hz)
+{
+    const double ddx = g.px[j] - sd.x, ddy = g.py[j] - sd.y, ddz = g.pz[j] - sd.z;
+    const double dr2 = ddx * ddx + ddy * ddy + ddz * ddz;
+    const double y0 = (double)rsqrtf((float)dr2);
+    const double y1 = y0 * (1.5 - 0.5 * dr2 * y0 * y0);
+    const double w = g.mass[j] * (y1 * y1 * y1);
+    hx += w * ddx;
+    hy += w * ddy;
+    hz += w * ddz;
+}
+
+constexpr int MX_GROUP = 8;  // sources summed in plain FP32 before each two-sum
+
+// One warp-slice of a source tile for MX_R sinks per lane.  DIAG: the slice may hold the
+// sinks themselves (self pairs are skipped); SCREEN: event screens are on.
+template <bool DIAG, bool SCREEN>
+__device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile, int j0, int q_begin, int q_end,
+                                            const float4* s_xy, const float4* s_zm, const float* s_R,
+                                            const float* s_rho, const SinkD* s_sink, const int* si,
+                                            const float* xh, const float* xl, const float* yh, const float* yl,
+                                            const float* zh, const float* zl, const float* near_lim, Acc2* ax,
+                                            Acc2* ay, Acc2* az, unsigned* near_mask, int lane)
+{
+    const GravArgs& g = a.g;
+    float px[MX_R], py[MX_R], pz[MX_R];
+#pragma unroll
+    for (int r = 0; r < MX_R; r++) {
+        px[r] = py[r] = pz[r] = 0.0f;
+        near_mask[r] = 0u;
+    }
+    for (int q = q_begin; q < q_end; q++) {
+        const float4 pxy = s_xy[q];
+        const float4 pzm = s_zm[q];
+        const float mj = pzm.z;
+        const int j = j0 + q;
+#pragma unroll
+        for (int r = 0; r < MX_R; r++) {
+            const float dx = (pxy.x - xh[r]) + (pxy.y - xl[r]);
+            const float dy = (pxy.z - yh[r]) + (pxy.w - yl[r]);
+            const float dz = (pzm.x - zh[r]) + (pzm.y - zl[r]);
+            // clamp: a merged body parked at 1e20 AU (pp_disk.cu:1184) overflows r^2 in FP32,
+            // and inf * 0 in the Newton step would poison the sum although its mass is 0
+            const float r2 = fminf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), 1.0e30f);
+            bool near = mj > near_lim[r] * r2;
+            if (DIAG) near = near && j != si[r];
+            const float y0 = rsqrt_approx(r2);
+            const float hr2 = 0.5f * r2;
+            const float y = y0 * fmaf(-hr2, y0 * y0, 1.5f);
+            float w = mj * (y * y * y);
+            if (DIAG) w = (j == si[r]) ? 0.0f : w;
+            w = near ? 0.0f : w;
+            px[r] = fmaf(w, dx, px[r]);
+            py[r] = fmaf(w, dy, py[r]);
+            pz[r] = fmaf(w, dz, pz[r]);
+            near_mask[r] |= (unsigned)near << (q - q_begin);
+            if (SCREEN) {
+                const int li = si[r] - tile.base, lj = j - tile.base;
+                if (li > 0 && li > lj && (!DIAG || j != si[r]) && mj >= 0.0f) {
+                    const SinkD& sd = s_sink[lane + 32 * r];
+                    const float margin = 1.001f;
+                    bool cand = false;
+                    if (g.record) {
+                        const float lim = (float)g.f_rad * ((float)sd.R + s_R[q]) * margin;
+                        cand = r2 < lim * lim;
+                    }
+                    if (g.hill && tile.block != 2 && lj > 0) {
+                        const float h = 0.5f * ((float)sd.rho + s_rho[q]);
+                        const float d3 = r2 * sqrtf(r2);
+                        const float inv3M = (float)(1.0 / (3.0 * g.mass[tile.base]));
+                        cand = cand || (d3 < (float)g.hill_f3 * ((float)sd.m + mj) * inv3M * (h * h * h) *
+                                                 (margin * margin * margin));
+                    }
+                    if (cand && 0 <= g.id[j])
+                        exact_event_tests(g, tile, si[r], j, sd.x, sd.y, sd.z, sd.R, sd.m, sd.rho);
+                }
+            }
+        }
+        if (((q - q_begin) & (MX_GROUP - 1)) == MX_GROUP - 1) {
+#pragma unroll
+            for (int r = 0; r < MX_R; r++) {
+                two_sum_add(ax[r], px[r]);
+                two_sum_add(ay[r], py[r]);
+                two_sum_add(az[r], pz[r]);
+                px[r] = py[r] = pz[r] = 0.0f;
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < MX_R; r++) {
+        two_sum_add(ax[r], px[r]);
+        two_sum_add(ay[r], py[r]);
+        two_sum_add(az[r], pz[r]);
+    }
+}
+
+template <bool SCREEN>
+__global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
 {
     const GravArgs& g = a.g;
     __shared__ float4 s_xy[MX_T];
     __shared__ float4 s_zm[MX_T];
-    __shared__ float s_R[MX_T];
-    __shared__ float s_rho[MX_T];
-    __shared__ int s_id[MX_T];
-    __shared__ float s_red[MX_WARPS][6][MX_S];  // per-warp (s, c) x 3 components
-    __shared__ double s_redh[MX_WARPS][3][MX_S];
+    __shared__ float s_R[SCREEN ? MX_T : 1];
+    __shared__ float s_rho[SCREEN ? MX_T : 1];
+    __shared__ SinkD s_sink[MX_S];
+    __shared__ double s_h[MX_WARPS][3][MX_S];  // per-warp FP64 sums: heavy sources and near pairs
 
     const Tile tile = g.tiles[blockIdx.x];
     const int heavy_end = a.heavy_end[blockIdx.x];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int src_lo = tile.src_begin + blockIdx.y * a.chunk;
+    const int src_hi = min(tile.src_end, src_lo + a.chunk);
+
+    for (int s = threadIdx.x; s < MX_S; s += blockDim.x) {
+        const int i = tile.sink_begin + s;
+        SinkD sd{0, 0, 0, 0, 0, 0};
+        if (i < tile.sink_end) {
+            sd.x = g.px[i]; sd.y = g.py[i]; sd.z = g.pz[i];
+            sd.R = g.radius[i]; sd.m = g.mass[i];
+            sd.rho = g.hill ? g.rho[i] : 0.0;
+        }
+        s_sink[s] = sd;
+    }
+    for (int k = threadIdx.x; k < MX_WARPS * 3 * MX_S; k += blockDim.x) (&s_h[0][0][0])[k] = 0.0;
+    __syncthreads();
 
     int si[MX_R];
-    bool act[MX_R];
-    double xi[MX_R], yi[MX_R], zi[MX_R], Ri[MX_R], mi[MX_R], rhoi[MX_R];
-    float xh[MX_R], xl[MX_R], yh[MX_R], yl[MX_R], zh[MX_R], zl[MX_R];
-    float Rf[MX_R], rhof[MX_R];
+    float xh[MX_R], xl[MX_R], yh[MX_R], yl[MX_R], zh[MX_R], zl[MX_R], near_lim[MX_R];
     Acc2 ax[MX_R], ay[MX_R], az[MX_R];
-    double hx[MX_R], hy[MX_R], hz[MX_R];
-    float heavy_pull[MX_R];
 #pragma unroll
     for (int r = 0; r < MX_R; r++) {
-        const int i = tile.sink_begin + lane + 32 * r;
+        const int s = lane + 32 * r;
+        const int i = tile.sink_begin + s;
         si[r] = i;
-        act[r] = false;
-        xi[r] = yi[r] = zi[r] = Ri[r] = mi[r] = rhoi[r] = 0.0;
         xh[r] = xl[r] = yh[r] = yl[r] = zh[r] = zl[r] = 0.0f;
-        Rf[r] = rhof[r] = 0.0f;
+        float pull = 0.0f;
         if (i < tile.sink_end) {
-            act[r] = 0 < g.id[i];
-            xi[r] = g.px[i]; yi[r] = g.py[i]; zi[r] = g.pz[i];
-            Ri[r] = g.radius[i]; mi[r] = g.mass[i];
-            rhoi[r] = g.hill ? g.rho[i] : 0.0;
             const SplitPos sp = a.sp[i];
             xh[r] = sp.xy.x; xl[r] = sp.xy.y; yh[r] = sp.xy.z; yl[r] = sp.xy.w;
             zh[r] = sp.zm.x; zl[r] = sp.zm.y;
-            Rf[r] = (float)Ri[r];
-            rhof[r] = (float)rhoi[r];
+            if (tile.src_begin < heavy_end) {  // m / r^2 of the first heavy source: the near-pair scale
+                const SinkD sd = s_sink[s];
+                const int j = tile.src_begin;
+                const double dx = g.px[j] - sd.x, dy = g.py[j] - sd.y, dz = g.pz[j] - sd.z;
+                pull = (float)(g.mass[j] / (dx * dx + dy * dy + dz * dz));
+            }
         }
+        // a pair is near when m_j > near_lim * r^2; without a heavy source there is no scale
+        near_lim[r] = pull > 0.0f ? a.near_ratio * pull : 3.0e38f;
         ax[r] = ay[r] = az[r] = Acc2{0.0f, 0.0f};
-        hx[r] = hy[r] = hz[r] = 0.0;
-        heavy_pull[r] = 0.0f;
     }
 
-    // heavy sources: exact FP64 terms, split over the warps
-    for (int j = tile.src_begin + warp; j < heavy_end; j += MX_WARPS) {
-        const double xj = g.px[j], yj = g.py[j], zj = g.pz[j], mj = g.mass[j];
-        const bool ok = 0 <= g.id[j];
+    // heavy sources (first chunk only): exact FP64 terms, split over the warps
+    if (blockIdx.y == 0) {
+        for (int j = tile.src_begin + warp; j < heavy_end; j += MX_WARPS) {
+            const double xj = g.px[j], yj = g.py[j], zj = g.pz[j], mj = g.mass[j];
+            if (0 > g.id[j]) continue;
 #pragma unroll
-        for (int r = 0; r < MX_R; r++) {
-            if (!act[r] || !ok || j == si[r]) continue;
-            const double dx = xj - xi[r], dy = yj - yi[r], dz = zj - zi[r];
-            const double r2 = dx * dx + dy * dy + dz * dz;
-            const double d = sqrt(r2);
-            const double w = mj / (d * r2);
-            hx[r] += w * dx;
-            hy[r] += w * dy;
-            hz[r] += w * dz;
-            heavy_pull[r] = fmaxf(heavy_pull[r], (float)(mj / r2));
-            const int li = si[r] - tile.base, lj = j - tile.base;
-            if ((g.record && li > 0 && li > lj && d < 1.001 * g.f_rad * (Ri[r] + g.radius[j])) ||
-                (g.hill && tile.block != 2 && li > 0 && li > lj && lj > 0))
-                exact_event_tests(g, tile, si[r], j, xi[r], yi[r], zi[r], Ri[r], mi[r], rhoi[r]);
+            for (int r = 0; r < MX_R; r++) {
+                const int s = lane + 32 * r;
+                if (si[r] >= tile.sink_end || j == si[r]) continue;
+                const SinkD sd = s_sink[s];
+                const double dx = xj - sd.x, dy = yj - sd.y, dz = zj - sd.z;
+                const double r2 = dx * dx + dy * dy + dz * dz;
+                const double d = sqrt(r2);
+                const double w = mj / (d * r2);
+                s_h[warp][0][s] += w * dx;
+                s_h[warp][1][s] += w * dy;
+                s_h[warp][2][s] += w * dz;
+                const int li = si[r] - tile.base, lj = j - tile.base;
+                if ((g.record && li > 0 && li > lj && d < 1.001 * g.f_rad * (sd.R + g.radius[j])) ||
+                    (g.hill && tile.block != 2 && li > 0 && li > lj && lj > 0))
+                    exact_event_tests(g, tile, si[r], j, sd.x, sd.y, sd.z, sd.R, sd.m, sd.rho);
+            }
         }
     }
-    // the near-pair criterion needs the heavy pull of the whole sink: max over warps
-    __shared__ float s_pull[MX_WARPS][MX_S];
-#pragma unroll
-    for (int r = 0; r < MX_R; r++) s_pull[warp][lane + 32 * r] = heavy_pull[r];
-    __syncthreads();
-    float near_lim[MX_R];
-#pragma unroll
-    for (int r = 0; r < MX_R; r++) {
-        float p = 0.0f;
-        for (int w = 0; w < MX_WARPS; w++) p = fmaxf(p, s_pull[w][lane + 32 * r]);
-        near_lim[r] = p > 0.0f ? a.near_ratio * p : 3.0e38f;
-    }
 
-    const float f_rad = (float)g.f_rad;
-    const float margin = 1.001f;
-    const bool screen_rad = g.record != 0;
-    const bool screen_hill = g.hill != 0 && tile.block != 2;
-    const float hill_f3 = (float)g.hill_f3;
-    const float inv3M = (float)(1.0 / (3.0 * g.mass[tile.base]));
-
-    for (int j0 = max(heavy_end, tile.src_begin); j0 < tile.src_end; j0 += MX_T) {
-        const int nj = min(MX_T, tile.src_end - j0);
+    constexpr int SLICE = MX_T / MX_WARPS;  // 32 sources per warp and tile: one near-mask bit each
+    for (int j0 = max(heavy_end, src_lo); j0 < src_hi; j0 += MX_T) {
+        const int nj = min(MX_T, src_hi - j0);
         __syncthreads();
         for (int q = threadIdx.x; q < nj; q += blockDim.x) {
             const SplitPos sp = a.sp[j0 + q];
             s_xy[q] = sp.xy;
             s_zm[q] = sp.zm;
-            s_R[q] = (float)g.radius[j0 + q];
-            s_rho[q] = g.hill ? (float)g.rho[j0 + q] : 0.0f;
-            s_id[q] = g.id[j0 + q];
+            if (SCREEN) {
+                s_R[q] = (float)g.radius[j0 + q];
+                s_rho[q] = g.hill ? (float)g.rho[j0 + q] : 0.0f;
+            }
         }
         __syncthreads();
-        const int q_begin = warp * (MX_T / MX_WARPS);
-        const int q_end = min(nj, q_begin + MX_T / MX_WARPS);
-        for (int q = q_begin; q < q_end; q++) {
-            const float4 pxy = s_xy[q];
-            const float4 pzm = s_zm[q];
-            const int idj = s_id[q];
-            const int j = j0 + q;
-            if (idj < 0) continue;
+        const int q_begin = warp * SLICE;
+        const int q_end = min(nj, q_begin + SLICE);
+        if (q_begin >= q_end) continue;
+        unsigned near_mask[MX_R];
+        // does this slice hold any of the CTA's sinks?
+        const bool diag = (j0 + q_begin < tile.sink_begin + MX_S) && (j0 + q_end > tile.sink_begin);
+        if (diag)
+            mixed_slice<true, SCREEN>(a, tile, j0, q_begin, q_end, s_xy, s_zm, s_R, s_rho, s_sink, si, xh, xl, yh,
+                                      yl, zh, zl, near_lim, ax, ay, az, near_mask, lane);
+        else
+            mixed_slice<false, SCREEN>(a, tile, j0, q_begin, q_end, s_xy, s_zm, s_R, s_rho, s_sink, si, xh, xl, yh,
+                                       yl, zh, zl, near_lim, ax, ay, az, near_mask, lane);
+        // near pairs of this slice: FP64 displacement, FP32 seed + one FP64 Newton step
 #pragma unroll
-            for (int r = 0; r < MX_R; r++) {
-                if (!act[r] || j == si[r]) continue;
-                const float dx = (pxy.x - xh[r]) + (pxy.y - xl[r]);
-                const float dy = (pxy.z - yh[r]) + (pxy.w - yl[r]);
-                const float dz = (pzm.x - zh[r]) + (pzm.y - zl[r]);
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                const float mj = pzm.z;
-                if (mj > near_lim[r] * r2) {
-                    // near pair: FP64 displacement, FP32 rsqrt seed + one FP64 Newton step
-                    const double ddx = g.px[j] - xi[r], ddy = g.py[j] - yi[r], ddz = g.pz[j] - zi[r];
-                    const double dr2 = ddx * ddx + ddy * ddy + ddz * ddz;
-                    const double y0 = (double)rsqrtf((float)dr2);
-                    const double y1 = y0 * (1.5 - 0.5 * dr2 * y0 * y0);
-                    const double w = g.mass[j] * (y1 * y1 * y1);
-                    hx[r] += w * ddx;
-                    hy[r] += w * ddy;
-                    hz[r] += w * ddz;
-                } else {
-                    float y = rsqrtf(r2);
-                    y = y * fmaf(-0.5f * r2, y * y, 1.5f);
-                    const float w = mj * (y * y * y);
-                    two_sum_add(ax[r], w * dx);
-                    two_sum_add(ay[r], w * dy);
-                    two_sum_add(az[r], w * dz);
-                }
-                // event screens with a relative margin, decided in FP64
-                const int li = si[r] - tile.base, lj = j - tile.base;
-                if (li > 0 && li > lj) {
-                    bool cand = false;
-                    if (screen_rad) {
-                        const float lim = f_rad * (Rf[r] + s_R[q]) * margin;
-                        cand = r2 < lim * lim;
-                    }
-                    if (screen_hill && lj > 0) {
-                        const float h = 0.5f * (rhof[r] + s_rho[q]);
-                        const float d3 = r2 * sqrtf(r2);
-                        cand = cand || (d3 < hill_f3 * ((float)mi[r] + mj) * inv3M * (h * h * h) * margin * margin * margin);
-                    }
-                    if (cand) exact_event_tests(g, tile, si[r], j, xi[r], yi[r], zi[r], Ri[r], mi[r], rhoi[r]);
-                }
+        for (int r = 0; r < MX_R; r++) {
+            unsigned m = near_mask[r];
+            while (m) {
+                const int b = __ffs(m) - 1;
+                m &= m - 1;
+                const int s = lane + 32 * r;
+                double hx = 0.0, hy = 0.0, hz = 0.0;
+                near_term(g, s_sink[s], j0 + q_begin + b, hx, hy, hz);
+                s_h[warp][0][s] += hx;
+                s_h[warp][1][s] += hy;
+                s_h[warp][2][s] += hz;
             }
         }
     }
-    // combine the warps' partial sums
+
+    // per-sink total: fixed-order sum over the warps of (FP32 compensated + FP64) partials
+    __syncthreads();
 #pragma unroll
     for (int r = 0; r < MX_R; r++) {
         const int s = lane + 32 * r;
-        s_red[warp][0][s] = ax[r].s; s_red[warp][1][s] = ax[r].c;
-        s_red[warp][2][s] = ay[r].s; s_red[warp][3][s] = ay[r].c;
-        s_red[warp][4][s] = az[r].s; s_red[warp][5][s] = az[r].c;
-        s_redh[warp][0][s] = hx[r]; s_redh[warp][1][s] = hy[r]; s_redh[warp][2][s] = hz[r];
+        s_h[warp][0][s] += (double)ax[r].s + (double)ax[r].c;
+        s_h[warp][1][s] += (double)ay[r].s + (double)ay[r].c;
+        s_h[warp][2][s] += (double)az[r].s + (double)az[r].c;
     }
     __syncthreads();
-    // threads 0..3*MX_S-1: one (sink, component) each
     for (int t = threadIdx.x; t < 3 * MX_S; t += blockDim.x) {
         const int comp = t / MX_S, s = t % MX_S;
         const int i = tile.sink_begin + s;
         if (i >= tile.sink_end) continue;
-        Acc2 acc{0.0f, 0.0f};
-        double h = 0.0;
-        for (int w = 0; w < MX_WARPS; w++) {
-            acc = two_sum_merge(acc, Acc2{s_red[w][2 * comp][s], s_red[w][2 * comp + 1][s]});
-            h += s_redh[w][comp][s];
-        }
-        const double v = h + ((double)acc.s + (double)acc.c);
-        (comp == 0 ? g.ax : (comp == 1 ? g.ay : g.az))[i] = v;
+        double v = 0.0;
+        for (int w = 0; w < MX_WARPS; w++) v += s_h[w][comp][s];
+        if (!(0 < g.id[i])) v = 0.0;  // inactive sinks feel nothing (pp_disk.cu:235-236)
+        if (a.partial)
+            a.partial[((long long)blockIdx.y * 3 + comp) * a.n_part + i] = v;
+        else
+            (comp == 0 ? g.ax : (comp == 1 ? g.ay : g.az))[i] = v;
     }
 }
 
-int launch_split_positions(const double* x, const double* y, const double* z, const double* m, int n, SplitPos* out,
-                           cudaStream_t st)
+// a_i = sum over source chunks of the partials, in chunk order
+__global__ void mixed_reduce_kernel(const double* __restrict__ partial, int n_chunks, int n_part, const Tile* tiles,
+                                    int n_tiles, double* ax, double* ay, double* az)
+{
+    const Tile tile = tiles[blockIdx.x];
+    const int i = tile.sink_begin + threadIdx.x;
+    if (i >= tile.sink_end) return;
+    for (int comp = 0; comp < 3; comp++) {
+        double v = 0.0;
+        for (int c = 0; c < n_chunks; c++) v += partial[((long long)c * 3 + comp) * n_part + i];
+        (comp == 0 ? ax : (comp == 1 ? ay : az))[i] = v;
+    }
+}
+
+int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id, int n,
+                           SplitPos* out, cudaStream_t st)
 {
     if (n <= 0) return 0;
-    split_positions_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, m, n, out);
+    split_positions_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, m, id, n, out);
     RG_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
 
 int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* heavy_end, float near_ratio,
-                            cudaStream_t st)
+                            int n_chunks, int chunk, double* partial, int n_part, cudaStream_t st)
 {
     if (g.n_tiles <= 0) return 0;
     MixedArgs a;
@@ -321,8 +419,19 @@ int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* hea
     a.sp = (const SplitPos*)split;
     a.heavy_end = heavy_end;
     a.near_ratio = near_ratio;
-    grav_mixed_kernel<<<g.n_tiles, 256, 0, st>>>(a);
+    a.chunk = n_chunks > 1 ? chunk : (1 << 30);
+    a.partial = n_chunks > 1 ? partial : nullptr;
+    a.n_part = n_part;
+    const dim3 grid(g.n_tiles, n_chunks > 1 ? n_chunks : 1);
+    if (g.record || g.hill)
+        grav_mixed_kernel<true><<<grid, 256, 0, st>>>(a);
+    else
+        grav_mixed_kernel<false><<<grid, 256, 0, st>>>(a);
     RG_CUDA_CHECK(cudaGetLastError());
+    if (n_chunks > 1) {
+        mixed_reduce_kernel<<<g.n_tiles, MX_S, 0, st>>>(partial, n_chunks, n_part, g.tiles, g.n_tiles, g.ax, g.ay, g.az);
+        RG_CUDA_CHECK(cudaGetLastError());
+    }
     return 0;
 }
 
