@@ -201,6 +201,61 @@ RG_API int rg_energy(rg_ctx* ctx, double* energy, double angmom[3]);
 /* Last step-size values in days: the step that was taken and the next trial step. */
 RG_API int rg_get_dt(rg_ctx* ctx, double* dt_did_day, double* dt_try_day);
 
+/* ------------------------------------------------------------------ ensembles */
+
+/*
+ * Many independent disks integrated together on one GPU (not in the reference, which
+ * runs one disk per process).  Every disk follows the reference's RKF7(8) adaptive step
+ * (int_rungekutta8.cu:704-797) with its own step size and clock; one attempt of all disks
+ * is one CUDA-graph launch, the step-size controller runs on the device.  Collisions,
+ * ejections and hit-star events follow the reference's rules (pp_disk.cu:683-1202); a disk
+ * with an event pauses until the host has applied it.  Differences from rg_advance: the
+ * controller's pow is the device's (the trial steps may differ from glibc's in the last
+ * bit), and inactive bodies stay in storage (no compaction; indices do not change).
+ */
+typedef struct rg_ens rg_ens;
+
+/* Bodies of disk s are records [off_s, off_s + n_total_s) of the arrays, off_s the sum of
+ * the previous disks' totals; `thr` holds RG_THRESHOLD_N values per disk. */
+RG_API int rg_ens_create(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const rg_vec_t* v,
+                         const rg_param_t* p, const rg_body_metadata_t* md, const double* thr,
+                         int event_capacity, rg_ens** out);
+RG_API int rg_ens_destroy(rg_ens* ens);
+
+/* RKF7(8) with tolerance `tol` (the only integrator of the ensemble), first trial step
+ * dt_day for every disk. */
+RG_API int rg_ens_set_integrator(rg_ens* ens, double dt_day, double tol, int error_check_for_tp);
+
+/* gravity mode (RG_GRAVITY_*), Hill-sphere close-encounter factor (0: off), CUDA graphs
+ * on/off (on by default). */
+RG_API int rg_ens_set_options(rg_ens* ens, int gravity_mode, double hill_factor, int use_graph);
+
+/* Integrates every disk until its clock exceeds t_stop_day (the reference's
+ * `while (t <= stop)` loop) or max_attempts attempts (<= 0: no limit) were launched. */
+RG_API int rg_ens_advance(rg_ens* ens, double t_stop_day, int64_t max_attempts, int64_t* n_attempts);
+
+/* State of disk `sys` in file units (arrays of its n_total records; any may be NULL). */
+RG_API int rg_ens_get_state(rg_ens* ens, int sys, rg_vec_t* r, rg_vec_t* v, rg_param_t* p,
+                            rg_body_metadata_t* md, double* t_day);
+RG_API int rg_ens_get_stats(rg_ens* ens, int sys, rg_ens_stats_t* stats);
+
+/* Drains the event log of all disks (records as rg_events; sys_of_event[k] = disk). */
+RG_API int rg_ens_events(rg_ens* ens, rg_event_t* out, int* sys_of_event, int cap, int* n);
+RG_API int rg_ens_event_count(rg_ens* ens, int* n);
+
+/* Drains the log of attempts (one record per disk and attempt, in launch order per disk)
+ * recorded since the last call; at most `cap` records.  Logging is on when
+ * rg_ens_set_step_log(ens, capacity) gave a capacity > 0. */
+RG_API int rg_ens_set_step_log(rg_ens* ens, int capacity);
+RG_API int rg_ens_step_log(rg_ens* ens, rg_step_rec_t* out, int cap, int* n);
+
+/* Energy and angular momentum of disk `sys` (as rg_energy). */
+RG_API int rg_ens_energy(rg_ens* ens, int sys, double* energy, double angmom[3]);
+
+/* The stream the ensemble launches on, and its kernel-launch count. */
+RG_API int rg_ens_get_stream(rg_ens* ens, void** stream);
+RG_API int rg_ens_kernel_count(rg_ens* ens, int64_t* n_kernels, int64_t* n_graph_launches);
+
 /* ------------------------------------------------------------------ measurement */
 
 /* The CUDA stream (cudaStream_t) the context launches on, for callers that time or

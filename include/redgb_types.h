@@ -72,6 +72,31 @@ typedef struct rg_profile {
     double  stage_ms;
 } rg_profile_t;
 
+/* per-system statistics of an ensemble (rg_ens_get_stats) */
+typedef struct rg_ens_stats {
+    double  t_day;          /* simulation clock of the system            */
+    double  dt_try_day;     /* next trial step                           */
+    double  dt_did_day;     /* last accepted step                        */
+    int64_t n_tried_step, n_passed_step, n_failed_step;
+    int32_t status;         /* RG_SYS_*                                  */
+    int32_t n_total;        /* bodies (active and inactive)              */
+    int64_t n_proposed, n_proposal_accepted, n_fallback;  /* learned step proposer */
+} rg_ens_stats_t;
+
+enum { RG_SYS_RUNNING = 0, RG_SYS_HELD = 1, RG_SYS_DONE = 2, RG_SYS_ERROR = 3 };
+
+/* one attempt of one disk of an ensemble (rg_ens_step_log): the integrator's own record,
+ * also the training data of the learned step proposer */
+typedef struct rg_step_rec {
+    int32_t sys;
+    int32_t accepted;      /* the RKF error estimate accepted the attempt          */
+    int32_t proposed;      /* the trial step came from the learned proposer          */
+    int32_t step;          /* accepted steps of the disk before this attempt        */
+    double  dt;            /* trial step, internal units (1/k days)                 */
+    double  err;           /* |dt * 41/840 * max(err)|, the controller's error      */
+    float   feat[8];       /* proposer inputs at the attempt (see rg_ens_set_proposer) */
+} rg_step_rec_t;
+
 /* red_type.h:46-54 threshold_t */
 enum {
     RG_THRESHOLD_HIT_CENTRUM_DISTANCE = 0,

@@ -65,7 +65,21 @@ struct GravArgs {
     uint32_t seq;
     EventBuf ev;  // radius-criterion records
     EventBuf hv;  // Hill-sphere records
+    // ensembles: tiles of systems whose flag is 0 are skipped; records are counted per system
+    // and carry the system's attempt number (collisions) or step-start number (Hill)
+    const int* sys_active;
+    unsigned int* sys_events;
+    const unsigned int* sys_attempt;
+    const unsigned int* sys_f0;
 };
+
+// sequence tag of a record: (attempt << 8) | stage, or the step-start number for Hill
+__device__ __forceinline__ uint32_t record_seq(const GravArgs& g, const Tile& t, int kind)
+{
+    if (kind == 1 && g.sys_f0) return g.sys_f0[t.sys];
+    if (g.sys_attempt) return (g.sys_attempt[t.sys] << 8) | g.seq;
+    return g.seq;
+}
 
 }  // namespace redgb
 

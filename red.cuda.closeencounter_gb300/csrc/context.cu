@@ -117,6 +117,7 @@ struct rg_ctx {
         int n;          // tiles
         int row_base;   // few-sink groups: first row in the terms buffer
         int rows;       // few-sink groups: rows
+        int max_src;    // few-sink groups: largest source count of a tile
     };
     std::vector<Group> plan[2];
     std::vector<Tile> tiles;       // all groups' tiles, uploaded to d_tiles
@@ -133,6 +134,7 @@ struct rg_ctx {
     int* d_row_sink = nullptr;
     int* d_row_nsrc = nullptr;
     int rows_cap = 0;
+    int* d_few_row0 = nullptr;  // per tile
     int64_t pairs_per_eval = 0;
     bool tiles_dirty = true;
 
@@ -179,6 +181,7 @@ void free_all(rg_ctx* c)
     cudaFree(c->d_partial);
     cudaFree(c->d_row_sink);
     cudaFree(c->d_row_nsrc);
+    cudaFree(c->d_few_row0);
     cudaFree(c->d_ev);
     cudaFree(c->d_ev_count);
     cudaFree(c->d_hill);
@@ -317,7 +320,7 @@ void build_tiles(rg_ctx* c)
 
     auto add_group = [&](int mode, int kind, int s0, int s1, int src1, int block, int step) {
         if (s1 <= s0) return;
-        rg_ctx::Group gr{kind, c->tiles.size(), 0, c->few_rows, 0};
+        rg_ctx::Group gr{kind, c->tiles.size(), 0, c->few_rows, 0, src1};
         for (int s = s0; s < s1; s += step) {
             c->tiles.push_back(Tile{s, std::min(s + step, s1), 0, src1, 0, 0, block, 0});
             c->heavy_mx.push_back(kind == GROUP_MIXED ? std::min(n_heavy, src1) : 0);
@@ -369,10 +372,13 @@ int sync_tiles(rg_ctx* c)
     if (n > c->tiles_cap) {
         cudaFree(c->d_tiles);
         cudaFree(c->d_heavy);
+        cudaFree(c->d_few_row0);
         c->d_tiles = nullptr;
         c->d_heavy = nullptr;
+        c->d_few_row0 = nullptr;
         int rc = dalloc(&c->d_tiles, (size_t)n);
         if (!rc) rc = dalloc(&c->d_heavy, (size_t)n);
+        if (!rc) rc = dalloc(&c->d_few_row0, (size_t)n);
         if (rc) return rc;
         c->tiles_cap = n;
     }
@@ -396,6 +402,7 @@ int sync_tiles(rg_ctx* c)
     if (n > 0) {
         RG_CUDA_CHECK(cudaMemcpyAsync(c->d_tiles, c->tiles.data(), n * sizeof(Tile), cudaMemcpyHostToDevice, c->st));
         RG_CUDA_CHECK(cudaMemcpyAsync(c->d_heavy, c->heavy_mx.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->st));
+        RG_CUDA_CHECK(cudaMemcpyAsync(c->d_few_row0, c->few_row0.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->st));
     }
     if (c->few_rows > 0) {
         RG_CUDA_CHECK(cudaMemcpyAsync(c->d_row_sink, c->row_sink.data(), c->few_rows * sizeof(int),
@@ -462,10 +469,10 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
             break;
         case GROUP_FEW_SERIAL:
         case GROUP_FEW_TREE:
-            rc = launch_grav_fp64_few(g, c->few_row0.data() + gr.off, c->few_nsrc.data() + gr.off, c->d_terms,
-                                      c->few_rows, c->few_pitch, c->d_row_sink, c->d_row_nsrc, gr.row_base, gr.rows,
+            rc = launch_grav_fp64_few(g, c->d_few_row0 + gr.off, gr.max_src, c->d_terms, c->few_rows, c->few_pitch,
+                                      c->d_row_sink, c->d_row_nsrc, nullptr, gr.row_base, gr.rows,
                                       gr.kind == GROUP_FEW_SERIAL, c->st);
-            c->n_kernels += gr.n + 1;
+            c->n_kernels += 2;
             break;
         case GROUP_MIXED:
             if (!split_done) {

@@ -1,0 +1,1549 @@
+// ensemble.cu -- many independent disks on one GPU, each following the reference's
+// RKF7(8) adaptive step (int_rungekutta8.cu:704-797) with its own step size and clock.
+//
+// Layout: the disks' bodies are concatenated (disk s owns [base_s, base_s + n_s)), with the
+// same structure-of-arrays rows as a single context (common.cuh).  Per-disk scalars (clock,
+// trial step, status, error maximum, counters) live on the device, so one attempt of every
+// running disk is a fixed sequence of launches -- captured once as a CUDA graph:
+//
+//   stage 0 (disks that start a new step) -> 12 stage combines + force evaluations ->
+//   y_{n+1} -> error maximum per disk -> step-size controller (one thread per disk) ->
+//   accepted disks copy y_{n+1} into y and screen for ejection / hit-star -> finalize.
+//
+// Kernels take per-disk activity masks, so finished or paused disks cost nothing but an
+// early exit.  A disk whose accepted step recorded a collision (or whose new state has an
+// ejection / hit-star candidate) is held; the host then applies the reference's handlers
+// (pp_disk.cu:717-738,934-976,1078-1202) to that disk's state and releases it.  Differences
+// from the single-disk path: the controller's pow is the device's (trial steps may differ
+// from glibc's in the last bit), and inactive bodies are not compacted away.
+//
+// Built with -fmad=false: the stage combinations and the error norm keep the reference's
+// operation order.
+#include <algorithm>
+#include <array>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/redgb.h"
+#include "common.cuh"
+#include "host_tools.h"
+#include "kernels.h"
+#include "rk_tables.h"
+
+namespace redgb {
+int set_error(int code, const std::string& msg);
+
+// bodies [b0, b1) of disk `sys`; the error norm covers [b0, e1)
+struct StageTile {
+    int sys, b0, b1, e1;
+};
+
+struct EnsStageArgs {
+    const StageTile* tiles;
+    const int* active;    // per disk
+    const double* dt;     // per disk trial step
+    const double* y;      // 6 rows
+    const double* k[MAXT];
+    double c[MAXT];
+    int nterm;
+    int stride;
+    double* out_lo;       // rows 0..2
+    double* out_hi;       // rows 3..5
+};
+
+// FORM_SUM (stage rows) or FORM_RK8_NP1 (y_{n+1}), one CTA per stage tile
+template <int FORM, int NTERM>
+__global__ void __launch_bounds__(256) ens_combine_kernel(EnsStageArgs a)
+{
+    const StageTile t = a.tiles[blockIdx.x];
+    if (!a.active[t.sys]) return;
+    const double dt = a.dt[t.sys];
+    const int nb = t.b1 - t.b0;
+    for (int f = threadIdx.x; f < 6 * nb; f += blockDim.x) {
+        const int row = f / nb;
+        const long long e = (long long)row * a.stride + t.b0 + (f - row * nb);
+        const double y = a.y[e];
+        double out;
+        if (FORM == FORM_SUM) {
+            double sum = a.c[0] * a.k[0][e];
+#pragma unroll
+            for (int q = 1; q < NTERM; q++) sum = sum + a.c[q] * a.k[q][e];
+            out = y + dt * sum;
+        } else {
+            out = y + dt * (a.c[0] * a.k[0][e] + a.c[1] * a.k[1][e] + a.c[2] * (a.k[2][e] + a.k[3][e]) +
+                            a.c[3] * (a.k[4][e] + a.k[5][e]) + a.c[4] * a.k[6][e]);
+        }
+        if (row < 3)
+            a.out_lo[e] = out;
+        else
+            a.out_hi[e - 3LL * a.stride] = out;
+    }
+}
+
+// rows [r0, r0 + nr) of src -> rows [d0, d0 + nr) of dst, for disks whose mask is set
+__global__ void ens_copy_kernel(const StageTile* tiles, const int* mask, const double* src, int r0, double* dst,
+                                int d0, int nr, int stride)
+{
+    const StageTile t = tiles[blockIdx.x];
+    if (!mask[t.sys]) return;
+    const int nb = t.b1 - t.b0;
+    for (int f = threadIdx.x; f < nr * nb; f += blockDim.x) {
+        const int row = f / nb;
+        const long long o = (long long)t.b0 + (f - row * nb);
+        dst[(long long)(d0 + row) * stride + o] = src[(long long)(r0 + row) * stride + o];
+    }
+}
+
+// e = ((k0 + k10) - k11) - k12, signed maximum starting at 0 (integrator.cu:240-255)
+__global__ void __launch_bounds__(256) ens_error_kernel(const StageTile* tiles, const int* active, const double* k0,
+                                                        const double* k10, const double* k11, const double* k12,
+                                                        int stride, unsigned long long* max_bits)
+{
+    const StageTile t = tiles[blockIdx.x];
+    if (!active[t.sys]) return;
+    const int nb = t.e1 - t.b0;
+    double m = 0.0;
+    for (int f = threadIdx.x; f < 6 * nb; f += blockDim.x) {
+        const int row = f / nb;
+        const long long e = (long long)row * stride + t.b0 + (f - row * nb);
+        const double v = (k0[e] + k10[e] - k11[e] - k12[e]);
+        if (m < v) m = v;
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const double o = __shfl_xor_sync(0xffffffffu, m, off);
+        if (m < o) m = o;
+    }
+    __shared__ double wmax[8];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) wmax[warp] = m;
+    __syncthreads();
+    if (warp == 0) {
+        m = lane < (int)(blockDim.x >> 5) ? wmax[lane] : 0.0;
+#pragma unroll
+        for (int off = 4; off > 0; off >>= 1) {
+            const double o = __shfl_xor_sync(0xffffffffu, m, off);
+            if (m < o) m = o;
+        }
+        if (lane == 0 && m > 0.0) atomicMax(&max_bits[t.sys], (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+struct EnsSys {
+    int n;
+    int* status;
+    int* active;
+    int* active_f0;
+    int* acc;
+    int* ej;
+    unsigned int* events;
+    unsigned long long* max_bits;
+    double* t;
+    double* t_prev;
+    double* t_stop;
+    double* dt_try;
+    double* dt_did;
+    long long* n_tried;
+    long long* n_passed;
+    long long* n_failed;
+    unsigned int* attempt;   // per disk: attempts so far (event records carry it)
+    unsigned int* acc_attempt;
+    unsigned int* n_f0;      // per disk: step-start force evaluations so far
+    double tol;
+    rg_step_rec_t* log;      // attempt log (nullptr: off)
+    unsigned int* log_count;
+    unsigned int log_cap;
+};
+
+// the controller of rungekutta8::step, one thread per disk
+__global__ void ens_controller_kernel(EnsSys s)
+{
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= s.n) return;
+    if (!s.active[d]) {
+        s.acc[d] = 0;
+        return;
+    }
+    const double raw = __longlong_as_double((long long)s.max_bits[d]);
+    const double dt = s.dt_try[d];
+    const double max_err = fabs(dt * (41.0 / 840.0) * raw);
+    const double new_dt = dt * (0.9 * pow(s.tol / max_err, 1.0 / 8.0));
+    if (s.log) {
+        const unsigned int slot = atomicAdd(s.log_count, 1u);
+        if (slot < s.log_cap) {
+            rg_step_rec_t& rec = s.log[slot];
+            rec.sys = d;
+            rec.accepted = !(max_err > s.tol);
+            rec.proposed = 0;
+            rec.step = (int)s.n_passed[d];
+            rec.dt = dt;
+            rec.err = max_err;
+            for (int q = 0; q < 8; q++) rec.feat[q] = 0.0f;
+        }
+    }
+    s.n_tried[d]++;
+    if (!(max_err > s.tol)) {
+        s.t_prev[d] = s.t[d];
+        s.t[d] = s.t[d] + dt;
+        s.dt_did[d] = dt;
+        s.n_passed[d]++;
+        s.acc[d] = 1;
+        s.acc_attempt[d] = s.attempt[d];
+    } else {
+        s.n_failed[d]++;
+        s.acc[d] = 0;
+    }
+    s.dt_try[d] = new_dt;
+}
+
+// ejection / hit-star screen of the accepted disks' new states (kernel_pp_disk::
+// check_for_ejection_hit_centrum, pp_disk.cu:72-142); the host applies the handlers
+__global__ void ens_eject_screen_kernel(const StageTile* tiles, const int* mask, const double* y, int stride,
+                                        const int* id, const int* type, const double* thr, int* ej)
+{
+    const StageTile t = tiles[blockIdx.x];
+    if (!mask[t.sys]) return;
+    const double* th = thr + 5 * t.sys;
+    if (!(0.0 < th[0]) && !(0.0 < th[1])) return;
+    for (int i = t.b0 + threadIdx.x; i < t.b1; i += blockDim.x) {
+        if (!(0 < id[i] && type[i] != 0)) continue;
+        const double x = y[i], yy = y[stride + i], z = y[2LL * stride + i];
+        const double r2 = x * x + yy * yy + z * z;
+        if ((0.0 < th[1] && th[4] < r2) || (0.0 < th[0] && th[3] > r2)) ej[t.sys] = 1;
+    }
+}
+
+__global__ void ens_finalize_kernel(EnsSys s)
+{
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= s.n) return;
+    if (s.active_f0[d]) s.n_f0[d]++;
+    if (s.active[d]) {
+        s.attempt[d]++;
+        if (s.acc[d]) {
+            if (s.events[d] > 0 || s.ej[d])
+                s.status[d] = RG_SYS_HELD;
+            else if (!(s.t[d] <= s.t_stop[d]))
+                s.status[d] = RG_SYS_DONE;
+        }
+        if (s.status[d] == RG_SYS_RUNNING && (!isfinite(s.dt_try[d]) || s.dt_try[d] == 0.0))
+            s.status[d] = RG_SYS_ERROR;
+    }
+    const int run = s.status[d] == RG_SYS_RUNNING;
+    s.active_f0[d] = run && (s.acc[d] || !s.active[d]);
+    s.active[d] = run;
+    s.events[d] = 0;
+    s.ej[d] = 0;
+    s.max_bits[d] = 0ull;
+}
+
+// per-body energy partials of an ensemble (as energy_kernel, with disk offsets)
+__global__ void ens_energy_kernel(const double* y, const double* mass, const int* id, int stride, int base, int n,
+                                  int n_si, int n_massive, double* part)
+{
+    const int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n) return;
+    const int i = base + li;
+    const long long sd = stride;
+    const double *rx = y, *ry = y + sd, *rz = y + 2 * sd, *vx = y + 3 * sd, *vy = y + 4 * sd, *vz = y + 5 * sd;
+    double T = 0, U = 0, Uc = 0, Lx = 0, Ly = 0, Lz = 0;
+    if (id[i] > 0) {
+        const double m = mass[i];
+        T = 0.5 * m * (vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
+        Lx = m * (ry[i] * vz[i] - rz[i] * vy[i]);
+        Ly = m * (rz[i] * vx[i] - rx[i] * vz[i]);
+        Lz = m * (rx[i] * vy[i] - ry[i] * vx[i]);
+        if (li >= 1 && li < n_massive) {
+            const int jmax = li < n_si ? li : n_si;
+            for (int lj = 0; lj < jmax; lj++) {
+                const int j = base + lj;
+                if (id[j] <= 0) continue;
+                const double dx = rx[j] - rx[i], dy = ry[j] - ry[i], dz = rz[j] - rz[i];
+                const double d = sqrt(dx * dx + dy * dy + dz * dz);
+                const double term = -(m * mass[j]) / d;
+                const double tt = U + term;
+                if (fabs(U) >= fabs(term))
+                    Uc += (U - tt) + term;
+                else
+                    Uc += (term - tt) + U;
+                U = tt;
+            }
+        }
+    }
+    part[li] = T;
+    part[n + li] = U + Uc;
+    part[2 * n + li] = Lx;
+    part[3 * n + li] = Ly;
+    part[4 * n + li] = Lz;
+}
+
+}  // namespace redgb
+
+using namespace redgb;
+
+// ============================================================================ host side
+struct rg_ens {
+    int n_sys = 0;
+    int cap = 0;
+    int device = 0, n_sm = 152;
+    std::vector<int> base, ntot;
+    std::vector<std::array<int, 7>> cnt;
+    std::vector<rg_param_t> p;
+    std::vector<rg_body_metadata_t> md;
+    std::vector<double> thr;  // 5 per disk
+    cudaStream_t st = nullptr;
+    // device, per body
+    double* d_y = nullptr;
+    double* d_yout = nullptr;
+    double* d_k[13] = {};
+    double* d_P = nullptr;
+    double* d_mass = nullptr;
+    double* d_radius = nullptr;
+    double* d_rho = nullptr;
+    int* d_id = nullptr;
+    int* d_type = nullptr;
+    void* d_split = nullptr;
+    double* d_partial = nullptr;
+    size_t partial_cap = 0;
+    double* d_thr = nullptr;
+    // device, per disk
+    int *d_status = nullptr, *d_active = nullptr, *d_active_f0 = nullptr, *d_acc = nullptr, *d_ej = nullptr;
+    unsigned int* d_sys_events = nullptr;
+    unsigned long long* d_maxbits = nullptr;
+    double *d_t = nullptr, *d_tprev = nullptr, *d_tstop = nullptr, *d_dt_try = nullptr, *d_dt_did = nullptr;
+    long long *d_ntried = nullptr, *d_npassed = nullptr, *d_nfailed = nullptr;
+    unsigned int *d_attempt = nullptr, *d_acc_attempt = nullptr, *d_nf0 = nullptr;
+    // stage tiles
+    std::vector<StageTile> stiles;
+    StageTile* d_stiles = nullptr;
+    // gravity plan
+    struct Group {
+        int kind;
+        size_t off;
+        int n;
+        int row_base, rows, max_src;
+    };
+    std::vector<Group> plan[2];
+    std::vector<Tile> tiles;
+    std::vector<int> heavy, few_row0, row_sink, row_nsrc, row_sys;
+    int few_rows = 0;
+    long long few_pitch = 0;
+    Tile* d_tiles = nullptr;
+    int* d_heavy = nullptr;
+    int* d_few_row0 = nullptr;
+    int *d_row_sink = nullptr, *d_row_nsrc = nullptr, *d_row_sys = nullptr;
+    double* d_terms = nullptr;
+    int64_t pairs_per_eval = 0;
+    // events
+    DevEvent* d_ev = nullptr;
+    unsigned int* d_ev_count = nullptr;
+    DevEvent* d_hill = nullptr;
+    unsigned int* d_hill_count = nullptr;
+    unsigned int ev_cap = 0;
+    std::vector<std::pair<int, rg_event_t>> log;
+    std::vector<std::vector<int64_t>> hill_prev;
+    std::vector<int64_t> hill_last;  // f0 index of the last processed Hill set per disk
+    // options
+    int has_int = 0, ectp = 0, gravity_mode = RG_GRAVITY_FP64, use_graph = 1;
+    double tol = 1e-10, dt0 = 0.0, hill_factor = 0.0;
+    float near_ratio = 1.0e-5f;
+    int started = 0;
+    // graph
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool graph_valid = false;
+    int64_t n_kernels = 0, n_graph_launches = 0, n_attempts = 0;
+    int64_t kernels_per_attempt = 0;
+    double* d_part = nullptr;
+    int* d_base_of = nullptr;  // per body: index of its disk's body 0
+    rg_step_rec_t* d_log = nullptr;
+    unsigned int* d_log_count = nullptr;
+    unsigned int log_cap = 0;
+    std::vector<rg_step_rec_t> host_log;
+
+    int n_si(int s) const { return cnt[s][0] + cnt[s][1] + cnt[s][2] + cnt[s][3]; }
+    int n_massive(int s) const { return n_si(s) + cnt[s][4] + cnt[s][5]; }
+    EnsSys sys() const
+    {
+        return EnsSys{n_sys, d_status, d_active, d_active_f0, d_acc, d_ej, d_sys_events, d_maxbits, d_t, d_tprev,
+                      d_tstop, d_dt_try, d_dt_did, d_ntried, d_npassed, d_nfailed, d_attempt, d_acc_attempt, d_nf0,
+                      tol, d_log, d_log_count, log_cap};
+    }
+};
+
+namespace {
+
+constexpr double GAUSS = 1.720209895e-2;
+constexpr double GAUSS2 = 2.959122082855911025e-4;
+constexpr int STAGE_TILE = 2048;
+constexpr int ENS_FEW_BLOCK = 32;
+enum { GROUP_PAIRPAR = 0, GROUP_ROWSEQ = 1, GROUP_FEW_SERIAL = 2, GROUP_FEW_TREE = 3, GROUP_MIXED = 4 };
+
+template <class T>
+int dalloc(T** p, size_t count)
+{
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return set_error(RG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    return RG_OK;
+}
+
+void free_all(rg_ens* e)
+{
+    if (e->exec) cudaGraphExecDestroy(e->exec);
+    if (e->graph) cudaGraphDestroy(e->graph);
+    void* ptrs[] = {e->d_y, e->d_yout, e->d_P, e->d_mass, e->d_radius, e->d_rho, e->d_id, e->d_type, e->d_split,
+                    e->d_partial, e->d_thr, e->d_status, e->d_active, e->d_active_f0, e->d_acc, e->d_ej,
+                    e->d_sys_events, e->d_maxbits, e->d_t, e->d_tprev, e->d_tstop, e->d_dt_try, e->d_dt_did,
+                    e->d_ntried, e->d_npassed, e->d_nfailed, e->d_attempt, e->d_acc_attempt, e->d_nf0, e->d_stiles,
+                    e->d_tiles, e->d_heavy, e->d_few_row0, e->d_row_sink, e->d_row_nsrc, e->d_row_sys, e->d_terms,
+                    e->d_ev, e->d_ev_count, e->d_hill, e->d_hill_count, e->d_part, e->d_base_of, e->d_log,
+                    e->d_log_count};
+    for (void* q : ptrs) cudaFree(q);
+    for (auto& k : e->d_k) cudaFree(k);
+    if (e->st) cudaStreamDestroy(e->st);
+}
+
+// ------------------------------------------------------------------- plans
+void build_stage_tiles(rg_ens* e)
+{
+    e->stiles.clear();
+    for (int s = 0; s < e->n_sys; s++) {
+        const int b = e->base[s], n = e->ntot[s];
+        const int nerr = e->ectp ? n : e->n_massive(s);
+        for (int o = 0; o < n; o += STAGE_TILE) {
+            const int b0 = b + o, b1 = b + std::min(n, o + STAGE_TILE);
+            e->stiles.push_back(StageTile{s, b0, b1, std::max(b0, std::min(b1, b + nerr))});
+        }
+    }
+}
+
+void build_gravity_plan(rg_ens* e)
+{
+    e->tiles.clear();
+    e->heavy.clear();
+    e->few_row0.clear();
+    e->row_sink.clear();
+    e->row_nsrc.clear();
+    e->row_sys.clear();
+    e->few_rows = 0;
+    e->few_pitch = 0;
+    e->pairs_per_eval = 0;
+    struct Pending {
+        int kind, mode;
+        std::vector<Tile> t;
+        std::vector<int> heavy;
+    };
+    // group tiles of all disks by (mode, kind)
+    std::vector<Tile> by[2][5];
+    std::vector<int> hv[2][5];
+    for (int s = 0; s < e->n_sys; s++) {
+        const int b = e->base[s];
+        const int nsi = e->n_si(s), nm = e->n_massive(s), nt = e->ntot[s];
+        const int n_heavy = std::min(nsi, e->cnt[s][0] + e->cnt[s][1] + e->cnt[s][2]);
+        e->pairs_per_eval += (int64_t)nsi * (nm > 0 ? nm - 1 : 0) + (int64_t)(nm - nsi) * nsi + (int64_t)(nt - nm) * nm;
+        struct Blk {
+            int s0, s1, src1, block;
+        } blks[3] = {{0, nsi, nm, 0}, {nsi, nm, nsi, 1}, {nm, nt, nm, 2}};
+        auto add = [&](int mode, int kind, int s0, int s1, int src1, int block, int step) {
+            for (int q = s0; q < s1; q += step) {
+                by[mode][kind].push_back(Tile{b + q, b + std::min(q + step, s1), b, b + src1, s, b, block, 0});
+                hv[mode][kind].push_back(b + std::min(n_heavy, src1));
+            }
+        };
+        for (const auto& k : blks) {
+            if (k.s1 <= k.s0) continue;
+            if (k.src1 <= 64) {
+                add(0, GROUP_ROWSEQ, k.s0, k.s1, k.src1, k.block, 128);
+                add(1, GROUP_ROWSEQ, k.s0, k.s1, k.src1, k.block, 128);
+            } else if (k.s1 - k.s0 <= ENS_FEW_BLOCK) {
+                add(0, GROUP_FEW_SERIAL, k.s0, k.s1, k.src1, k.block, FEW_SINKS_MAX);
+                add(1, GROUP_FEW_TREE, k.s0, k.s1, k.src1, k.block, FEW_SINKS_MAX);
+            } else {
+                add(0, GROUP_PAIRPAR, k.s0, k.s1, k.src1, k.block, 16);
+                const int light0 = k.block == 0 ? std::max(k.s0, std::min(n_heavy, k.s1)) : k.s0;
+                add(1, GROUP_FEW_TREE, k.s0, light0, k.src1, k.block, FEW_SINKS_MAX);
+                add(1, GROUP_MIXED, light0, k.s1, k.src1, k.block, MIXED_SINKS_PER_TILE);
+            }
+        }
+    }
+    for (int mode = 0; mode < 2; mode++) {
+        e->plan[mode].clear();
+        for (int kind = 0; kind < 5; kind++) {
+            auto& T = by[mode][kind];
+            if (T.empty()) continue;
+            rg_ens::Group gr{kind, e->tiles.size(), (int)T.size(), e->few_rows, 0, 0};
+            for (size_t k = 0; k < T.size(); k++) {
+                e->tiles.push_back(T[k]);
+                e->heavy.push_back(hv[mode][kind][k]);
+                if (kind == GROUP_FEW_SERIAL || kind == GROUP_FEW_TREE) {
+                    e->few_row0.push_back(e->few_rows);
+                    const int nsrc = T[k].src_end - T[k].src_begin;
+                    for (int i = T[k].sink_begin; i < T[k].sink_end; i++) {
+                        e->row_sink.push_back(i);
+                        e->row_nsrc.push_back(nsrc);
+                        e->row_sys.push_back(T[k].sys);
+                        e->few_rows++;
+                        gr.rows++;
+                    }
+                    gr.max_src = std::max(gr.max_src, nsrc);
+                    e->few_pitch = std::max<long long>(e->few_pitch, nsrc);
+                } else {
+                    e->few_row0.push_back(0);
+                }
+            }
+            e->plan[mode].push_back(gr);
+        }
+    }
+}
+
+int upload_plans(rg_ens* e)
+{
+    const size_t nt = e->tiles.size();
+    int rc = RG_OK;
+    auto chk = [&](int x) {
+        if (!rc) rc = x;
+    };
+    cudaFree(e->d_stiles);
+    cudaFree(e->d_tiles);
+    cudaFree(e->d_heavy);
+    cudaFree(e->d_few_row0);
+    cudaFree(e->d_row_sink);
+    cudaFree(e->d_row_nsrc);
+    cudaFree(e->d_row_sys);
+    cudaFree(e->d_terms);
+    e->d_stiles = nullptr;
+    e->d_tiles = nullptr;
+    e->d_heavy = e->d_few_row0 = e->d_row_sink = e->d_row_nsrc = e->d_row_sys = nullptr;
+    e->d_terms = nullptr;
+    chk(dalloc(&e->d_stiles, e->stiles.size()));
+    chk(dalloc(&e->d_tiles, nt));
+    chk(dalloc(&e->d_heavy, nt));
+    chk(dalloc(&e->d_few_row0, nt));
+    chk(dalloc(&e->d_row_sink, (size_t)e->few_rows));
+    chk(dalloc(&e->d_row_nsrc, (size_t)e->few_rows));
+    chk(dalloc(&e->d_row_sys, (size_t)e->few_rows));
+    chk(dalloc(&e->d_terms, (size_t)3 * e->few_rows * (size_t)std::max<long long>(e->few_pitch, 1)));
+    if (rc) return rc;
+    auto up = [&](void* dst, const void* src, size_t bytes) {
+        if (bytes && !rc) {
+            cudaError_t err = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, e->st);
+            if (err != cudaSuccess) rc = cuda_fail(err, "upload", __FILE__, __LINE__);
+        }
+    };
+    up(e->d_stiles, e->stiles.data(), e->stiles.size() * sizeof(StageTile));
+    up(e->d_tiles, e->tiles.data(), nt * sizeof(Tile));
+    up(e->d_heavy, e->heavy.data(), nt * sizeof(int));
+    up(e->d_few_row0, e->few_row0.data(), nt * sizeof(int));
+    up(e->d_row_sink, e->row_sink.data(), e->row_sink.size() * sizeof(int));
+    up(e->d_row_nsrc, e->row_nsrc.data(), e->row_nsrc.size() * sizeof(int));
+    up(e->d_row_sys, e->row_sys.data(), e->row_sys.size() * sizeof(int));
+    if (!rc) RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    e->graph_valid = false;
+    return rc;
+}
+
+// ------------------------------------------------------------------- one attempt
+int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, int stage, const int* mask,
+                bool hill)
+{
+    const size_t cap = (size_t)e->cap;
+    GravArgs g{};
+    g.px = pos;
+    g.py = pos + cap;
+    g.pz = pos + 2 * cap;
+    g.vx = vel;
+    g.vy = vel + cap;
+    g.vz = vel + 2 * cap;
+    g.mass = e->d_mass;
+    g.radius = e->d_radius;
+    g.id = e->d_id;
+    g.rho = e->d_rho;
+    g.ax = acc;
+    g.ay = acc + cap;
+    g.az = acc + 2 * cap;
+    // one collision factor for the ensemble (the first disk's): the kernels take a scalar
+    g.f_rad = e->thr[RG_THRESHOLD_RADII_ENHANCE_FACTOR];
+    g.hill_f3 = e->hill_factor * e->hill_factor * e->hill_factor;
+    g.record = (stage > 0 && g.f_rad > 0.0) ? 1 : 0;
+    g.hill = hill ? 1 : 0;
+    g.seq = (uint32_t)stage;
+    g.ev = EventBuf{e->d_ev, e->d_ev_count, e->ev_cap};
+    g.hv = EventBuf{e->d_hill, e->d_hill_count, e->ev_cap};
+    g.sys_active = mask;
+    g.sys_events = e->d_sys_events;
+    g.sys_attempt = e->d_attempt;
+    g.sys_f0 = e->d_nf0;
+    int rc = RG_OK;
+    if (hill) {
+        // distance from each disk's body 0 (the per-body base is the tile's base: use a
+        // base-of array built from the stage tiles)
+        rc = launch_star_distance(g.px, g.py, g.pz, e->d_base_of, e->cap, e->d_rho, e->st);
+        if (rc) return rc;
+        e->n_kernels++;
+    }
+    bool split_done = false;
+    for (const auto& gr : e->plan[e->gravity_mode == RG_GRAVITY_MIXED ? 1 : 0]) {
+        g.tiles = e->d_tiles + gr.off;
+        g.n_tiles = gr.n;
+        switch (gr.kind) {
+        case GROUP_PAIRPAR: rc = launch_grav_fp64_pairpar(g, 16, e->st); e->n_kernels++; break;
+        case GROUP_ROWSEQ: rc = launch_grav_fp64_rowseq(g, e->st); e->n_kernels++; break;
+        case GROUP_FEW_SERIAL:
+        case GROUP_FEW_TREE:
+            rc = launch_grav_fp64_few(g, e->d_few_row0 + gr.off, gr.max_src, e->d_terms, e->few_rows, e->few_pitch,
+                                      e->d_row_sink, e->d_row_nsrc, e->d_row_sys, gr.row_base, gr.rows,
+                                      gr.kind == GROUP_FEW_SERIAL, e->st);
+            e->n_kernels += 2;
+            break;
+        case GROUP_MIXED:
+            if (!split_done) {
+                rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->cap, (SplitPos*)e->d_split, e->st);
+                split_done = true;
+                e->n_kernels++;
+            }
+            if (!rc) {
+                const int src = std::max(1, (int)(e->pairs_per_eval / std::max(1, e->cap)));
+                int chunks = std::max(1, std::min((4 * e->n_sm + gr.n - 1) / gr.n, src / (4 * MIXED_SOURCE_TILE)));
+                chunks = 1;  // per-disk source counts differ; one chunk keeps the partial buffer simple
+                (void)src;
+                rc = launch_grav_mixed_tiles(g, e->d_split, e->d_heavy + gr.off, e->near_ratio, chunks,
+                                             MIXED_SOURCE_TILE, nullptr, e->cap, e->st);
+                e->n_kernels++;
+            }
+            break;
+        }
+        if (rc) return rc;
+    }
+    return rc;
+}
+
+int launch_stage(rg_ens* e, int form, int nterm, const int* stages, const double* coef, double* out_lo,
+                 double* out_hi)
+{
+    EnsStageArgs a{};
+    a.tiles = e->d_stiles;
+    a.active = e->d_active;
+    a.dt = e->d_dt_try;
+    a.y = e->d_y;
+    for (int q = 0; q < nterm; q++) {
+        a.k[q] = e->d_k[stages[q]];
+        a.c[q] = coef[q];
+    }
+    a.nterm = nterm;
+    a.stride = e->cap;
+    a.out_lo = out_lo;
+    a.out_hi = out_hi;
+    const int g = (int)e->stiles.size();
+    if (g <= 0) return RG_OK;
+#define RG_ENS(F, T) ens_combine_kernel<F, T><<<g, 256, 0, e->st>>>(a)
+    if (form == FORM_RK8_NP1) {
+        RG_ENS(FORM_RK8_NP1, 7);
+    } else {
+        switch (nterm) {
+        case 1: RG_ENS(FORM_SUM, 1); break;
+        case 2: RG_ENS(FORM_SUM, 2); break;
+        case 3: RG_ENS(FORM_SUM, 3); break;
+        case 4: RG_ENS(FORM_SUM, 4); break;
+        case 6: RG_ENS(FORM_SUM, 6); break;
+        case 7: RG_ENS(FORM_SUM, 7); break;
+        case 8: RG_ENS(FORM_SUM, 8); break;
+        case 9: RG_ENS(FORM_SUM, 9); break;
+        default: return set_error(RG_ERR_ARG, "stage row length");
+        }
+    }
+#undef RG_ENS
+    RG_CUDA_CHECK(cudaGetLastError());
+    e->n_kernels++;
+    return RG_OK;
+}
+
+// The launch sequence of one attempt of every running disk (captured as a graph).
+int record_attempt(rg_ens* e)
+{
+    const size_t cap = (size_t)e->cap;
+    const int ns = (int)e->stiles.size();
+    const int nb = (e->n_sys + 127) / 128;
+    // stage 0 for the disks that start a new step: k0 = (v, a(y))
+    ens_copy_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active_f0, e->d_y, 3, e->d_k[0], 0, 3, e->cap);
+    RG_CUDA_CHECK(cudaGetLastError());
+    e->n_kernels++;
+    int rc = ens_gravity(e, e->d_y, e->d_y + 3 * cap, e->d_k[0] + 3 * cap, 0, e->d_active_f0, e->hill_factor > 0.0);
+    if (rc) return rc;
+    for (int r = 1; r <= 12 && !rc; r++) {
+        double a[9];
+        for (int q = 0; q < rk8_nterm[r]; q++) a[q] = rk8_a[rk8_aidx[r][q]];
+        rc = launch_stage(e, FORM_SUM, rk8_nterm[r], rk8_stage[r], a, e->d_P, e->d_k[r]);
+        if (!rc) rc = ens_gravity(e, e->d_P, e->d_k[r], e->d_k[r] + 3 * cap, r, e->d_active, false);
+    }
+    if (rc) return rc;
+    const int snp[7] = {0, 5, 6, 7, 8, 9, 10};
+    const double bnp[7] = {rk8_b[0], rk8_b[5], rk8_b[6], rk8_b[8], rk8_b[10], 0.0, 0.0};
+    rc = launch_stage(e, FORM_RK8_NP1, 7, snp, bnp, e->d_yout, e->d_yout + 3 * cap);
+    if (rc) return rc;
+    ens_error_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active, e->d_k[0], e->d_k[10], e->d_k[11], e->d_k[12],
+                                           e->cap, e->d_maxbits);
+    RG_CUDA_CHECK(cudaGetLastError());
+    ens_controller_kernel<<<nb, 128, 0, e->st>>>(e->sys());
+    RG_CUDA_CHECK(cudaGetLastError());
+    ens_copy_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_acc, e->d_yout, 0, e->d_y, 0, 6, e->cap);
+    RG_CUDA_CHECK(cudaGetLastError());
+    ens_eject_screen_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_acc, e->d_y, e->cap, e->d_id, e->d_type,
+                                                  e->d_thr, e->d_ej);
+    RG_CUDA_CHECK(cudaGetLastError());
+    ens_finalize_kernel<<<nb, 128, 0, e->st>>>(e->sys());
+    RG_CUDA_CHECK(cudaGetLastError());
+    e->n_kernels += 5;
+    return RG_OK;
+}
+
+int launch_attempt(rg_ens* e)
+{
+    if (!e->use_graph) {
+        const int64_t k0 = e->n_kernels;
+        int rc = record_attempt(e);
+        e->kernels_per_attempt = e->n_kernels - k0;
+        return rc;
+    }
+    if (!e->graph_valid) {
+        if (e->exec) cudaGraphExecDestroy(e->exec);
+        if (e->graph) cudaGraphDestroy(e->graph);
+        e->exec = nullptr;
+        e->graph = nullptr;
+        RG_CUDA_CHECK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
+        const int64_t k0 = e->n_kernels;
+        int rc = record_attempt(e);
+        e->kernels_per_attempt = e->n_kernels - k0;
+        e->n_kernels = k0;
+        cudaGraph_t g = nullptr;
+        cudaError_t err = cudaStreamEndCapture(e->st, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (err != cudaSuccess) return cuda_fail(err, "cudaStreamEndCapture", __FILE__, __LINE__);
+        e->graph = g;
+        RG_CUDA_CHECK(cudaGraphInstantiate(&e->exec, e->graph, 0));
+        e->graph_valid = true;
+    }
+    RG_CUDA_CHECK(cudaGraphLaunch(e->exec, e->st));
+    e->n_graph_launches++;
+    e->n_kernels += e->kernels_per_attempt;
+    return RG_OK;
+}
+
+// ------------------------------------------------------------------- host event handling
+rg_event_t zero_event()
+{
+    rg_event_t v;
+    std::memset(&v, 0, sizeof(v));
+    return v;
+}
+
+// one disk's state on the host while its events are applied
+struct HostDisk {
+    rg_ens* e;
+    int s, b, n;
+    std::vector<double> rows;  // 6 rows of n
+    double t;
+    double& at(int row, int i) { return rows[(size_t)row * n + (i - b)]; }
+    rg_vec_t r(int i) { return rg_vec_t{at(0, i), at(1, i), at(2, i), 0.0}; }
+    rg_vec_t v(int i) { return rg_vec_t{at(3, i), at(4, i), at(5, i), 0.0}; }
+    void set(int i, const rg_vec_t& rr, const rg_vec_t& vv)
+    {
+        at(0, i) = rr.x; at(1, i) = rr.y; at(2, i) = rr.z;
+        at(3, i) = vv.x; at(4, i) = vv.y; at(5, i) = vv.z;
+    }
+};
+
+// pp_disk::handle_collision_pair (pp_disk.cu:1151-1202) on a host disk (indices global)
+int merge_pair(HostDisk& h, rg_event_t* c)
+{
+    rg_ens* e = h.e;
+    const int surv = c->idx1 + h.b, merg = c->idx2 + h.b;
+    if (RG_BODY_SUPERPLANETESIMAL == e->md[merg].body_type)
+        return set_error(RG_ERR_NOT_IMPLEMENTED, "collision with a super-planetesimal is not implemented");
+    c->p1 = e->p[surv];
+    c->p2 = e->p[merg];
+    host::calc_position_after_collision(c->p1.mass, c->p2.mass, &c->r1, &c->r2, &c->rs);
+    host::calc_velocity_after_collision(c->p1.mass, c->p2.mass, &c->v1, &c->v2, &c->vs);
+    h.set(surv, c->rs, c->vs);
+    host::calc_physical_properties(c->p1, c->p2, &c->ps);
+    e->p[surv] = c->ps;
+    e->md[merg].id *= -1;
+    e->p[merg].mass = 0.0;
+    e->p[merg].density = 0.0;
+    e->p[merg].radius = 0.0;
+    h.set(merg, rg_vec_t{1.0e20, 0.0, 0.0, 0.0}, rg_vec_t{0.0, 0.0, 0.0, 0.0});
+    return RG_OK;
+}
+
+// applies the accepted step's collision records and the ejection / hit-star check
+int handle_disk(rg_ens* e, int s, const std::vector<DevEvent>& recs, double t_prev, double dt_did)
+{
+    HostDisk h{e, s, e->base[s], e->ntot[s], {}, 0.0};
+    h.rows.resize((size_t)6 * h.n);
+    RG_CUDA_CHECK(cudaMemcpy2DAsync(h.rows.data(), h.n * sizeof(double), e->d_y + h.b, e->cap * sizeof(double),
+                                    h.n * sizeof(double), 6, cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&h.t, e->d_t + s, sizeof(double), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    const int nsi = e->n_si(s);
+    // raw records in the reference's order, then create_sp_events + handle_collision_pair
+    std::vector<rg_event_t> ev;
+    for (const DevEvent& d : recs) {
+        rg_event_t x = zero_event();
+        const int stage = (int)(d.seq & 0xff);
+        const double curr_t = t_prev + rk8_c[stage] * dt_did;
+        x.t = (d.i - h.b >= nsi) ? t_prev : curr_t;  // pp_disk.cu:576,581
+        x.d = d.d;
+        int surv = d.i, merg = d.j;
+        const double *rs = d.ri, *vs = d.vi, *rm = d.rj, *vm = d.vj;
+        if (e->p[merg].mass > e->p[surv].mass) {
+            std::swap(surv, merg);
+            std::swap(rs, rm);
+            std::swap(vs, vm);
+        }
+        x.event_name = RG_EVENT_COLLISION;
+        x.id1 = e->md[surv].id;
+        x.id2 = e->md[merg].id;
+        x.idx1 = surv - h.b;
+        x.idx2 = merg - h.b;
+        x.r1 = rg_vec_t{rs[0], rs[1], rs[2], 0.0};
+        x.v1 = rg_vec_t{vs[0], vs[1], vs[2], 0.0};
+        x.r2 = rg_vec_t{rm[0], rm[1], rm[2], 0.0};
+        x.v2 = rg_vec_t{vm[0], vm[1], vm[2], 0.0};
+        ev.push_back(x);
+    }
+    std::vector<char> done(ev.size(), 0);
+    for (size_t k = 0; k < ev.size(); k++) {
+        if (done[k]) continue;
+        done[k] = 1;
+        rg_event_t cur = ev[k];
+        for (size_t i = k + 1; i < ev.size(); i++)
+            if (cur.id1 == ev[i].id1 && cur.id2 == ev[i].id2) {
+                done[i] = 1;
+                if (cur.t > ev[i].t) cur = ev[i];
+            }
+        int rc = merge_pair(h, &cur);
+        if (rc) return rc;
+        e->log.emplace_back(s, cur);
+    }
+    // ejection / hit-star check of the new state (pp_disk.cu:934-976,1091-1109)
+    const double* th = &e->thr[5 * (size_t)s];
+    std::vector<rg_event_t> ej;
+    for (int i = h.b; i < h.b + h.n; i++) {
+        if (!(0 < e->md[i].id && RG_BODY_STAR != e->md[i].body_type)) continue;
+        const rg_vec_t ri = h.r(i);
+        const double r2 = ri.x * ri.x + ri.y * ri.y + ri.z * ri.z;
+        int name = 0;
+        if (0.0 < th[1] && th[4] < r2)
+            name = RG_EVENT_EJECTION;
+        else if (0.0 < th[0] && th[3] > r2)
+            name = RG_EVENT_HIT_CENTRUM;
+        if (!name) continue;
+        rg_event_t x = zero_event();
+        x.event_name = name;
+        x.d = std::sqrt(r2);
+        x.t = h.t;
+        x.id1 = e->md[h.b].id;
+        x.id2 = e->md[i].id;
+        x.idx1 = 0;
+        x.idx2 = i - h.b;
+        x.r1 = h.r(h.b);
+        x.v1 = h.v(h.b);
+        x.r2 = ri;
+        x.v2 = h.v(i);
+        if (name == RG_EVENT_EJECTION) {
+            x.p1 = e->p[h.b];
+            x.p2 = e->p[i];
+            x.rs = x.r1;
+            x.vs = x.v1;
+            x.ps = x.p1;
+        }
+        e->md[i].id *= -1;
+        ej.push_back(x);
+    }
+    for (auto& x : ej) {
+        if (x.event_name == RG_EVENT_HIT_CENTRUM) {
+            int rc = merge_pair(h, &x);
+            if (rc) return rc;
+        }
+        e->log.emplace_back(s, x);
+    }
+    // upload the disk
+    std::vector<double> m(h.n), R(h.n);
+    std::vector<int> id(h.n);
+    for (int i = 0; i < h.n; i++) {
+        m[i] = e->p[h.b + i].mass;
+        R[i] = e->p[h.b + i].radius;
+        id[i] = e->md[h.b + i].id;
+    }
+    RG_CUDA_CHECK(cudaMemcpy2DAsync(e->d_y + h.b, e->cap * sizeof(double), h.rows.data(), h.n * sizeof(double),
+                                    h.n * sizeof(double), 6, cudaMemcpyHostToDevice, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(e->d_mass + h.b, m.data(), h.n * sizeof(double), cudaMemcpyHostToDevice, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(e->d_radius + h.b, R.data(), h.n * sizeof(double), cudaMemcpyHostToDevice, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(e->d_id + h.b, id.data(), h.n * sizeof(int), cudaMemcpyHostToDevice, e->st));
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    return RG_OK;
+}
+
+// Hill-sphere records -> log entries (a pair is logged when it enters the sphere)
+void handle_hill(rg_ens* e, std::vector<DevEvent>& recs, const std::vector<unsigned int>& nf0)
+{
+    std::sort(recs.begin(), recs.end(), [](const DevEvent& a, const DevEvent& b) {
+        if (a.sys != b.sys) return a.sys < b.sys;
+        if (a.seq != b.seq) return a.seq < b.seq;
+        if (a.i != b.i) return a.i < b.i;
+        return a.j < b.j;
+    });
+    size_t k = 0;
+    while (k < recs.size()) {
+        const int s = recs[k].sys;
+        const int64_t f0 = recs[k].seq;
+        std::vector<int64_t> cur;
+        size_t q = k;
+        for (; q < recs.size() && recs[q].sys == s && (int64_t)recs[q].seq == f0; q++) {
+            const DevEvent& d = recs[q];
+            const int64_t key = ((int64_t)(uint32_t)e->md[d.i].id << 32) | (int64_t)(uint32_t)e->md[d.j].id;
+            const bool seen = (e->hill_last[s] == f0 - 1) &&
+                              std::find(e->hill_prev[s].begin(), e->hill_prev[s].end(), key) != e->hill_prev[s].end();
+            if (!seen) {
+                rg_event_t x = zero_event();
+                x.event_name = RG_EVENT_CLOSE_ENCOUNTER;
+                x.d = d.d;
+                x.id1 = e->md[d.i].id;
+                x.id2 = e->md[d.j].id;
+                x.idx1 = d.i - e->base[s];
+                x.idx2 = d.j - e->base[s];
+                x.p1 = e->p[d.i];
+                x.p2 = e->p[d.j];
+                x.r1 = rg_vec_t{d.ri[0], d.ri[1], d.ri[2], 0.0};
+                x.v1 = rg_vec_t{d.vi[0], d.vi[1], d.vi[2], 0.0};
+                x.r2 = rg_vec_t{d.rj[0], d.rj[1], d.rj[2], 0.0};
+                x.v2 = rg_vec_t{d.vj[0], d.vj[1], d.vj[2], 0.0};
+                e->log.emplace_back(s, x);
+            }
+            cur.push_back(key);
+        }
+        e->hill_prev[s].swap(cur);
+        e->hill_last[s] = f0;
+        k = q;
+    }
+    // disks whose later step-start evaluations found no pair have left every sphere
+    for (int s = 0; s < e->n_sys; s++)
+        if ((int64_t)nf0[s] > e->hill_last[s] + 1) {
+            e->hill_prev[s].clear();
+            e->hill_last[s] = (int64_t)nf0[s] - 1;
+        }
+}
+
+}  // namespace
+
+// ============================================================================ C ABI
+#define RG_GUARD(expr)                                                    \
+    try {                                                                 \
+        return (expr);                                                    \
+    } catch (const std::bad_alloc&) {                                     \
+        return set_error(RG_ERR_NOMEM, "host allocation failed");         \
+    } catch (...) {                                                       \
+        return set_error(RG_ERR_STATE, "unexpected exception");           \
+    }
+
+namespace {
+
+template <class T>
+int upload(rg_ens* e, T* dst, const std::vector<T>& src)
+{
+    if (!src.empty())
+        RG_CUDA_CHECK(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, e->st));
+    return RG_OK;
+}
+
+template <class T>
+int download(rg_ens* e, std::vector<T>& dst, const T* src, size_t n)
+{
+    dst.resize(n);
+    if (n) RG_CUDA_CHECK(cudaMemcpyAsync(dst.data(), src, n * sizeof(T), cudaMemcpyDeviceToHost, e->st));
+    return RG_OK;
+}
+
+int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,
+                const rg_body_metadata_t* md, const double* thr, int event_capacity, rg_ens** out)
+{
+    if (n_sys <= 0 || !counts || !r || !v || !p || !md || !thr || !out) return set_error(RG_ERR_ARG, "bad argument");
+    *out = nullptr;
+    int dev_count = 0;
+    if (cudaGetDeviceCount(&dev_count) != cudaSuccess || dev_count <= 0) {
+        cudaGetLastError();
+        return set_error(RG_ERR_NO_DEVICE, "no CUDA device");
+    }
+    rg_ens* e = new rg_ens();
+    e->n_sys = n_sys;
+    int64_t tot = 0;
+    for (int s = 0; s < n_sys; s++) {
+        std::array<int, 7> c;
+        const int32_t* cn = &counts[s].n_s;
+        int n = 0;
+        for (int k = 0; k < 7; k++) {
+            if (cn[k] < 0) {
+                delete e;
+                return set_error(RG_ERR_ARG, "negative body count");
+            }
+            c[k] = cn[k];
+            n += cn[k];
+        }
+        if (n <= 0) {
+            delete e;
+            return set_error(RG_ERR_ARG, "empty disk");
+        }
+        e->cnt.push_back(c);
+        e->base.push_back((int)tot);
+        e->ntot.push_back(n);
+        tot += n;
+    }
+    if (tot > (1 << 28)) {
+        delete e;
+        return set_error(RG_ERR_ARG, "too many bodies");
+    }
+    e->cap = (int)tot;
+    cudaGetDevice(&e->device);
+    cudaDeviceGetAttribute(&e->n_sm, cudaDevAttrMultiProcessorCount, e->device);
+    e->ev_cap = (unsigned int)(event_capacity > 0 ? event_capacity : std::max<int64_t>(tot, 4096));
+    const size_t nt = (size_t)tot, ns = (size_t)n_sys;
+    int rc = RG_OK;
+    auto chk = [&](int x) {
+        if (!rc) rc = x;
+    };
+    if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess) chk(set_error(RG_ERR_CUDA, "stream"));
+    chk(dalloc(&e->d_y, 6 * nt));
+    chk(dalloc(&e->d_yout, 6 * nt));
+    for (auto& k : e->d_k) chk(dalloc(&k, 6 * nt));
+    chk(dalloc(&e->d_P, 3 * nt));
+    chk(dalloc(&e->d_mass, nt));
+    chk(dalloc(&e->d_radius, nt));
+    chk(dalloc(&e->d_rho, nt));
+    chk(dalloc(&e->d_id, nt));
+    chk(dalloc(&e->d_type, nt));
+    chk(dalloc(&e->d_base_of, nt));
+    chk(dalloc((char**)&e->d_split, SPLIT_POS_BYTES * nt));
+    chk(dalloc(&e->d_thr, 5 * ns));
+    chk(dalloc(&e->d_status, ns));
+    chk(dalloc(&e->d_active, ns));
+    chk(dalloc(&e->d_active_f0, ns));
+    chk(dalloc(&e->d_acc, ns));
+    chk(dalloc(&e->d_ej, ns));
+    chk(dalloc(&e->d_sys_events, ns));
+    chk(dalloc(&e->d_maxbits, ns));
+    chk(dalloc(&e->d_t, ns));
+    chk(dalloc(&e->d_tprev, ns));
+    chk(dalloc(&e->d_tstop, ns));
+    chk(dalloc(&e->d_dt_try, ns));
+    chk(dalloc(&e->d_dt_did, ns));
+    chk(dalloc(&e->d_ntried, ns));
+    chk(dalloc(&e->d_npassed, ns));
+    chk(dalloc(&e->d_nfailed, ns));
+    chk(dalloc(&e->d_attempt, ns));
+    chk(dalloc(&e->d_acc_attempt, ns));
+    chk(dalloc(&e->d_nf0, ns));
+    chk(dalloc(&e->d_ev, e->ev_cap));
+    chk(dalloc(&e->d_ev_count, 1));
+    chk(dalloc(&e->d_hill, e->ev_cap));
+    chk(dalloc(&e->d_hill_count, 1));
+    if (rc) {
+        free_all(e);
+        delete e;
+        return rc;
+    }
+    e->p.assign(p, p + nt);
+    e->md.assign(md, md + nt);
+    e->thr.assign(thr, thr + 5 * ns);
+    e->hill_prev.assign(ns, {});
+    e->hill_last.assign(ns, -2);
+    // per disk: barycentric transform and time rescale as rg_create does
+    std::vector<double> h(6 * nt);
+    std::vector<int> base_of(nt);
+    for (int s = 0; s < n_sys; s++) {
+        const int b = e->base[s], n = e->ntot[s];
+        std::vector<rg_vec_t> rr(r + b, r + b + n), vv(v + b, v + b + n);
+        if (0 == std::fabs(rr[0].x) && 0 == std::fabs(rr[0].y) && 0 == std::fabs(rr[0].z) && 0 == std::fabs(vv[0].x) &&
+            0 == std::fabs(vv[0].y) && 0 == std::fabs(vv[0].z)) {
+            rg_vec_t R0{0, 0, 0, 0}, V0{0, 0, 0, 0};
+            for (int j = n - 1; j >= 0; j--) {
+                const double m = e->p[b + j].mass;
+                R0.x += m * rr[j].x; R0.y += m * rr[j].y; R0.z += m * rr[j].z;
+                V0.x += m * vv[j].x; V0.y += m * vv[j].y; V0.z += m * vv[j].z;
+            }
+            double M0 = 0.0;
+            for (int j = n - 1; j >= 0; j--) M0 += e->p[b + j].mass;
+            R0.x /= M0; R0.y /= M0; R0.z /= M0;
+            V0.x /= M0; V0.y /= M0; V0.z /= M0;
+            for (int j = n - 1; j >= 0; j--) {
+                rr[j].x -= R0.x; rr[j].y -= R0.y; rr[j].z -= R0.z;
+                vv[j].x -= V0.x; vv[j].y -= V0.y; vv[j].z -= V0.z;
+            }
+        }
+        for (int j = 0; j < n; j++) {
+            const size_t i = (size_t)b + j;
+            h[i] = rr[j].x;
+            h[nt + i] = rr[j].y;
+            h[2 * nt + i] = rr[j].z;
+            h[3 * nt + i] = vv[j].x / GAUSS;
+            h[4 * nt + i] = vv[j].y / GAUSS;
+            h[5 * nt + i] = vv[j].z / GAUSS;
+            base_of[i] = b;
+        }
+    }
+    std::vector<double> m(nt), R(nt);
+    std::vector<int> id(nt), ty(nt);
+    for (size_t i = 0; i < nt; i++) {
+        m[i] = e->p[i].mass;
+        R[i] = e->p[i].radius;
+        id[i] = e->md[i].id;
+        ty[i] = e->md[i].body_type;
+    }
+    chk(upload(e, e->d_y, h));
+    chk(upload(e, e->d_mass, m));
+    chk(upload(e, e->d_radius, R));
+    chk(upload(e, e->d_id, id));
+    chk(upload(e, e->d_type, ty));
+    chk(upload(e, e->d_base_of, base_of));
+    chk(upload(e, e->d_thr, e->thr));
+    std::vector<int> zi(ns, 0);
+    std::vector<double> zd(ns, 0.0);
+    std::vector<long long> zl(ns, 0);
+    std::vector<unsigned int> zu(ns, 0);
+    std::vector<unsigned long long> zb(ns, 0);
+    chk(upload(e, e->d_status, zi));
+    chk(upload(e, e->d_acc, zi));
+    chk(upload(e, e->d_ej, zi));
+    chk(upload(e, e->d_t, zd));
+    chk(upload(e, e->d_tprev, zd));
+    chk(upload(e, e->d_dt_did, zd));
+    chk(upload(e, e->d_ntried, zl));
+    chk(upload(e, e->d_npassed, zl));
+    chk(upload(e, e->d_nfailed, zl));
+    chk(upload(e, e->d_attempt, zu));
+    chk(upload(e, e->d_acc_attempt, zu));
+    chk(upload(e, e->d_nf0, zu));
+    chk(upload(e, e->d_sys_events, zu));
+    chk(upload(e, e->d_maxbits, zb));
+    if (!rc && cudaMemsetAsync(e->d_ev_count, 0, sizeof(unsigned int), e->st) != cudaSuccess) chk(RG_ERR_CUDA);
+    if (!rc && cudaMemsetAsync(e->d_hill_count, 0, sizeof(unsigned int), e->st) != cudaSuccess) chk(RG_ERR_CUDA);
+    if (!rc && cudaStreamSynchronize(e->st) != cudaSuccess) chk(set_error(RG_ERR_CUDA, "upload"));
+    if (rc) {
+        free_all(e);
+        delete e;
+        return rc;
+    }
+    build_stage_tiles(e);
+    build_gravity_plan(e);
+    rc = upload_plans(e);
+    if (rc) {
+        free_all(e);
+        delete e;
+        return rc;
+    }
+    *out = e;
+    return RG_OK;
+}
+
+// host view of the per-disk control arrays
+struct Ctl {
+    std::vector<int> status, active, active_f0;
+    std::vector<double> t, t_stop;
+};
+
+int set_control(rg_ens* e, const std::vector<int>& status, bool fresh_f0)
+{
+    std::vector<int> active(e->n_sys), f0(e->n_sys);
+    for (int s = 0; s < e->n_sys; s++) {
+        active[s] = status[s] == RG_SYS_RUNNING;
+        f0[s] = active[s] && fresh_f0;
+    }
+    int rc = upload(e, e->d_status, status);
+    if (!rc) rc = upload(e, e->d_active, active);
+    if (!rc) rc = upload(e, e->d_active_f0, f0);
+    return rc;
+}
+
+int drain_log(rg_ens* e)
+{
+    if (!e->d_log) return RG_OK;
+    unsigned int n = 0;
+    RG_CUDA_CHECK(cudaMemcpyAsync(&n, e->d_log_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    if (n > e->log_cap) return set_error(RG_ERR_EVENT_OVERFLOW, "attempt log full between two host synchronisations");
+    if (n == 0) return RG_OK;
+    const size_t old = e->host_log.size();
+    e->host_log.resize(old + n);
+    RG_CUDA_CHECK(cudaMemcpyAsync(e->host_log.data() + old, e->d_log, n * sizeof(rg_step_rec_t), cudaMemcpyDeviceToHost,
+                                  e->st));
+    RG_CUDA_CHECK(cudaMemsetAsync(e->d_log_count, 0, sizeof(unsigned int), e->st));
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    // one thread per disk appended in slot order; within a disk the attempts are ordered
+    std::stable_sort(e->host_log.begin() + old, e->host_log.end(),
+                     [](const rg_step_rec_t& a, const rg_step_rec_t& b) { return a.sys < b.sys; });
+    return RG_OK;
+}
+
+int drain(rg_ens* e, double stop)
+{
+    int lrc = drain_log(e);
+    if (lrc) return lrc;
+    unsigned int counts[2];
+    RG_CUDA_CHECK(cudaMemcpyAsync(&counts[0], e->d_ev_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&counts[1], e->d_hill_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
+    std::vector<int> status;
+    std::vector<unsigned int> nf0;
+    int rc = download(e, status, e->d_status, e->n_sys);
+    if (!rc) rc = download(e, nf0, e->d_nf0, e->n_sys);
+    if (rc) return rc;
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    if (counts[0] > e->ev_cap || counts[1] > e->ev_cap)
+        return set_error(RG_ERR_EVENT_OVERFLOW, "ensemble event buffer full between two host synchronisations");
+    if (counts[1] > 0) {
+        std::vector<DevEvent> hill;
+        rc = download(e, hill, e->d_hill, counts[1]);
+        RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+        handle_hill(e, hill, nf0);
+        RG_CUDA_CHECK(cudaMemsetAsync(e->d_hill_count, 0, sizeof(unsigned int), e->st));
+    } else if (e->hill_factor > 0.0) {
+        std::vector<DevEvent> none;
+        handle_hill(e, none, nf0);
+    }
+    std::vector<int> held;
+    for (int s = 0; s < e->n_sys; s++)
+        if (status[s] == RG_SYS_HELD) held.push_back(s);
+    if (!held.empty()) {
+        std::vector<DevEvent> recs;
+        std::vector<double> tprev, dtdid, t;
+        std::vector<unsigned int> acc_attempt;
+        rc = download(e, recs, e->d_ev, counts[0]);
+        if (!rc) rc = download(e, tprev, e->d_tprev, e->n_sys);
+        if (!rc) rc = download(e, dtdid, e->d_dt_did, e->n_sys);
+        if (!rc) rc = download(e, t, e->d_t, e->n_sys);
+        if (!rc) rc = download(e, acc_attempt, e->d_acc_attempt, e->n_sys);
+        if (rc) return rc;
+        RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+        std::sort(recs.begin(), recs.end(), [](const DevEvent& a, const DevEvent& b) {
+            if (a.sys != b.sys) return a.sys < b.sys;
+            if (a.seq != b.seq) return a.seq < b.seq;
+            if (a.i != b.i) return a.i < b.i;
+            return a.j < b.j;
+        });
+        for (int s : held) {
+            std::vector<DevEvent> mine;
+            for (const DevEvent& d : recs)
+                if (d.sys == s && (d.seq >> 8) == acc_attempt[s]) mine.push_back(d);
+            rc = handle_disk(e, s, mine, tprev[s], dtdid[s]);
+            if (rc) return rc;
+            status[s] = (t[s] <= stop) ? RG_SYS_RUNNING : RG_SYS_DONE;
+        }
+        // every record was of a rejected attempt or of a disk handled now
+        RG_CUDA_CHECK(cudaMemsetAsync(e->d_ev_count, 0, sizeof(unsigned int), e->st));
+        rc = upload(e, e->d_status, status);
+        std::vector<int> active(e->n_sys), f0(e->n_sys);
+        std::vector<int> cur_f0;
+        if (!rc) rc = download(e, cur_f0, e->d_active_f0, e->n_sys);
+        RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+        for (int s = 0; s < e->n_sys; s++) {
+            active[s] = status[s] == RG_SYS_RUNNING;
+            const bool was_held = std::find(held.begin(), held.end(), s) != held.end();
+            f0[s] = active[s] && (was_held || cur_f0[s]);
+        }
+        if (!rc) rc = upload(e, e->d_active, active);
+        if (!rc) rc = upload(e, e->d_active_f0, f0);
+        if (!rc) RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    } else if (counts[0] > 0) {
+        RG_CUDA_CHECK(cudaMemsetAsync(e->d_ev_count, 0, sizeof(unsigned int), e->st));
+    }
+    return rc;
+}
+
+int advance_impl(rg_ens* e, double t_stop_day, int64_t max_attempts, int64_t* n_attempts)
+{
+    if (!e->has_int) return set_error(RG_ERR_STATE, "no integrator set (rg_ens_set_integrator)");
+    const double stop = t_stop_day * GAUSS;
+    std::vector<int> status;
+    std::vector<double> t;
+    int rc = download(e, status, e->d_status, e->n_sys);
+    if (!rc) rc = download(e, t, e->d_t, e->n_sys);
+    if (rc) return rc;
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    for (int s = 0; s < e->n_sys; s++)
+        if (status[s] != RG_SYS_ERROR) status[s] = (t[s] <= stop) ? RG_SYS_RUNNING : RG_SYS_DONE;
+    std::vector<double> tstop(e->n_sys, stop);
+    rc = upload(e, e->d_tstop, tstop);
+    if (!rc) rc = set_control(e, status, true);
+    if (rc) return rc;
+    if (!e->started) {
+        // the reference checks for ejection / hit-star before the first step (main.cu:201)
+        ens_eject_screen_kernel<<<(int)e->stiles.size(), 256, 0, e->st>>>(e->d_stiles, e->d_active, e->d_y, e->cap,
+                                                                          e->d_id, e->d_type, e->d_thr, e->d_ej);
+        RG_CUDA_CHECK(cudaGetLastError());
+        e->n_kernels++;
+        std::vector<int> ej;
+        rc = download(e, ej, e->d_ej, e->n_sys);
+        RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+        for (int s = 0; s < e->n_sys && !rc; s++)
+            if (ej[s]) rc = handle_disk(e, s, {}, 0.0, 0.0);
+        std::vector<int> zero(e->n_sys, 0);
+        if (!rc) rc = upload(e, e->d_ej, zero);
+        if (rc) return rc;
+        e->started = 1;
+    }
+    int64_t k = 0;
+    const int per_sync = 8;
+    while (max_attempts <= 0 || k < max_attempts) {
+        const int batch = max_attempts > 0 ? (int)std::min<int64_t>(per_sync, max_attempts - k) : per_sync;
+        for (int b = 0; b < batch; b++) {
+            rc = launch_attempt(e);
+            if (rc) return rc;
+        }
+        k += batch;
+        e->n_attempts += batch;
+        rc = drain(e, stop);
+        if (rc) return rc;
+        rc = download(e, status, e->d_status, e->n_sys);
+        if (rc) return rc;
+        RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+        bool running = false, error = false;
+        for (int s = 0; s < e->n_sys; s++) {
+            running = running || status[s] == RG_SYS_RUNNING;
+            error = error || status[s] == RG_SYS_ERROR;
+        }
+        if (error) {
+            if (n_attempts) *n_attempts = k;
+            return set_error(RG_ERR_DT_NONFINITE, "a disk's step-size controller produced a non-finite or zero step");
+        }
+        if (!running) break;
+    }
+    if (n_attempts) *n_attempts = k;
+    return RG_OK;
+}
+
+int get_state_impl(rg_ens* e, int s, rg_vec_t* r, rg_vec_t* v, rg_param_t* p, rg_body_metadata_t* md, double* t_day)
+{
+    const int b = e->base[s], n = e->ntot[s];
+    std::vector<double> h((size_t)6 * n);
+    double t = 0.0;
+    RG_CUDA_CHECK(cudaMemcpy2DAsync(h.data(), n * sizeof(double), e->d_y + b, e->cap * sizeof(double),
+                                    n * sizeof(double), 6, cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&t, e->d_t + s, sizeof(double), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    for (int i = 0; i < n; i++) {
+        if (r) r[i] = rg_vec_t{h[i], h[(size_t)n + i], h[(size_t)2 * n + i], 0.0};
+        if (v)
+            v[i] = rg_vec_t{h[(size_t)3 * n + i] * GAUSS, h[(size_t)4 * n + i] * GAUSS, h[(size_t)5 * n + i] * GAUSS, 0.0};
+    }
+    if (p) std::memcpy(p, e->p.data() + b, (size_t)n * sizeof(rg_param_t));
+    if (md) std::memcpy(md, e->md.data() + b, (size_t)n * sizeof(rg_body_metadata_t));
+    if (t_day) *t_day = t / GAUSS;
+    return RG_OK;
+}
+
+int stats_impl(rg_ens* e, int s, rg_ens_stats_t* o)
+{
+    double t, dtt, dtd;
+    long long a, b, c;
+    int st;
+    RG_CUDA_CHECK(cudaMemcpyAsync(&t, e->d_t + s, sizeof(double), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&dtt, e->d_dt_try + s, sizeof(double), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&dtd, e->d_dt_did + s, sizeof(double), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&a, e->d_ntried + s, sizeof(long long), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&b, e->d_npassed + s, sizeof(long long), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&c, e->d_nfailed + s, sizeof(long long), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&st, e->d_status + s, sizeof(int), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    std::memset(o, 0, sizeof(*o));
+    o->t_day = t / GAUSS;
+    o->dt_try_day = dtt / GAUSS;
+    o->dt_did_day = dtd / GAUSS;
+    o->n_tried_step = a;
+    o->n_passed_step = b;
+    o->n_failed_step = c;
+    o->status = st;
+    o->n_total = e->ntot[s];
+    return RG_OK;
+}
+
+int energy_impl(rg_ens* e, int s, double* energy, double* angmom)
+{
+    const int n = e->ntot[s];
+    if (!e->d_part) {
+        int rc = dalloc(&e->d_part, (size_t)5 * e->cap);
+        if (rc) return rc;
+    }
+    ens_energy_kernel<<<(n + 127) / 128, 128, 0, e->st>>>(e->d_y, e->d_mass, e->d_id, e->cap, e->base[s], n, e->n_si(s),
+                                                          e->n_massive(s), e->d_part);
+    RG_CUDA_CHECK(cudaGetLastError());
+    e->n_kernels++;
+    std::vector<double> h;
+    int rc = download(e, h, e->d_part, (size_t)5 * n);
+    if (rc) return rc;
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    double sum[5], comp[5];
+    for (int q = 0; q < 5; q++) {
+        sum[q] = comp[q] = 0.0;
+        for (int i = 0; i < n; i++) {
+            const double x = h[(size_t)q * n + i];
+            const double tt = sum[q] + x;
+            comp[q] += std::fabs(sum[q]) >= std::fabs(x) ? (sum[q] - tt) + x : (x - tt) + sum[q];
+            sum[q] = tt;
+        }
+    }
+    if (energy) *energy = (sum[0] + comp[0]) + (sum[1] + comp[1]);
+    if (angmom)
+        for (int q = 0; q < 3; q++) angmom[q] = sum[2 + q] + comp[2 + q];
+    return RG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rg_ens_create(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,
+                  const rg_body_metadata_t* md, const double* thr, int event_capacity, rg_ens** out)
+{
+    RG_GUARD(create_impl(n_sys, counts, r, v, p, md, thr, event_capacity, out));
+}
+
+int rg_ens_destroy(rg_ens* e)
+{
+    if (!e) return set_error(RG_ERR_ARG, "null ensemble");
+    cudaStreamSynchronize(e->st);
+    free_all(e);
+    delete e;
+    return RG_OK;
+}
+
+int rg_ens_set_integrator(rg_ens* e, double dt_day, double tol, int error_check_for_tp)
+{
+    if (!e || !(dt_day > 0.0) || !(tol > 0.0)) return set_error(RG_ERR_ARG, "bad argument");
+    e->tol = tol;
+    e->dt0 = dt_day * GAUSS;
+    e->ectp = error_check_for_tp ? 1 : 0;
+    std::vector<double> dt(e->n_sys, e->dt0);
+    int rc = upload(e, e->d_dt_try, dt);
+    if (rc) return rc;
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    build_stage_tiles(e);
+    rc = upload_plans(e);
+    if (!rc) e->has_int = 1;
+    return rc;
+}
+
+int rg_ens_set_options(rg_ens* e, int gravity_mode, double hill_factor, int use_graph)
+{
+    if (!e || (gravity_mode != RG_GRAVITY_FP64 && gravity_mode != RG_GRAVITY_MIXED) || !(hill_factor >= 0.0))
+        return set_error(RG_ERR_ARG, "bad option");
+    e->gravity_mode = gravity_mode;
+    e->hill_factor = hill_factor;
+    e->use_graph = use_graph ? 1 : 0;
+    e->graph_valid = false;
+    return RG_OK;
+}
+
+int rg_ens_advance(rg_ens* e, double t_stop_day, int64_t max_attempts, int64_t* n_attempts)
+{
+    if (!e) return set_error(RG_ERR_ARG, "null ensemble");
+    RG_GUARD(advance_impl(e, t_stop_day, max_attempts, n_attempts));
+}
+
+int rg_ens_get_state(rg_ens* e, int sys, rg_vec_t* r, rg_vec_t* v, rg_param_t* p, rg_body_metadata_t* md,
+                     double* t_day)
+{
+    if (!e || sys < 0 || sys >= e->n_sys) return set_error(RG_ERR_ARG, "bad disk index");
+    RG_GUARD(get_state_impl(e, sys, r, v, p, md, t_day));
+}
+
+int rg_ens_get_stats(rg_ens* e, int sys, rg_ens_stats_t* o)
+{
+    if (!e || !o || sys < 0 || sys >= e->n_sys) return set_error(RG_ERR_ARG, "bad argument");
+    RG_GUARD(stats_impl(e, sys, o));
+}
+
+int rg_ens_events(rg_ens* e, rg_event_t* out, int* sys_of_event, int cap, int* n)
+{
+    if (!e || !n || cap < 0 || (cap > 0 && !out)) return set_error(RG_ERR_ARG, "bad argument");
+    const int m = std::min<int>((int)e->log.size(), cap);
+    for (int k = 0; k < m; k++) {
+        out[k] = e->log[k].second;
+        if (sys_of_event) sys_of_event[k] = e->log[k].first;
+    }
+    e->log.erase(e->log.begin(), e->log.begin() + m);
+    *n = m;
+    return RG_OK;
+}
+
+int rg_ens_event_count(rg_ens* e, int* n)
+{
+    if (!e || !n) return set_error(RG_ERR_ARG, "bad argument");
+    *n = (int)e->log.size();
+    return RG_OK;
+}
+
+int rg_ens_set_step_log(rg_ens* e, int capacity)
+{
+    if (!e || capacity < 0) return set_error(RG_ERR_ARG, "bad argument");
+    cudaFree(e->d_log);
+    cudaFree(e->d_log_count);
+    e->d_log = nullptr;
+    e->d_log_count = nullptr;
+    e->log_cap = 0;
+    if (capacity > 0) {
+        int rc = dalloc(&e->d_log, (size_t)capacity);
+        if (!rc) rc = dalloc(&e->d_log_count, 1);
+        if (rc) return rc;
+        RG_CUDA_CHECK(cudaMemsetAsync(e->d_log_count, 0, sizeof(unsigned int), e->st));
+        RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+        e->log_cap = (unsigned int)capacity;
+    }
+    e->graph_valid = false;
+    return RG_OK;
+}
+
+int rg_ens_step_log(rg_ens* e, rg_step_rec_t* out, int cap, int* n)
+{
+    if (!e || !n || cap < 0 || (cap > 0 && !out)) return set_error(RG_ERR_ARG, "bad argument");
+    int rc = drain_log(e);
+    if (rc) return rc;
+    // records of one disk stay in attempt order across drains: stable by disk on output
+    std::stable_sort(e->host_log.begin(), e->host_log.end(),
+                     [](const rg_step_rec_t& a, const rg_step_rec_t& b) { return a.sys < b.sys; });
+    const int m = std::min<int>((int)e->host_log.size(), cap);
+    if (m > 0) std::memcpy(out, e->host_log.data(), (size_t)m * sizeof(rg_step_rec_t));
+    e->host_log.erase(e->host_log.begin(), e->host_log.begin() + m);
+    *n = m;
+    return RG_OK;
+}
+
+int rg_ens_energy(rg_ens* e, int sys, double* energy, double angmom[3])
+{
+    if (!e || sys < 0 || sys >= e->n_sys) return set_error(RG_ERR_ARG, "bad disk index");
+    RG_GUARD(energy_impl(e, sys, energy, angmom));
+}
+
+int rg_ens_get_stream(rg_ens* e, void** stream)
+{
+    if (!e || !stream) return set_error(RG_ERR_ARG, "bad argument");
+    *stream = (void*)e->st;
+    return RG_OK;
+}
+
+int rg_ens_kernel_count(rg_ens* e, int64_t* n_kernels, int64_t* n_graph_launches)
+{
+    if (!e) return set_error(RG_ERR_ARG, "null ensemble");
+    if (n_kernels) *n_kernels = e->n_kernels;
+    if (n_graph_launches) *n_graph_launches = e->n_graph_launches;
+    return RG_OK;
+}
+
+}  // extern "C"

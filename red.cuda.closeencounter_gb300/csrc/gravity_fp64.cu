@@ -52,9 +52,10 @@ __device__ __forceinline__ void pair_term(const GravArgs& g, const Tile& tile, i
             if (!(kind == 0 ? rad : hill)) continue;
             const EventBuf& eb = kind == 0 ? g.ev : g.hv;
             unsigned int slot = atomicAdd(eb.count, 1u);
+            if (kind == 0 && g.sys_events) atomicAdd(&g.sys_events[tile.sys], 1u);
             if (slot < eb.cap) {
                 DevEvent* e = &eb.rec[slot];
-                e->seq = g.seq;
+                e->seq = record_seq(g, tile, kind);
                 e->kind = kind;
                 e->i = i;
                 e->j = j;
@@ -87,6 +88,7 @@ __global__ void __launch_bounds__(256) grav_fp64_pairpar(GravArgs g)
     __shared__ int sid[J];
 
     const Tile tile = g.tiles[blockIdx.x];
+    if (g.sys_active && !g.sys_active[tile.sys]) return;
     const int t = threadIdx.x;
     const int s = t % S;
     const int q0 = t / S;
@@ -144,6 +146,7 @@ __global__ void __launch_bounds__(128) grav_fp64_rowseq(GravArgs g)
     __shared__ double sx[NT], sy[NT], sz[NT], sm[NT], sR[NT], srho[NT];
     __shared__ int sid[NT];
     const Tile tile = g.tiles[blockIdx.x];
+    if (g.sys_active && !g.sys_active[tile.sys]) return;
     const int t = threadIdx.x;
     const int i = tile.sink_begin + t;
     const bool sink_ok = i < tile.sink_end;
@@ -209,16 +212,19 @@ constexpr int FEW_MAX = 8;
 
 struct FewArgs {
     GravArgs g;
-    int row0;        // first row of this tile in the terms buffer
-    double* terms;   // 3 x rows x pitch
-    int rows;        // rows of the buffer
-    long long pitch; // >= largest source count
+    const int* tile_row0;  // first row of each tile in the terms buffer
+    double* terms;         // 3 x rows x pitch
+    int rows;              // rows of the buffer
+    long long pitch;       // >= largest source count
 };
 
 __global__ void __launch_bounds__(256) grav_fp64_few_terms(FewArgs a)
 {
     const GravArgs& g = a.g;
     const Tile tile = g.tiles[blockIdx.y];
+    if (g.sys_active && !g.sys_active[tile.sys]) return;
+    if ((int)(blockIdx.x * blockDim.x) >= tile.src_end - tile.src_begin) return;
+    const int row0 = a.tile_row0[blockIdx.y];
     const int q = blockIdx.x * blockDim.x + threadIdx.x;  // source offset within the tile
     const int j = tile.src_begin + q;
     __shared__ double sx[FEW_MAX], sy[FEW_MAX], sz[FEW_MAX], sR[FEW_MAX], sm[FEW_MAX], srho[FEW_MAX];
@@ -242,7 +248,7 @@ __global__ void __launch_bounds__(256) grav_fp64_few_terms(FewArgs a)
         PairOut o{0.0, 0.0, 0.0};
         if (sact[s] && src_ok && j != i)
             pair_term(g, tile, i, j, sx[s], sy[s], sz[s], sR[s], sm[s], srho[s], xj, yj, zj, mj, Rj, rhoj, o);
-        const long long e = (long long)(a.row0 + s) * a.pitch + q;
+        const long long e = (long long)(row0 + s) * a.pitch + q;
         a.terms[e] = o.tx;
         a.terms[plane + e] = o.ty;
         a.terms[2 * plane + e] = o.tz;
@@ -256,6 +262,8 @@ struct FewSumArgs {
     long long pitch;
     const int* row_sink;   // sink index of each row
     const int* row_nsrc;   // sources of each row
+    const int* row_sys;    // system of each row (ensembles) or nullptr
+    const int* sys_active;
     double* ax;
     double* ay;
     double* az;
@@ -267,6 +275,7 @@ __global__ void few_sum_serial(FewSumArgs a)
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * a.nrows) return;
     const int comp = t / a.nrows, row = a.row0 + t % a.nrows;
+    if (a.sys_active && !a.sys_active[a.row_sys[row]]) return;
     const double* T = a.terms + ((long long)comp * a.rows + row) * a.pitch;
     const int n = a.row_nsrc[row];
     double acc = 0.0;
@@ -286,6 +295,7 @@ __global__ void few_sum_serial(FewSumArgs a)
 __global__ void __launch_bounds__(256) few_sum_tree(FewSumArgs a)
 {
     const int comp = blockIdx.x / a.nrows, row = a.row0 + blockIdx.x % a.nrows;
+    if (a.sys_active && !a.sys_active[a.row_sys[row]]) return;
     const double* T = a.terms + ((long long)comp * a.rows + row) * a.pitch;
     const int n = a.row_nsrc[row];
     double s = 0.0, c = 0.0;
@@ -332,19 +342,18 @@ int launch_grav_fp64_rowseq(const GravArgs& g, cudaStream_t st)
 // Few-sink tiles (at most FEW_MAX sinks each) -> terms -> row sums.  `tiles` holds
 // n_tiles tiles, rows are numbered tile by tile; host arrays row_sink/row_nsrc are on the
 // device already (dev_row_sink, dev_row_nsrc).
-int launch_grav_fp64_few(const GravArgs& g, const int* tile_row0, const int* tile_nsrc, double* terms, int rows,
-                         long long pitch, const int* dev_row_sink, const int* dev_row_nsrc, int group_row0,
-                         int group_rows, bool serial, cudaStream_t st)
+// Few-sink tiles -> terms -> row sums, one launch each for all tiles of the group.
+// tile_row0 (device) gives each tile's first row; max_src bounds the tiles' source counts.
+int launch_grav_fp64_few(const GravArgs& g, const int* tile_row0, int max_src, double* terms, int rows,
+                         long long pitch, const int* dev_row_sink, const int* dev_row_nsrc, const int* dev_row_sys,
+                         int group_row0, int group_rows, bool serial, cudaStream_t st)
 {
-    if (g.n_tiles <= 0 || rows <= 0 || group_rows <= 0) return 0;
-    for (int k = 0; k < g.n_tiles; k++) {
-        if (tile_nsrc[k] <= 0) continue;
-        FewArgs a{g, tile_row0[k], terms, rows, pitch};
-        a.g.tiles = g.tiles + k;
-        grav_fp64_few_terms<<<(tile_nsrc[k] + 255) / 256, 256, 0, st>>>(a);
-        RG_CUDA_CHECK(cudaGetLastError());
-    }
-    FewSumArgs b{terms, rows, group_row0, group_rows, pitch, dev_row_sink, dev_row_nsrc, g.ax, g.ay, g.az};
+    if (g.n_tiles <= 0 || rows <= 0 || group_rows <= 0 || max_src <= 0) return 0;
+    FewArgs a{g, tile_row0, terms, rows, pitch};
+    grav_fp64_few_terms<<<dim3((max_src + 255) / 256, g.n_tiles), 256, 0, st>>>(a);
+    RG_CUDA_CHECK(cudaGetLastError());
+    FewSumArgs b{terms, rows, group_row0, group_rows, pitch, dev_row_sink, dev_row_nsrc, dev_row_sys, g.sys_active,
+                 g.ax, g.ay, g.az};
     if (serial)
         few_sum_serial<<<(3 * group_rows + 127) / 128, 128, 0, st>>>(b);
     else

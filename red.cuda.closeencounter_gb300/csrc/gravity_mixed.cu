@@ -117,9 +117,10 @@ __device__ __forceinline__ void exact_event_tests(const GravArgs& g, const Tile&
         if (!(kind == 0 ? rad : hill)) continue;
         const EventBuf& eb = kind == 0 ? g.ev : g.hv;
         unsigned int slot = atomicAdd(eb.count, 1u);
+        if (kind == 0 && g.sys_events) atomicAdd(&g.sys_events[tile.sys], 1u);
         if (slot < eb.cap) {
             DevEvent* e = &eb.rec[slot];
-            e->seq = g.seq;
+            e->seq = record_seq(g, tile, kind);
             e->kind = kind;
             e->i = i;
             e->j = j;
@@ -251,6 +252,7 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
     __shared__ double s_h[MX_WARPS][3][MX_S];  // per-warp FP64 sums: heavy sources and near pairs
 
     const Tile tile = g.tiles[blockIdx.x];
+    if (g.sys_active && !g.sys_active[tile.sys]) return;
     const int heavy_end = a.heavy_end[blockIdx.x];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int src_lo = tile.src_begin + blockIdx.y * a.chunk;
@@ -389,9 +391,10 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
 
 // a_i = sum over source chunks of the partials, in chunk order
 __global__ void mixed_reduce_kernel(const double* __restrict__ partial, int n_chunks, int n_part, const Tile* tiles,
-                                    int n_tiles, double* ax, double* ay, double* az)
+                                    int n_tiles, const int* sys_active, double* ax, double* ay, double* az)
 {
     const Tile tile = tiles[blockIdx.x];
+    if (sys_active && !sys_active[tile.sys]) return;
     const int i = tile.sink_begin + threadIdx.x;
     if (i >= tile.sink_end) return;
     for (int comp = 0; comp < 3; comp++) {
@@ -429,7 +432,8 @@ int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* hea
         grav_mixed_kernel<false><<<grid, 256, 0, st>>>(a);
     RG_CUDA_CHECK(cudaGetLastError());
     if (n_chunks > 1) {
-        mixed_reduce_kernel<<<g.n_tiles, MX_S, 0, st>>>(partial, n_chunks, n_part, g.tiles, g.n_tiles, g.ax, g.ay, g.az);
+        mixed_reduce_kernel<<<g.n_tiles, MX_S, 0, st>>>(partial, n_chunks, n_part, g.tiles, g.n_tiles, g.sys_active,
+                                                        g.ax, g.ay, g.az);
         RG_CUDA_CHECK(cudaGetLastError());
     }
     return 0;

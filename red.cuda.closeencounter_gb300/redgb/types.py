@@ -96,6 +96,24 @@ class Profile(ctypes.Structure):
                 ("stage_launches", ctypes.c_int64), ("stage_ms", ctypes.c_double)]
 
 
+STEP_REC = np.dtype([("sys", "<i4"), ("accepted", "<i4"), ("proposed", "<i4"), ("step", "<i4"), ("dt", "<f8"),
+                     ("err", "<f8"), ("feat", "<f4", 8)], align=True)
+assert STEP_REC.itemsize == 64
+
+SYS_RUNNING, SYS_HELD, SYS_DONE, SYS_ERROR = 0, 1, 2, 3
+
+
+class EnsStats(ctypes.Structure):
+    """rg_ens_stats_t."""
+    _fields_ = [("t_day", ctypes.c_double), ("dt_try_day", ctypes.c_double), ("dt_did_day", ctypes.c_double),
+                ("n_tried_step", ctypes.c_int64), ("n_passed_step", ctypes.c_int64), ("n_failed_step", ctypes.c_int64),
+                ("status", ctypes.c_int32), ("n_total", ctypes.c_int32), ("n_proposed", ctypes.c_int64),
+                ("n_proposal_accepted", ctypes.c_int64), ("n_fallback", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 def ptr(a):
     """ctypes void pointer to a contiguous numpy array (or None)."""
     if a is None:

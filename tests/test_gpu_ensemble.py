@@ -1,0 +1,101 @@
+"""Ensemble (many disks, one GPU): every disk reproduces the FP64 oracle bit for bit when
+the oracle replays the trial steps the ensemble's device controller chose (the device pow
+may round differently from glibc's, so the step sizes are the only free input)."""
+import numpy as np
+import pytest
+
+import helpers as H
+import pyoracle
+from redgb import bodies, types as T
+from redgb.ensemble import Ensemble
+
+pytestmark = pytest.mark.gpu
+
+
+def _replay_check(ens, disks, thr, log, events=None):
+    for s, disk in enumerate(disks):
+        mine = log[log["sys"] == s]
+        assert len(mine) > 0
+        st = ens.stats(s)
+        assert st["n_tried_step"] == len(mine)
+        assert st["n_passed_step"] == int(mine["accepted"].sum())
+        o = pyoracle.OracleSystem(disk, thr[s] if np.ndim(thr) == 2 else thr)
+        o.set_integrator(T.INT_RKF78, 0.001, True, 1e-10)
+        o.set_dt_replay(mine["dt"])
+        n_steps = st["n_passed_step"]
+        o.advance(1e30, max_steps=n_steps)
+        rg, vg, pg, mg, tg = ens.state(s)
+        ro, vo, po, mo, to = o.state()
+        # inactive bodies stay in the ensemble's storage; the oracle compacts them away
+        act = (mg["id"] > 0)
+        assert np.array_equal(mg["id"][act], mo["id"][mo["id"] > 0])
+        for f in "xyz":
+            assert H.same(rg[f][act], ro[f][mo["id"] > 0]), (s, f)
+            assert H.same(vg[f][act], vo[f][mo["id"] > 0]), (s, f)
+        assert tg == to
+
+
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_ensemble_replay_bit_exact(gpulib, use_graph):
+    disks = [bodies.make_disk(n_pl=120 + 60 * k, seed=30 + k, giant_scale=(0.5 + 0.4 * k, 1.0)) for k in range(3)]
+    disks.append(bodies.make_disk(n_pl=80, pl_type=T.BODY_PROTOPLANET, seed=40, m_range=(1e-9, 1e-7), giants=()))
+    thr = bodies.thresholds(collision_factor=0.0)
+    ens = Ensemble(disks, thr)
+    ens.set_integrator(0.001, 1e-10)
+    ens.set_options(use_graph=use_graph)
+    ens.set_step_log(1 << 16)
+    ens.advance(40.0)
+    log = ens.step_log()
+    _replay_check(ens, disks, thr, log)
+    for s in range(len(disks)):
+        assert ens.stats(s)["status"] == T.SYS_DONE
+
+
+def test_ensemble_collisions_match_oracle(gpulib):
+    """The reference's collision-merge run as a one-disk ensemble next to a second disk:
+    merges, their event records and the resulting states match the oracle."""
+    disk, params, _, ref_events = H.load_fixture("disk_si_rkf78_collide")
+    other = bodies.make_disk(n_pl=64, seed=9)
+    thr = np.stack([H.thresholds_of(params), H.thresholds_of(params)])
+    ens = Ensemble([disk, other], thr)
+    ens.set_integrator(0.001, 1e-10)
+    ens.set_step_log(1 << 18)
+    ens.advance(0.5 * T.YEAR)
+    log = ens.step_log()
+    ev, sysv = ens.events()
+    mine = ev[sysv == 0]
+    # replay disk 0 in the oracle's full loop (with its merges and compactions)
+    o = pyoracle.OracleSystem(disk, thr[0])
+    o.set_integrator(T.INT_RKF78, 0.001, True, 1e-10)
+    d0 = log[log["sys"] == 0]
+    o.set_dt_replay(d0["dt"])
+    o.advance(1e30, max_steps=ens.stats(0)["n_passed_step"])
+    eo = o.events()
+    assert len(mine) == len(eo) and len(eo) > 0
+    for a, b in zip(mine, eo):
+        assert (a["event_name"], a["id1"], a["id2"]) == (b["event_name"], b["id1"], b["id2"])
+        assert H.same(a["t"], b["t"]) and H.same(a["d"], b["d"])
+        for f in ("rs", "vs"):
+            for c in "xyz":
+                assert H.same(a[f][c], b[f][c])
+    rg, vg, pg, mg, tg = ens.state(0)
+    ro, vo, po, mo, to = o.state()
+    act_g, act_o = mg["id"] > 0, mo["id"] > 0
+    assert np.array_equal(mg["id"][act_g], mo["id"][act_o])
+    for f in "xyz":
+        assert H.same(rg[f][act_g], ro[f][act_o])
+
+
+def test_ensemble_mixed_and_energy(gpulib):
+    disks = [bodies.config_disk("ensemble_member", seed=s, n=600) for s in (1, 2, 3)]
+    ens = Ensemble(disks, bodies.thresholds(collision_factor=0.0))
+    ens.set_integrator(0.001, 1e-10)
+    ens.set_options(gravity_mode=T.GRAVITY_MIXED, hill_factor=3.0)
+    E0 = [ens.energy(s)[0] for s in range(3)]
+    ens.advance(365.25)
+    for s in range(3):
+        E1 = ens.energy(s)[0]
+        assert abs((E1 - E0[s]) / E0[s]) < 1e-10
+        assert ens.stats(s)["status"] == T.SYS_DONE
+    n_k, n_g = ens.kernel_count()
+    assert n_g > 0 and n_k > n_g
