@@ -256,6 +256,55 @@ RG_API int rg_ens_energy(rg_ens* ens, int sys, double* energy, double angmom[3])
 RG_API int rg_ens_get_stream(rg_ens* ens, void** stream);
 RG_API int rg_ens_kernel_count(rg_ens* ens, int64_t* n_kernels, int64_t* n_graph_launches);
 
+/* ------------------------------------------------------------------ learned step proposer */
+
+/*
+ * A small perceptron (8 inputs -> 64 -> 64 -> 1, SiLU, BF16 weights, FP32 accumulation)
+ * that proposes each disk's next trial step from features the integrator logs (not in the
+ * reference).  Trained on the GPU by the library's own forward / backward / AdamW kernels.
+ * Parameter vector layout (RG_MLP_NPARAM FP32 values): W1[64][8] b1[64] W2[64][64] b2[64]
+ * w3[64] b3.  Inputs are standardised with (x - mean) / std before the first layer.
+ */
+#define RG_MLP_IN 8
+#define RG_MLP_NPARAM 4801
+typedef struct rg_mlp rg_mlp;
+
+RG_API int rg_mlp_create(uint64_t seed, rg_mlp** out);
+RG_API int rg_mlp_destroy(rg_mlp* mlp);
+RG_API int rg_mlp_set_normalisation(rg_mlp* mlp, const float mean[RG_MLP_IN], const float stdev[RG_MLP_IN]);
+RG_API int rg_mlp_get_normalisation(rg_mlp* mlp, float mean[RG_MLP_IN], float stdev[RG_MLP_IN]);
+RG_API int rg_mlp_get_params(rg_mlp* mlp, float* params, int n);
+RG_API int rg_mlp_set_params(rg_mlp* mlp, const float* params, int n);
+/* predictions for n samples (x: n x RG_MLP_IN, raw features) */
+RG_API int rg_mlp_forward(rg_mlp* mlp, const float* x, int n, float* y);
+/* gradient of the mean squared error over the n samples (no update) */
+RG_API int rg_mlp_gradient(rg_mlp* mlp, const float* x, const float* y, int n, float* grads, float* loss);
+/* AdamW over `epochs` shuffled passes in minibatches of `batch` */
+RG_API int rg_mlp_train(rg_mlp* mlp, const float* x, const float* y, int n, int epochs, int batch, float lr,
+                        float weight_decay, uint64_t seed, float* final_loss);
+
+/*
+ * Attaches a trained network to an ensemble (NULL detaches).  The network predicts
+ * log(ideal step / last ideal step), where a step's ideal size is the one the controller's
+ * error model says meets the tolerance exactly, dt * (tol / err)^(1/8).  At the start of
+ * every step a disk's trial step becomes safety * last ideal step * exp(network(features)),
+ * bounded to [1/2, 2] times the plain controller's own estimate; the embedded RKF error
+ * estimate accepts or rejects it, a rejected attempt retries with the plain controller's
+ * step, and after two steps in a row whose proposals were rejected the disk uses the plain
+ * controller alone for `cooldown` steps.  Features (rg_step_rec_t.feat): log10 min(d /
+ * mutual Hill radius) over pairs with a massive non-star body, log10 max |a|, log10 last
+ * accepted dt [day], log10 last error / tolerance, last attempt accepted (0/1), log of the
+ * last three ratios of consecutive ideal steps.
+ */
+RG_API int rg_ens_set_proposer(rg_ens* ens, rg_mlp* mlp, double safety, int cooldown);
+/*
+ * Training-data collection: every step whose trial size comes from the plain controller
+ * starts from that size times exp(sigma * u), u uniform in [-1, 1) from (seed, disk, step),
+ * so that the attempt log covers error ratios away from the plain controller's fixed point.
+ * The error estimate still accepts or rejects every attempt.  sigma in [0, 1]; 0 is off.
+ */
+RG_API int rg_ens_set_dither(rg_ens* ens, double sigma, uint64_t seed);
+
 /* ------------------------------------------------------------------ measurement */
 
 /* The CUDA stream (cudaStream_t) the context launches on, for callers that time or

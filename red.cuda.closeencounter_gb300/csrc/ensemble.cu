@@ -33,9 +33,13 @@
 #include "host_tools.h"
 #include "kernels.h"
 #include "rk_tables.h"
+#include "mlp.h"
+#include <cuda_bf16.h>
 
 namespace redgb {
 int set_error(int code, const std::string& msg);
+const void* mlp_device_weights(const rg_mlp* m);
+void mlp_normalisation(const rg_mlp* m, float* mean, float* stdev);
 
 // bodies [b0, b1) of disk `sys`; the error norm covers [b0, e1)
 struct StageTile {
@@ -157,6 +161,21 @@ struct EnsSys {
     rg_step_rec_t* log;      // attempt log (nullptr: off)
     unsigned int* log_count;
     unsigned int log_cap;
+    // learned proposer: per-disk history and features
+    float* feat;             // n x 8, features of the current step
+    double* dt_last;         // last accepted step
+    double* ideal_last;      // the error model's ideal step for the last accepted step
+    float* hist;             // n x 5: err_last, acc_last, ir0, ir1, ir2 (log ideal-step ratios)
+    int* proposed;           // the current attempt's step came from the network
+    int* step_prop_rej;      // a proposal of the current step was rejected
+    int* prop_rej_steps;     // consecutive steps with a rejected proposal
+    int* cool;               // steps left on the plain controller
+    long long* n_prop;
+    long long* n_prop_acc;
+    long long* n_fallback;
+    int cooldown;
+    float dither;                    // > 0: plain trial steps scaled by exp(dither * U[-1, 1))
+    unsigned long long dither_seed;
 };
 
 // the controller of rungekutta8::step, one thread per disk
@@ -172,27 +191,58 @@ __global__ void ens_controller_kernel(EnsSys s)
     const double dt = s.dt_try[d];
     const double max_err = fabs(dt * (41.0 / 840.0) * raw);
     const double new_dt = dt * (0.9 * pow(s.tol / max_err, 1.0 / 8.0));
+    const bool accepted = !(max_err > s.tol);
+    const int proposed = s.proposed[d];
     if (s.log) {
         const unsigned int slot = atomicAdd(s.log_count, 1u);
         if (slot < s.log_cap) {
             rg_step_rec_t& rec = s.log[slot];
             rec.sys = d;
-            rec.accepted = !(max_err > s.tol);
-            rec.proposed = 0;
+            rec.accepted = accepted;
+            rec.proposed = proposed;
             rec.step = (int)s.n_passed[d];
             rec.dt = dt;
             rec.err = max_err;
-            for (int q = 0; q < 8; q++) rec.feat[q] = 0.0f;
+            for (int q = 0; q < 8; q++) rec.feat[q] = s.feat[8 * d + q];
         }
     }
     s.n_tried[d]++;
-    if (!(max_err > s.tol)) {
+    float* h = s.hist + 5 * d;
+    h[0] = (float)log10(max_err / s.tol);
+    h[1] = accepted ? 1.0f : 0.0f;
+    if (proposed) {
+        s.n_prop[d]++;
+        if (accepted) s.n_prop_acc[d]++;
+        else s.step_prop_rej[d] = 1;
+    }
+    s.proposed[d] = 0;
+    if (accepted) {
         s.t_prev[d] = s.t[d];
         s.t[d] = s.t[d] + dt;
         s.dt_did[d] = dt;
         s.n_passed[d]++;
         s.acc[d] = 1;
         s.acc_attempt[d] = s.attempt[d];
+        // the step that would have met the tolerance exactly (the error scales as dt^8)
+        const double ideal = max_err > 0.0 ? dt * pow(s.tol / max_err, 1.0 / 8.0) : 8.0 * dt;
+        const double last = s.ideal_last[d];
+        h[4] = h[3];
+        h[3] = h[2];
+        h[2] = last > 0.0 && isfinite(ideal) ? fminf(fmaxf((float)log(ideal / last), -3.0f), 3.0f) : 0.0f;
+        s.dt_last[d] = dt;
+        if (isfinite(ideal)) s.ideal_last[d] = ideal;
+        // fallback: two steps in a row whose proposals were rejected
+        if (s.step_prop_rej[d]) {
+            if (++s.prop_rej_steps[d] >= 2) {
+                s.cool[d] = s.cooldown;
+                s.prop_rej_steps[d] = 0;
+                s.n_fallback[d]++;
+            }
+        } else if (proposed) {
+            s.prop_rej_steps[d] = 0;
+        }
+        s.step_prop_rej[d] = 0;
+        if (s.cool[d] > 0) s.cool[d]--;
     } else {
         s.n_failed[d]++;
         s.acc[d] = 0;
@@ -239,6 +289,138 @@ __global__ void ens_finalize_kernel(EnsSys s)
     s.events[d] = 0;
     s.ej[d] = 0;
     s.max_bits[d] = 0ull;
+}
+
+// features of a step start: max |a| and min (d / mutual Hill radius)^3 over the pairs of
+// every body with a massive non-star self-interacting body (float bits: positive floats
+// order like unsigned integers)
+__global__ void ens_feat_reset_kernel(EnsSys s, unsigned int* amax, unsigned int* hill3)
+{
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= s.n || !s.active_f0[d]) return;
+    amax[d] = 0u;
+    hill3[d] = __float_as_uint(3.0e38f);
+}
+
+__global__ void ens_feat_kernel(const StageTile* tiles, const int* mask, const double* y, const double* k0,
+                                const double* mass, const int* id, const int* base_of, const int* nsi_of, int stride,
+                                unsigned int* amax, unsigned int* hill3)
+{
+    const StageTile t = tiles[blockIdx.x];
+    if (!mask[t.sys]) return;
+    float am = 0.0f, h3 = 3.0e38f;
+    for (int i = t.b0 + threadIdx.x; i < t.b1; i += blockDim.x) {
+        if (id[i] <= 0) continue;
+        const double ax = k0[3LL * stride + i], ay = k0[4LL * stride + i], az = k0[5LL * stride + i];
+        am = fmaxf(am, (float)sqrt(ax * ax + ay * ay + az * az));
+        const int b = base_of[i], ns = nsi_of[i];
+        const double M = mass[b];
+        const double x0 = y[b], y0 = y[stride + b], z0 = y[2LL * stride + b];
+        const double xi = y[i], yi = y[stride + i], zi = y[2LL * stride + i];
+        const double ri = sqrt((xi - x0) * (xi - x0) + (yi - y0) * (yi - y0) + (zi - z0) * (zi - z0));
+        for (int j = b + 1; j < b + ns; j++) {
+            if (j == i || id[j] <= 0) continue;
+            const double xj = y[j], yj = y[stride + j], zj = y[2LL * stride + j];
+            const double dx = xj - xi, dy = yj - yi, dz = zj - zi;
+            const double d2 = dx * dx + dy * dy + dz * dz;
+            const double rj = sqrt((xj - x0) * (xj - x0) + (yj - y0) * (yj - y0) + (zj - z0) * (zj - z0));
+            const double hh = 0.5 * (ri + rj);
+            const double rh3 = (mass[i] + mass[j]) / (3.0 * M) * hh * hh * hh;
+            if (rh3 > 0.0) h3 = fminf(h3, (float)(d2 * sqrt(d2) / rh3));
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, off));
+        h3 = fminf(h3, __shfl_xor_sync(0xffffffffu, h3, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&amax[t.sys], __float_as_uint(am));
+        atomicMin(&hill3[t.sys], __float_as_uint(h3));
+    }
+}
+
+struct PropArgs {
+    EnsSys s;
+    const unsigned int* amax;
+    const unsigned int* hill3;
+    const __nv_bfloat16* w;  // nullptr: features only
+    float mean[8], inv_std[8];
+    float safety;
+};
+
+// uniform in [-1, 1) from (seed, disk, step): splitmix64 finaliser
+__device__ __forceinline__ double dither_uniform(unsigned long long seed, int d, long long step)
+{
+    unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (((unsigned long long)(unsigned)d << 40) ^ (unsigned long long)step);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+}
+
+// one warp per disk that starts a step: features -> network -> trial step
+__global__ void __launch_bounds__(128) ens_propose_kernel(PropArgs a)
+{
+    const int d = blockIdx.x * 4 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    const EnsSys& s = a.s;
+    if (d >= s.n || !s.active_f0[d]) return;
+    const float* h = s.hist + 5 * d;
+    float f[8];
+    const float am = __uint_as_float(a.amax[d]);
+    const float h3 = __uint_as_float(a.hill3[d]);
+    f[0] = h3 < 1.0e38f ? log10f(fmaxf(h3, 1e-30f)) / 3.0f : 6.0f;
+    f[1] = log10f(fmaxf(am, 1e-30f));
+    f[2] = s.dt_last[d] > 0.0 ? (float)log10(s.dt_last[d] / 1.720209895e-2) : -3.0f;
+    f[3] = h[0];
+    f[4] = h[1];
+    f[5] = h[2];
+    f[6] = h[3];
+    f[7] = h[4];
+    if (lane < 8) s.feat[8 * d + lane] = f[lane];
+    if (!a.w || s.cool[d] > 0 || s.n_passed[d] < 4 || !(s.ideal_last[d] > 0.0)) {
+        if (lane == 0 && s.dither > 0.0f)
+            s.dt_try[d] *= exp((double)s.dither * dither_uniform(s.dither_seed, d, s.n_passed[d]));
+        return;
+    }
+    float x[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) x[q] = fminf(fmaxf((f[q] - a.mean[q]) * a.inv_std[q], -6.0f), 6.0f);
+    // hidden layer 1: lane owns units lane and lane + 32
+    float h1[2];
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        const int u = lane + 32 * r;
+        float z = __bfloat162float(a.w[MLP_OFF_B1 + u]);
+#pragma unroll
+        for (int q = 0; q < 8; q++) z = fmaf(__bfloat162float(a.w[MLP_OFF_W1 + u * 8 + q]), x[q], z);
+        h1[r] = z / (1.0f + __expf(-z));
+    }
+    float h2[2];
+#pragma unroll
+    for (int r = 0; r < 2; r++) {
+        const int u = lane + 32 * r;
+        float z = __bfloat162float(a.w[MLP_OFF_B2 + u]);
+        for (int v = 0; v < 64; v++) {
+            const float hv = __shfl_sync(0xffffffffu, h1[v >> 5], v & 31);
+            z = fmaf(__bfloat162float(a.w[MLP_OFF_W2 + u * 64 + v]), hv, z);
+        }
+        h2[r] = z / (1.0f + __expf(-z));
+    }
+    float o = __bfloat162float(a.w[MLP_OFF_W3 + lane]) * h2[0] + __bfloat162float(a.w[MLP_OFF_W3 + lane + 32]) * h2[1];
+    for (int off = 16; off > 0; off >>= 1) o += __shfl_xor_sync(0xffffffffu, o, off);
+    o += __bfloat162float(a.w[MLP_OFF_B3]);
+    if (lane == 0 && isfinite(o)) {
+        // the network predicts log(ideal step / last ideal step); the plain controller bounds
+        // the proposal to [1/2, 2] of its own estimate
+        const double plain = s.dt_try[d];
+        double dt = (double)a.safety * s.ideal_last[d] * exp((double)o);
+        dt = fmin(fmax(dt, 0.5 * plain), 2.0 * plain);
+        if (isfinite(dt) && dt > 0.0) {
+            s.dt_try[d] = dt;
+            s.proposed[d] = 1;
+        }
+    }
 }
 
 // per-body energy partials of an ensemble (as energy_kernel, with disk offsets)
@@ -364,6 +546,21 @@ struct rg_ens {
     unsigned int* d_log_count = nullptr;
     unsigned int log_cap = 0;
     std::vector<rg_step_rec_t> host_log;
+    // learned proposer
+    float* d_feat = nullptr;
+    double* d_dt_last = nullptr;
+    double* d_ideal_last = nullptr;
+    float* d_hist = nullptr;
+    int *d_proposed = nullptr, *d_step_prop_rej = nullptr, *d_prop_rej_steps = nullptr, *d_cool = nullptr;
+    long long *d_nprop = nullptr, *d_nprop_acc = nullptr, *d_nfallback = nullptr;
+    unsigned int *d_amax = nullptr, *d_hill3 = nullptr;
+    int* d_nsi_of = nullptr;
+    const rg_mlp* mlp = nullptr;
+    float mlp_mean[8] = {0}, mlp_inv_std[8] = {1, 1, 1, 1, 1, 1, 1, 1};
+    float safety = 0.95f;
+    int cooldown = 16;
+    float dither = 0.0f;
+    unsigned long long dither_seed = 0;
 
     int n_si(int s) const { return cnt[s][0] + cnt[s][1] + cnt[s][2] + cnt[s][3]; }
     int n_massive(int s) const { return n_si(s) + cnt[s][4] + cnt[s][5]; }
@@ -371,7 +568,9 @@ struct rg_ens {
     {
         return EnsSys{n_sys, d_status, d_active, d_active_f0, d_acc, d_ej, d_sys_events, d_maxbits, d_t, d_tprev,
                       d_tstop, d_dt_try, d_dt_did, d_ntried, d_npassed, d_nfailed, d_attempt, d_acc_attempt, d_nf0,
-                      tol, d_log, d_log_count, log_cap};
+                      tol, d_log, d_log_count, log_cap, d_feat, d_dt_last, d_ideal_last, d_hist, d_proposed,
+                      d_step_prop_rej, d_prop_rej_steps, d_cool, d_nprop, d_nprop_acc, d_nfallback, cooldown,
+                      dither, dither_seed};
     }
 };
 
@@ -405,7 +604,9 @@ void free_all(rg_ens* e)
                     e->d_ntried, e->d_npassed, e->d_nfailed, e->d_attempt, e->d_acc_attempt, e->d_nf0, e->d_stiles,
                     e->d_tiles, e->d_heavy, e->d_few_row0, e->d_row_sink, e->d_row_nsrc, e->d_row_sys, e->d_terms,
                     e->d_ev, e->d_ev_count, e->d_hill, e->d_hill_count, e->d_part, e->d_base_of, e->d_log,
-                    e->d_log_count};
+                    e->d_log_count, e->d_feat, e->d_dt_last, e->d_ideal_last, e->d_hist, e->d_proposed, e->d_step_prop_rej,
+                    e->d_prop_rej_steps, e->d_cool, e->d_nprop, e->d_nprop_acc, e->d_nfallback, e->d_amax,
+                    e->d_hill3, e->d_nsi_of};
     for (void* q : ptrs) cudaFree(q);
     for (auto& k : e->d_k) cudaFree(k);
     if (e->st) cudaStreamDestroy(e->st);
@@ -677,6 +878,25 @@ int record_attempt(rg_ens* e)
     e->n_kernels++;
     int rc = ens_gravity(e, e->d_y, e->d_y + 3 * cap, e->d_k[0] + 3 * cap, 0, e->d_active_f0, e->hill_factor > 0.0);
     if (rc) return rc;
+    if (e->d_log || e->mlp || e->dither > 0.0f) {
+        // step-start features (and, with a network attached, the proposed trial step)
+        ens_feat_reset_kernel<<<nb, 128, 0, e->st>>>(e->sys(), e->d_amax, e->d_hill3);
+        ens_feat_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active_f0, e->d_y, e->d_k[0], e->d_mass, e->d_id,
+                                              e->d_base_of, e->d_nsi_of, e->cap, e->d_amax, e->d_hill3);
+        PropArgs pa{};
+        pa.s = e->sys();
+        pa.amax = e->d_amax;
+        pa.hill3 = e->d_hill3;
+        pa.w = (const __nv_bfloat16*)mlp_device_weights(e->mlp);
+        for (int q = 0; q < 8; q++) {
+            pa.mean[q] = e->mlp_mean[q];
+            pa.inv_std[q] = e->mlp_inv_std[q];
+        }
+        pa.safety = e->safety;
+        ens_propose_kernel<<<(e->n_sys + 3) / 4, 128, 0, e->st>>>(pa);
+        RG_CUDA_CHECK(cudaGetLastError());
+        e->n_kernels += 3;
+    }
     for (int r = 1; r <= 12 && !rc; r++) {
         double a[9];
         for (int q = 0; q < rk8_nterm[r]; q++) a[q] = rk8_a[rk8_aidx[r][q]];
@@ -1052,6 +1272,20 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     chk(dalloc(&e->d_attempt, ns));
     chk(dalloc(&e->d_acc_attempt, ns));
     chk(dalloc(&e->d_nf0, ns));
+    chk(dalloc(&e->d_feat, 8 * ns));
+    chk(dalloc(&e->d_dt_last, ns));
+    chk(dalloc(&e->d_ideal_last, ns));
+    chk(dalloc(&e->d_hist, 5 * ns));
+    chk(dalloc(&e->d_proposed, ns));
+    chk(dalloc(&e->d_step_prop_rej, ns));
+    chk(dalloc(&e->d_prop_rej_steps, ns));
+    chk(dalloc(&e->d_cool, ns));
+    chk(dalloc(&e->d_nprop, ns));
+    chk(dalloc(&e->d_nprop_acc, ns));
+    chk(dalloc(&e->d_nfallback, ns));
+    chk(dalloc(&e->d_amax, ns));
+    chk(dalloc(&e->d_hill3, ns));
+    chk(dalloc(&e->d_nsi_of, nt));
     chk(dalloc(&e->d_ev, e->ev_cap));
     chk(dalloc(&e->d_ev_count, 1));
     chk(dalloc(&e->d_hill, e->ev_cap));
@@ -1114,6 +1348,15 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     chk(upload(e, e->d_id, id));
     chk(upload(e, e->d_type, ty));
     chk(upload(e, e->d_base_of, base_of));
+    {
+        std::vector<int> nsi_of(nt);
+        for (int s2 = 0; s2 < n_sys; s2++)
+            for (int j = 0; j < e->ntot[s2]; j++) nsi_of[(size_t)e->base[s2] + j] = e->n_si(s2);
+        chk(upload(e, e->d_nsi_of, nsi_of));
+        std::vector<float> zf(8 * ns, 0.0f), zh(5 * ns, 0.0f);
+        chk(upload(e, e->d_feat, zf));
+        chk(upload(e, e->d_hist, zh));
+    }
     chk(upload(e, e->d_thr, e->thr));
     std::vector<int> zi(ns, 0);
     std::vector<double> zd(ns, 0.0);
@@ -1134,6 +1377,15 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     chk(upload(e, e->d_nf0, zu));
     chk(upload(e, e->d_sys_events, zu));
     chk(upload(e, e->d_maxbits, zb));
+    chk(upload(e, e->d_dt_last, zd));
+    chk(upload(e, e->d_ideal_last, zd));
+    chk(upload(e, e->d_proposed, zi));
+    chk(upload(e, e->d_step_prop_rej, zi));
+    chk(upload(e, e->d_prop_rej_steps, zi));
+    chk(upload(e, e->d_cool, zi));
+    chk(upload(e, e->d_nprop, zl));
+    chk(upload(e, e->d_nprop_acc, zl));
+    chk(upload(e, e->d_nfallback, zl));
     if (!rc && cudaMemsetAsync(e->d_ev_count, 0, sizeof(unsigned int), e->st) != cudaSuccess) chk(RG_ERR_CUDA);
     if (!rc && cudaMemsetAsync(e->d_hill_count, 0, sizeof(unsigned int), e->st) != cudaSuccess) chk(RG_ERR_CUDA);
     if (!rc && cudaStreamSynchronize(e->st) != cudaSuccess) chk(set_error(RG_ERR_CUDA, "upload"));
@@ -1371,6 +1623,14 @@ int stats_impl(rg_ens* e, int s, rg_ens_stats_t* o)
     o->n_failed_step = c;
     o->status = st;
     o->n_total = e->ntot[s];
+    long long pr, pa, fb;
+    RG_CUDA_CHECK(cudaMemcpyAsync(&pr, e->d_nprop + s, sizeof(long long), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&pa, e->d_nprop_acc + s, sizeof(long long), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&fb, e->d_nfallback + s, sizeof(long long), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    o->n_proposed = pr;
+    o->n_proposal_accepted = pa;
+    o->n_fallback = fb;
     return RG_OK;
 }
 
@@ -1529,6 +1789,33 @@ int rg_ens_energy(rg_ens* e, int sys, double* energy, double angmom[3])
 {
     if (!e || sys < 0 || sys >= e->n_sys) return set_error(RG_ERR_ARG, "bad disk index");
     RG_GUARD(energy_impl(e, sys, energy, angmom));
+}
+
+int rg_ens_set_proposer(rg_ens* e, rg_mlp* mlp, double safety, int cooldown)
+{
+    if (!e || (mlp && !(safety > 0.0 && safety <= 1.5)) || cooldown < 0) return set_error(RG_ERR_ARG, "bad argument");
+    e->mlp = mlp;
+    if (mlp) {
+        float mean[8], sd[8];
+        redgb::mlp_normalisation(mlp, mean, sd);
+        for (int q = 0; q < 8; q++) {
+            e->mlp_mean[q] = mean[q];
+            e->mlp_inv_std[q] = 1.0f / sd[q];
+        }
+        e->safety = (float)safety;
+        e->cooldown = cooldown;
+    }
+    e->graph_valid = false;
+    return RG_OK;
+}
+
+int rg_ens_set_dither(rg_ens* e, double sigma, uint64_t seed)
+{
+    if (!e || !(sigma >= 0.0 && sigma <= 1.0)) return set_error(RG_ERR_ARG, "dither must be in [0, 1]");
+    e->dither = (float)sigma;
+    e->dither_seed = (unsigned long long)seed;
+    e->graph_valid = false;
+    return RG_OK;
 }
 
 int rg_ens_get_stream(rg_ens* e, void** stream)

@@ -269,26 +269,56 @@ struct FewSumArgs {
     double* az;
 };
 
-// exact: one thread per (row, component), ascending source order
-__global__ void few_sum_serial(FewSumArgs a)
+// exact: one warp per (row, component).  The warp streams the row through shared memory
+// in coalesced chunks (the next chunk's loads are in flight while lane 0 adds the current
+// one) and lane 0 adds the terms in ascending source order -- the reference's serial sum.
+constexpr int SUM_CHUNK = 256;
+
+__global__ void __launch_bounds__(128) few_sum_serial(FewSumArgs a)
 {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ double buf[4][2][SUM_CHUNK];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int t = blockIdx.x * 4 + warp;
     if (t >= 3 * a.nrows) return;
     const int comp = t / a.nrows, row = a.row0 + t % a.nrows;
     if (a.sys_active && !a.sys_active[a.row_sys[row]]) return;
     const double* T = a.terms + ((long long)comp * a.rows + row) * a.pitch;
     const int n = a.row_nsrc[row];
+    double (*B)[SUM_CHUNK] = buf[warp];
+    double reg[SUM_CHUNK / 32];
+    auto load = [&](int c0) {
+#pragma unroll
+        for (int k = 0; k < SUM_CHUNK / 32; k++) {
+            const int q = c0 + k * 32 + lane;
+            reg[k] = q < n ? T[q] : 0.0;
+        }
+    };
     double acc = 0.0;
-    int q = 0;
-    for (; q + 8 <= n; q += 8) {
-        const double t0 = T[q], t1 = T[q + 1], t2 = T[q + 2], t3 = T[q + 3];
-        const double t4 = T[q + 4], t5 = T[q + 5], t6 = T[q + 6], t7 = T[q + 7];
-        acc = acc + t0; acc = acc + t1; acc = acc + t2; acc = acc + t3;
-        acc = acc + t4; acc = acc + t5; acc = acc + t6; acc = acc + t7;
+    int cur = 0;
+    load(0);
+    for (int c0 = 0; c0 < n; c0 += SUM_CHUNK) {
+#pragma unroll
+        for (int k = 0; k < SUM_CHUNK / 32; k++) B[cur][k * 32 + lane] = reg[k];
+        __syncwarp();
+        if (c0 + SUM_CHUNK < n) load(c0 + SUM_CHUNK);
+        if (lane == 0) {
+            const int m = min(SUM_CHUNK, n - c0);
+            int q = 0;
+            for (; q + 8 <= m; q += 8) {
+                const double t0 = B[cur][q], t1 = B[cur][q + 1], t2 = B[cur][q + 2], t3 = B[cur][q + 3];
+                const double t4 = B[cur][q + 4], t5 = B[cur][q + 5], t6 = B[cur][q + 6], t7 = B[cur][q + 7];
+                acc = acc + t0; acc = acc + t1; acc = acc + t2; acc = acc + t3;
+                acc = acc + t4; acc = acc + t5; acc = acc + t6; acc = acc + t7;
+            }
+            for (; q < m; q++) acc = acc + B[cur][q];
+        }
+        __syncwarp();
+        cur ^= 1;
     }
-    for (; q < n; q++) acc = acc + T[q];
-    double* out = comp == 0 ? a.ax : (comp == 1 ? a.ay : a.az);
-    out[a.row_sink[row]] = acc;
+    if (lane == 0) {
+        double* out = comp == 0 ? a.ax : (comp == 1 ? a.ay : a.az);
+        out[a.row_sink[row]] = acc;
+    }
 }
 
 // mixed-precision heavy rows: one CTA per (row, component), compensated tree reduction
@@ -355,7 +385,7 @@ int launch_grav_fp64_few(const GravArgs& g, const int* tile_row0, int max_src, d
     FewSumArgs b{terms, rows, group_row0, group_rows, pitch, dev_row_sink, dev_row_nsrc, dev_row_sys, g.sys_active,
                  g.ax, g.ay, g.az};
     if (serial)
-        few_sum_serial<<<(3 * group_rows + 127) / 128, 128, 0, st>>>(b);
+        few_sum_serial<<<(3 * group_rows + 3) / 4, 128, 0, st>>>(b);
     else
         few_sum_tree<<<3 * group_rows, 256, 0, st>>>(b);
     RG_CUDA_CHECK(cudaGetLastError());
