@@ -198,6 +198,30 @@ RG_API int rg_get_counters(rg_ctx* ctx, rg_counters_t* c);
  * G = 1), FP64 with compensated sums.  Not in the reference. */
 RG_API int rg_energy(rg_ctx* ctx, double* energy, double angmom[3]);
 
+/*
+ * No counterpart in the reference.  rg_energy for a caller that cannot allocate device
+ * memory -- one that owns a fixed memory budget it has already handed out (an arena or
+ * pool sized at start-up, as a host code that keeps the reference's pp_disk device arrays
+ * does), or that must not let a library call cudaMalloc / cudaFree, which synchronise the
+ * device, in the middle of its loop.  The bodies are the caller's device arrays in the
+ * reference's layouts and internal units (velocities in AU per 1/k days, as pp_disk keeps
+ * them): n_total = the sum of *counts records each of r, v, p and md, in the reference's
+ * body order.  Same results as rg_energy on the same state.
+ *
+ * The call allocates nothing: its scratch is a fixed device array of
+ * RG_ENERGY_NOALLOC_MAX_BODIES bodies (2.5 MiB per device, part of the library image), and
+ * a larger n_total is rejected with RG_ERR_ARG before any device work.  The first call on
+ * each device looks the scratch's address up with that device current; a caller that
+ * captures streams makes that first call before its capture begins.  Nothing in the
+ * scratch needs to start at zero.  There is one scratch per device, so calls on the same
+ * device must not overlap (from two threads, or on two streams with both in flight): they
+ * would race on it.  The work runs on `stream` (NULL: the default stream), which the call
+ * synchronises before it returns the results.
+ */
+#define RG_ENERGY_NOALLOC_MAX_BODIES 65536
+RG_API int rg_energy_noalloc(const rg_counts_t* counts, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,
+                             const rg_body_metadata_t* md, void* stream, double* energy, double angmom[3]);
+
 /* Last step-size values in days: the step that was taken and the next trial step. */
 RG_API int rg_get_dt(rg_ctx* ctx, double* dt_did_day, double* dt_try_day);
 

@@ -32,6 +32,7 @@ UNITS = {
     "gravity_mixed.cu": [],
     "ensemble.cu": ["-fmad=false"],
     "mlp.cu": [],
+    "noalloc.cu": ["-fmad=false"],
 }
 
 
