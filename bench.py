@@ -9,6 +9,16 @@ combinations.  Metric: simulated years per second (and interacting pairs per sec
 
 --impl reference times the FP64 CPU path (the oracle port of the reference's CPU code,
 one core, the reference is single threaded) on the same workload.
+
+The line also carries an "ensemble" section: 256 independent disks (N ~ U[512, 8192],
+giants scaled by U[0.5, 2], seeds 65-320), RKF7(8) at tolerance 1e-10 with per-disk
+adaptive steps, integrated over the same interval in four forms -- learned step proposer +
+mixed-precision gravity + batching (the proposer trained first, untimed, on dithered attempt
+logs of disks with seeds 1-64), the plain controller with mixed gravity, the plain
+controller with FP64 gravity, both batched, and the plain FP64 form one disk at a time
+through the single-disk API (a sample of the disks, the rate scaled to all of them).  Each
+reports aggregate simulated years per second, the largest |dE/E| over the interval, the
+rejected-attempt fraction and the event list.
 """
 import argparse
 import json
@@ -32,6 +42,10 @@ WORKLOADS = {
     "planetesimal_disk_rkf78": ("planetesimal_disk", 1024, T.INT_RKF78, 0.001, True),
 }
 FLOP_PER_PAIR = 36  # the reference's own count (pp_disk.cu:170-184,293)
+# DRAM bytes (read + write) per launch of the dominant kernel of the default workload, from
+# one ncu capture of `python bench.py --no-ensemble --no-cpu-baseline --steps 3 --warmup 3`
+# (profiles/grav_mixed_kernel_self_gravitating_16384.md, .../grav_fp64_pairpar_...md)
+NCU_TRAFFIC = {("self_gravitating_16384_rk4", "mixed"): 1347328, ("self_gravitating_16384_rk4", "fp64"): 819712}
 
 
 def dist_init():
@@ -223,7 +237,9 @@ def run_ours(args, rank, ws, dist):
             "e2e": e2e,
             "gpu_launches": int(launches),
             "roofline": {"bound": "fp32" if kind == 0 else "fp64", "achieved": achieved, "peak": peak,
-                         "unit": "TFLOP/s", "frac": achieved / peak, "traffic": None,
+                         "unit": "TFLOP/s", "frac": achieved / peak,
+                         "traffic": NCU_TRAFFIC.get((args.workload, args.mode)),
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one capture",
                          "kernel": "grav_mixed_kernel" if kind == 0 else "grav_fp64_pairpar",
                          "peak_source": "measured FMA-chain microbenchmark on this GPU (rg_measure_pipe_peak)",
                          "flop_per_pair": FLOP_PER_PAIR, "avg_launch_ms": avg_ms},
@@ -236,6 +252,8 @@ def run_ours(args, rank, ws, dist):
         }
         if ws == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(args, disk, int_type, dt_day, adaptive, samples=args.cpu_steps)
+        if not args.no_ensemble:
+            out["ensemble"] = ensemble_section(args)
     return out
 
 
@@ -281,6 +299,119 @@ def run_reference(args, rank, ws):
             "e2e": {"value": value, "unit": "sim-years/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def ensemble_section(args):
+    """The batched / mixed / learned forms against the plain FP64 form (module docstring)."""
+    import torch
+
+    from redgb import lib
+    from redgb.ensemble import Ensemble
+    from redgb.proposer import dataset_from_log, fit, set_dither
+
+    tol = 1e-10
+    hill = 3.0
+    thr = bodies.thresholds(ejection=100.0, hit_centrum=0.05, collision_factor=1.0)
+    warm_day = 10.0
+    span_day = args.ensemble_years * T.YEAR
+
+    def advance_timed(ens, t_stop):
+        ext = torch.cuda.ExternalStream(ens.stream())
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        n = ens.advance(t_stop)
+        e1.record(ext)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3, n
+
+    # proposer training (untimed): dithered plain-controller logs of seeds 1-64
+    t0 = time.perf_counter()
+    train = [bodies.config_disk("ensemble_member", seed=s) for s in range(1, 65)]
+    ens = Ensemble(train, thr)
+    ens.set_integrator(0.001, tol)
+    ens.set_options(gravity_mode=T.GRAVITY_MIXED, hill_factor=hill)
+    ens.set_step_log(1 << 22)
+    set_dither(ens, 0.15, seed=7)
+    ens.advance(args.train_years * T.YEAR)
+    x, y = dataset_from_log(ens.step_log(1 << 22), tol)
+    ens.close()
+    del train
+    net, loss = fit(x, y, seed=0, epochs=30)
+    train_s = time.perf_counter() - t0
+
+    disks = [bodies.config_disk("ensemble_member", seed=s) for s in range(65, 65 + args.ensemble_disks)]
+    n_bodies = sum(d.n_total for d in disks)
+
+    def batched(mode, proposer):
+        e = Ensemble(disks, thr)
+        e.set_integrator(0.001, tol)
+        e.set_options(gravity_mode=mode, hill_factor=hill)
+        if proposer is not None:
+            proposer.attach(e)
+        e.advance(warm_day)
+        E0 = [e.energy(k)[0] for k in range(len(disks))]
+        st0 = [e.stats(k) for k in range(len(disks))]
+        secs, _ = advance_timed(e, warm_day + span_day)
+        st = [e.stats(k) for k in range(len(disks))]
+        dE = max(abs((e.energy(k)[0] - E0[k]) / E0[k]) for k in range(len(disks)))
+        sim_years = sum(a["t_day"] - b["t_day"] for a, b in zip(st, st0)) / T.YEAR
+        tried = sum(a["n_tried_step"] - b["n_tried_step"] for a, b in zip(st, st0))
+        failed = sum(a["n_failed_step"] - b["n_failed_step"] for a, b in zip(st, st0))
+        ev, sysv = e.events()
+        out = {"sim_years_per_s": sim_years / secs, "seconds": secs, "sim_years": sim_years, "attempts": tried,
+               "rejected_frac": failed / max(tried, 1), "max_dE_over_E": dE, "events": int(len(ev)),
+               "all_done": all(a["status"] == T.SYS_DONE for a in st)}
+        if proposer is not None:
+            out["proposed"] = sum(a["n_proposed"] for a in st)
+            out["proposals_accepted"] = sum(a["n_proposal_accepted"] for a in st)
+            out["fallbacks"] = sum(a["n_fallback"] for a in st)
+        keys = sorted((int(k), int(r["event_name"]), int(r["id1"]), int(r["id2"])) for r, k in zip(ev, sysv))
+        e.close()
+        return out, keys
+
+    learned, ev_l = batched(T.GRAVITY_MIXED, net)
+    plain_mixed, ev_m = batched(T.GRAVITY_MIXED, None)
+    plain_fp64, ev_f = batched(T.GRAVITY_FP64, None)
+
+    # the plain FP64 form, one disk at a time through the single-disk API
+    sample = disks[::max(1, len(disks) // args.sequential_sample)][:args.sequential_sample]
+    seq_s, seq_years, seq_dE = 0.0, 0.0, 0.0
+    for d in sample:
+        s = lib.System(d, thr)
+        s.set_integrator(T.INT_RKF78, 0.001, True, tol)
+        s.set_event_options(close_encounter=False, hill_factor=hill)
+        s.set_gravity_mode(T.GRAVITY_FP64)
+        s.advance(warm_day)
+        E0 = s.energy()[0]
+        t_a = s.state()[4]
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        s.advance(warm_day + span_day)
+        torch.cuda.synchronize()
+        seq_s += time.perf_counter() - t1
+        seq_years += (s.state()[4] - t_a) / T.YEAR
+        seq_dE = max(seq_dE, abs((s.energy()[0] - E0) / E0))
+        s.close()
+    sequential = {"sim_years_per_s": seq_years / seq_s, "seconds": seq_s, "sim_years": seq_years,
+                  "max_dE_over_E": seq_dE, "sample": f"{len(sample)} of {len(disks)} disks (every "
+                  f"{max(1, len(disks) // args.sequential_sample)}th), the rate applies to all of them"}
+    return {
+        "workload": f"{len(disks)} disks, {n_bodies} bodies (N ~ U[512, 8192]), RKF7(8) tol 1e-10, "
+                    f"{args.ensemble_years} yr per disk after a {warm_day:g}-day warm-up; CE at {hill:g} mutual "
+                    "Hill radii, collisions at R1+R2, ejection 100 AU, hit-star 0.05 AU",
+        "learned_mixed_batched": learned,
+        "plain_mixed_batched": plain_mixed,
+        "plain_fp64_batched": plain_fp64,
+        "plain_fp64_sequential": sequential,
+        "speedup_vs_plain_fp64_sequential": learned["sim_years_per_s"] / sequential["sim_years_per_s"],
+        "speedup_vs_plain_fp64_batched": learned["sim_years_per_s"] / plain_fp64["sim_years_per_s"],
+        "learned_vs_plain_attempts": plain_mixed["attempts"] / max(learned["attempts"], 1),
+        "event_lists_identical": {"learned_vs_fp64": ev_l == ev_f, "mixed_vs_fp64": ev_m == ev_f},
+        "proposer": {"train_records": int(len(x)), "train_disks": "seeds 1-64, dither 0.15",
+                     "train_years": args.train_years, "loss": loss, "drift_std": float(np.std(y)),
+                     "residual_std": net.residual_std, "safety": net.safety, "setup_seconds": train_s},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -291,7 +422,16 @@ def main():
     ap.add_argument("--workload", default="self_gravitating_16384_rk4", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--only-ensemble", action="store_true", help="the ensemble section alone (profiling)")
+    ap.add_argument("--ensemble-disks", type=int, default=256)
+    ap.add_argument("--ensemble-years", type=float, default=2.0)
+    ap.add_argument("--train-years", type=float, default=10.0)
+    ap.add_argument("--sequential-sample", type=int, default=16)
     args = ap.parse_args()
+    if args.only_ensemble:
+        print(json.dumps({"ensemble": ensemble_section(args)}))
+        return
     if args.impl == "reference":
         rank, ws = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
         out = run_reference(args, rank, ws)
