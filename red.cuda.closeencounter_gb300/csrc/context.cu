@@ -294,7 +294,15 @@ int set_param_dev(rg_ctx* c, int i)
 }
 
 // --------------------------------------------------------------------- launch plan
-enum { GROUP_PAIRPAR = 0, GROUP_ROWSEQ = 1, GROUP_FEW_SERIAL = 2, GROUP_FEW_TREE = 3, GROUP_MIXED = 4 };
+enum {
+    GROUP_PAIRPAR = 0,
+    GROUP_ROWSEQ = 1,
+    GROUP_FEW_SERIAL = 2,
+    GROUP_FEW_TREE = 3,
+    GROUP_MIXED = 4,
+    GROUP_DF_ROWSEQ = 5,  // mixed mode: the row kernel in double-float arithmetic
+    GROUP_DF_FEW = 6,     // mixed mode: few heavy sinks in double-float arithmetic
+};
 constexpr int FEW_BLOCK_SINKS = 32;  // blocks with at most this many sinks use the few-sink path
 
 // CTA tiles of the interaction matrix (number_of_bodies::get_bound_SI/NSI/NI,
@@ -311,7 +319,8 @@ void build_tiles(rg_ctx* c)
     c->few_pitch = 0;
     const int nsi = c->n_si(), nm = c->n_massive(), nt = c->n_total();
     // heavy bodies of the mixed kernel: the leading stars, giant and rocky planets.  As
-    // sources their terms are exact FP64; as sinks (few rows) they use the FP64 path.
+    // sources of the mixed kernel their terms are exact FP64; as sinks (few rows), and as
+    // the sources of row-kernel blocks, they use the double-float kernels.
     const int n_heavy = std::min(nsi, c->cnt[0] + c->cnt[1] + c->cnt[2]);
     struct Blk {
         int s0, s1, src1, block;
@@ -324,7 +333,7 @@ void build_tiles(rg_ctx* c)
         for (int s = s0; s < s1; s += step) {
             c->tiles.push_back(Tile{s, std::min(s + step, s1), 0, src1, 0, 0, block, 0});
             c->heavy_mx.push_back(kind == GROUP_MIXED ? std::min(n_heavy, src1) : 0);
-            if (kind == GROUP_FEW_SERIAL || kind == GROUP_FEW_TREE) {
+            if (kind == GROUP_FEW_SERIAL || kind == GROUP_FEW_TREE || kind == GROUP_DF_FEW) {
                 c->few_row0.push_back(c->few_rows);
                 c->few_nsrc.push_back(src1);
                 for (int i = s; i < std::min(s + step, s1); i++) {
@@ -347,19 +356,21 @@ void build_tiles(rg_ctx* c)
     for (const auto& b : blks) {
         if (b.s1 <= b.s0) continue;
         const int ns = b.s1 - b.s0;
-        if (b.src1 <= c->rowseq_max_src) {  // few sources: thread per sink, both modes
+        if (b.src1 <= c->rowseq_max_src) {  // few sources: thread per sink (same tiles in both modes)
             add_group(0, GROUP_ROWSEQ, b.s0, b.s1, b.src1, b.block, 128);
             c->plan[1].push_back(c->plan[0].back());
+            c->plan[1].back().kind = GROUP_DF_ROWSEQ;
             continue;
         }
-        if (ns <= FEW_BLOCK_SINKS) {  // few sinks, many sources: exact serial row sums, both modes
+        if (ns <= FEW_BLOCK_SINKS) {  // few sinks, many sources: exact serial row sums (same rows)
             add_group(0, GROUP_FEW_SERIAL, b.s0, b.s1, b.src1, b.block, FEW_SINKS_MAX);
             c->plan[1].push_back(c->plan[0].back());
+            c->plan[1].back().kind = GROUP_DF_FEW;
             continue;
         }
         add_group(0, GROUP_PAIRPAR, b.s0, b.s1, b.src1, b.block, c->pairpar_S);
         const int light0 = b.block == 0 ? std::max(b.s0, std::min(n_heavy, b.s1)) : b.s0;
-        add_group(1, GROUP_FEW_TREE, b.s0, light0, b.src1, b.block, FEW_SINKS_MAX);
+        add_group(1, GROUP_DF_FEW, b.s0, light0, b.src1, b.block, FEW_SINKS_MAX);
         add_group(1, GROUP_MIXED, light0, b.s1, b.src1, b.block, MIXED_SINKS_PER_TILE);
     }
     c->tiles_dirty = true;
@@ -473,6 +484,24 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
                                       c->d_row_sink, c->d_row_nsrc, nullptr, gr.row_base, gr.rows,
                                       gr.kind == GROUP_FEW_SERIAL, c->st);
             c->n_kernels += 2;
+            break;
+        case GROUP_DF_ROWSEQ:
+        case GROUP_DF_FEW:
+            if (!split_done) {
+                rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, c->n_total(), (SplitPos*)c->d_split, c->st);
+                split_done = true;
+                c->n_kernels++;
+            }
+            if (rc) break;
+            if (gr.kind == GROUP_DF_ROWSEQ) {
+                rc = launch_grav_df_rowseq(g, c->d_split, c->st);
+                c->n_kernels++;
+            } else {
+                rc = launch_grav_df_few(g, c->d_split, c->d_few_row0 + gr.off, gr.max_src, c->d_terms, c->few_rows,
+                                        c->few_pitch, c->d_row_sink, c->d_row_nsrc, nullptr, gr.row_base, gr.rows,
+                                        c->st);
+                c->n_kernels += 2;
+            }
             break;
         case GROUP_MIXED:
             if (!split_done) {

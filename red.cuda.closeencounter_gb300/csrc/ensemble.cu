@@ -580,7 +580,18 @@ constexpr double GAUSS = 1.720209895e-2;
 constexpr double GAUSS2 = 2.959122082855911025e-4;
 constexpr int STAGE_TILE = 2048;
 constexpr int ENS_FEW_BLOCK = 32;
-enum { GROUP_PAIRPAR = 0, GROUP_ROWSEQ = 1, GROUP_FEW_SERIAL = 2, GROUP_FEW_TREE = 3, GROUP_MIXED = 4 };
+// the FP64 plan uses the first four kinds; the mixed-precision plan uses DF_ROWSEQ, DF_FEW
+// (double-float heavy pairs) and MIXED
+enum {
+    GROUP_PAIRPAR = 0,
+    GROUP_ROWSEQ = 1,
+    GROUP_FEW_SERIAL = 2,
+    GROUP_FEW_TREE = 3,
+    GROUP_MIXED = 4,
+    GROUP_DF_ROWSEQ = 5,
+    GROUP_DF_FEW = 6,
+    GROUP_KINDS = 7
+};
 
 template <class T>
 int dalloc(T** p, size_t count)
@@ -643,8 +654,8 @@ void build_gravity_plan(rg_ens* e)
         std::vector<int> heavy;
     };
     // group tiles of all disks by (mode, kind)
-    std::vector<Tile> by[2][5];
-    std::vector<int> hv[2][5];
+    std::vector<Tile> by[2][GROUP_KINDS];
+    std::vector<int> hv[2][GROUP_KINDS];
     for (int s = 0; s < e->n_sys; s++) {
         const int b = e->base[s];
         const int nsi = e->n_si(s), nm = e->n_massive(s), nt = e->ntot[s];
@@ -663,28 +674,28 @@ void build_gravity_plan(rg_ens* e)
             if (k.s1 <= k.s0) continue;
             if (k.src1 <= 64) {
                 add(0, GROUP_ROWSEQ, k.s0, k.s1, k.src1, k.block, 128);
-                add(1, GROUP_ROWSEQ, k.s0, k.s1, k.src1, k.block, 128);
+                add(1, GROUP_DF_ROWSEQ, k.s0, k.s1, k.src1, k.block, 128);
             } else if (k.s1 - k.s0 <= ENS_FEW_BLOCK) {
                 add(0, GROUP_FEW_SERIAL, k.s0, k.s1, k.src1, k.block, FEW_SINKS_MAX);
-                add(1, GROUP_FEW_TREE, k.s0, k.s1, k.src1, k.block, FEW_SINKS_MAX);
+                add(1, GROUP_DF_FEW, k.s0, k.s1, k.src1, k.block, FEW_SINKS_MAX);
             } else {
                 add(0, GROUP_PAIRPAR, k.s0, k.s1, k.src1, k.block, 16);
                 const int light0 = k.block == 0 ? std::max(k.s0, std::min(n_heavy, k.s1)) : k.s0;
-                add(1, GROUP_FEW_TREE, k.s0, light0, k.src1, k.block, FEW_SINKS_MAX);
+                add(1, GROUP_DF_FEW, k.s0, light0, k.src1, k.block, FEW_SINKS_MAX);
                 add(1, GROUP_MIXED, light0, k.s1, k.src1, k.block, MIXED_SINKS_PER_TILE);
             }
         }
     }
     for (int mode = 0; mode < 2; mode++) {
         e->plan[mode].clear();
-        for (int kind = 0; kind < 5; kind++) {
+        for (int kind = 0; kind < GROUP_KINDS; kind++) {
             auto& T = by[mode][kind];
             if (T.empty()) continue;
             rg_ens::Group gr{kind, e->tiles.size(), (int)T.size(), e->few_rows, 0, 0};
             for (size_t k = 0; k < T.size(); k++) {
                 e->tiles.push_back(T[k]);
                 e->heavy.push_back(hv[mode][kind][k]);
-                if (kind == GROUP_FEW_SERIAL || kind == GROUP_FEW_TREE) {
+                if (kind == GROUP_FEW_SERIAL || kind == GROUP_FEW_TREE || kind == GROUP_DF_FEW) {
                     e->few_row0.push_back(e->few_rows);
                     const int nsrc = T[k].src_end - T[k].src_begin;
                     for (int i = T[k].sink_begin; i < T[k].sink_end; i++) {
@@ -803,6 +814,24 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
                                       e->d_row_sink, e->d_row_nsrc, e->d_row_sys, gr.row_base, gr.rows,
                                       gr.kind == GROUP_FEW_SERIAL, e->st);
             e->n_kernels += 2;
+            break;
+        case GROUP_DF_ROWSEQ:
+        case GROUP_DF_FEW:
+            if (!split_done) {
+                rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->cap, (SplitPos*)e->d_split, e->st);
+                split_done = true;
+                e->n_kernels++;
+            }
+            if (rc) break;
+            if (gr.kind == GROUP_DF_ROWSEQ) {
+                rc = launch_grav_df_rowseq(g, e->d_split, e->st);
+                e->n_kernels++;
+            } else {
+                rc = launch_grav_df_few(g, e->d_split, e->d_few_row0 + gr.off, gr.max_src, e->d_terms, e->few_rows,
+                                        e->few_pitch, e->d_row_sink, e->d_row_nsrc, e->d_row_sys, gr.row_base, gr.rows,
+                                        e->st);
+                e->n_kernels += 2;
+            }
             break;
         case GROUP_MIXED:
             if (!split_done) {

@@ -25,14 +25,20 @@
 // w-th slice of each source tile, so all 256 threads work however few sinks a tile has.
 // Sources are staged in shared memory as FP32 (hi, lo) quads; per-warp partial sums are
 // combined with two-sum at the end.
+#include <algorithm>
+#include <string>
+
+#include "../../include/redgb.h"
 #include "common.cuh"
 #include "kernels.h"
 
 namespace redgb {
 
+int set_error(int code, const std::string& msg);
+
 struct SplitPos {
     float4 xy;  // x_hi, x_lo, y_hi, y_lo
-    float4 zm;  // z_hi, z_lo, m, (unused)
+    float4 zm;  // z_hi, z_lo, m_hi, m_lo
 };
 
 // inactive bodies (id < 0, pp_disk.cu:242) get mass 0 here, so the pair loop needs no
@@ -46,7 +52,8 @@ __global__ void split_positions_kernel(const double* __restrict__ x, const doubl
     const double xd = x[i], yd = y[i], zd = z[i];
     const float xh = (float)xd, yh = (float)yd, zh = (float)zd;
     out[i].xy = make_float4(xh, (float)(xd - (double)xh), yh, (float)(yd - (double)yh));
-    out[i].zm = make_float4(zh, (float)(zd - (double)zh), id[i] < 0 ? 0.0f : (float)m[i], 0.0f);
+    const float mh = id[i] < 0 ? 0.0f : (float)m[i];
+    out[i].zm = make_float4(zh, (float)(zd - (double)zh), mh, id[i] < 0 ? 0.0f : (float)(m[i] - (double)mh));
 }
 
 __device__ __forceinline__ float rsqrt_approx(float x)
@@ -402,6 +409,330 @@ __global__ void mixed_reduce_kernel(const double* __restrict__ partial, int n_ch
         for (int c = 0; c < n_chunks; c++) v += partial[((long long)c * 3 + comp) * n_part + i];
         (comp == 0 ? ax : (comp == 1 ? ay : az))[i] = v;
     }
+}
+
+// ---------------------------------------------------------------------------------------
+// Heavy pairs in double-float arithmetic.
+//
+// The pairs whose terms need more than FP32 accuracy -- sinks against the star and giant
+// planets, and the star and giants' own rows -- would cost GB300 its scarce FP64 issue
+// (grav_fp64_rowseq and the few-sink kernels spend about 35 FP64 operations per pair).
+// Here they run on the FP32 pipes in unevaluated sums of two floats (hi + lo, about 44
+// significant bits), built from the error-free transformations two-sum (Knuth) and
+// two-product by FMA, with the double-double addition and multiplication of Hida, Li and
+// Bailey (2001) carried out in float.  The inputs are the split positions and masses of
+// split_positions_kernel (x = x_hi + x_lo to 2^-48 |x|), the displacement is formed from
+// them exactly up to that split, 1/r^3 comes from the FP32 rsqrt refined by one Newton
+// step evaluated in double-float (relative error about 2.5e-14), and the sums stay in
+// double-float until one conversion to FP64 per sink and component.  Event decisions are
+// screened in FP32 with the same 1e-3 margin as the mixed kernel and re-taken in FP64.
+
+struct DF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ DF df_two_sum(float a, float b)
+{
+    const float s = a + b;
+    const float bb = s - a;
+    return DF{s, (a - (s - bb)) + (b - bb)};
+}
+
+// |a| >= |b| (or a == 0)
+__device__ __forceinline__ DF df_fast_sum(float a, float b)
+{
+    const float s = a + b;
+    return DF{s, b - (s - a)};
+}
+
+__device__ __forceinline__ DF df_two_prod(float a, float b)
+{
+    const float p = a * b;
+    return DF{p, fmaf(a, b, -p)};
+}
+
+__device__ __forceinline__ DF df_add(DF a, DF b)
+{
+    DF s = df_two_sum(a.hi, b.hi);
+    const DF t = df_two_sum(a.lo, b.lo);
+    s.lo += t.hi;
+    s = df_fast_sum(s.hi, s.lo);
+    s.lo += t.lo;
+    return df_fast_sum(s.hi, s.lo);
+}
+
+__device__ __forceinline__ DF df_mul(DF a, DF b)
+{
+    DF p = df_two_prod(a.hi, b.hi);
+    p.lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
+    return df_fast_sum(p.hi, p.lo);
+}
+
+// (ah + al) - (bh + bl) of two split coordinates
+__device__ __forceinline__ DF df_diff(float ah, float al, float bh, float bl)
+{
+    const DF s = df_two_sum(ah, -bh);
+    return df_two_sum(s.hi, (al - bl) + s.lo);
+}
+
+__device__ __forceinline__ double df_to_double(DF a) { return (double)a.hi + (double)a.lo; }
+
+// the term m_j (r_j - r_i) / |r_j - r_i|^3 of one pair; r2f = |r_j - r_i|^2 in FP32
+__device__ __forceinline__ void df_term(const SplitPos& si, const SplitPos& pj, DF& tx, DF& ty, DF& tz, float& r2f)
+{
+    const DF dx = df_diff(pj.xy.x, pj.xy.y, si.xy.x, si.xy.y);
+    const DF dy = df_diff(pj.xy.z, pj.xy.w, si.xy.z, si.xy.w);
+    const DF dz = df_diff(pj.zm.x, pj.zm.y, si.zm.x, si.zm.y);
+    DF r2 = df_add(df_add(df_mul(dx, dx), df_mul(dy, dy)), df_mul(dz, dz));
+    // a merged body parked at 1e20 AU (pp_disk.cu:1184) overflows r^2 in FP32; its mass is 0
+    if (!(r2.hi < 1.0e30f)) r2 = DF{1.0e30f, 0.0f};
+    const float y0 = rsqrt_approx(r2.hi);
+    const DF p = df_mul(r2, df_two_prod(y0, y0));
+    const float h = (1.0f - p.hi) - p.lo;  // 1 - r^2 y0^2, small: FP32 suffices
+    const DF y = df_fast_sum(y0, 0.5f * y0 * h);
+    const DF w = df_mul(df_mul(df_mul(y, y), y), DF{pj.zm.z, pj.zm.w});
+    tx = df_mul(w, dx);
+    ty = df_mul(w, dy);
+    tz = df_mul(w, dz);
+    r2f = r2.hi;
+}
+
+// FP32 screen of the event tests of pair_term (pp_disk.cu:262-280) with a 1e-3 margin;
+// candidates are decided in FP64 by exact_event_tests
+__device__ __forceinline__ void df_screen(const GravArgs& g, const Tile& tile, int i, int j, float r2f, float Ri,
+                                          float Rj, float rhoi, float rhoj, float mi, float mj, float inv3M)
+{
+    const int li = i - tile.base, lj = j - tile.base;
+    if (!(li > 0 && li > lj)) return;
+    const float margin = 1.001f;
+    bool cand = false;
+    if (g.record) {
+        const float lim = (float)g.f_rad * (Ri + Rj) * margin;
+        cand = r2f < lim * lim;
+    }
+    if (g.hill && tile.block != 2 && lj > 0) {
+        const float h = 0.5f * (rhoi + rhoj);
+        const float d3 = r2f * sqrtf(r2f);
+        cand = cand || d3 < (float)g.hill_f3 * (mi + mj) * inv3M * (h * h * h) * (margin * margin * margin);
+    }
+    if (cand)
+        exact_event_tests(g, tile, i, j, g.px[i], g.py[i], g.pz[i], g.radius[i], g.mass[i], g.hill ? g.rho[i] : 0.0);
+}
+
+// Row kernel: one thread per sink, the tile's sources (a few massive bodies) staged in
+// shared memory -- the mixed-precision counterpart of grav_fp64_rowseq.
+constexpr int DF_ROW_NT = 128;
+
+template <bool SCREEN>
+__global__ void __launch_bounds__(DF_ROW_NT) grav_df_rowseq(GravArgs g, const SplitPos* __restrict__ sp)
+{
+    __shared__ SplitPos s_p[DF_ROW_NT];
+    __shared__ float s_R[DF_ROW_NT], s_rho[DF_ROW_NT];
+    __shared__ int s_id[DF_ROW_NT];
+    const Tile tile = g.tiles[blockIdx.x];
+    if (g.sys_active && !g.sys_active[tile.sys]) return;
+    const int t = threadIdx.x;
+    const int i = tile.sink_begin + t;
+    const bool sink_ok = i < tile.sink_end;
+    const bool active = sink_ok && 0 < g.id[i];
+    SplitPos si{};
+    float Ri = 0.0f, rhoi = 0.0f, mi = 0.0f;
+    if (active) {
+        si = sp[i];
+        if (SCREEN) {
+            Ri = (float)g.radius[i];
+            rhoi = g.hill ? (float)g.rho[i] : 0.0f;
+            mi = (float)g.mass[i];
+        }
+    }
+    const float inv3M = (SCREEN && g.hill) ? (float)(1.0 / (3.0 * g.mass[tile.base])) : 0.0f;
+    DF ax{0.0f, 0.0f}, ay{0.0f, 0.0f}, az{0.0f, 0.0f};
+    for (int j0 = tile.src_begin; j0 < tile.src_end; j0 += DF_ROW_NT) {
+        const int nj = min(DF_ROW_NT, tile.src_end - j0);
+        if (t < nj) {
+            const int j = j0 + t;
+            s_p[t] = sp[j];
+            s_id[t] = g.id[j];
+            if (SCREEN) {
+                s_R[t] = (float)g.radius[j];
+                s_rho[t] = g.hill ? (float)g.rho[j] : 0.0f;
+            }
+        }
+        __syncthreads();
+        if (active) {
+            for (int q = 0; q < nj; q++) {
+                const int j = j0 + q;
+                if (j == i || s_id[q] < 0) continue;
+                DF tx, ty, tz;
+                float r2f;
+                df_term(si, s_p[q], tx, ty, tz, r2f);
+                ax = df_add(ax, tx);
+                ay = df_add(ay, ty);
+                az = df_add(az, tz);
+                if (SCREEN) df_screen(g, tile, i, j, r2f, Ri, s_R[q], rhoi, s_rho[q], mi, s_p[q].zm.z, inv3M);
+            }
+        }
+        __syncthreads();
+    }
+    if (sink_ok) {
+        g.ax[i] = df_to_double(ax);
+        g.ay[i] = df_to_double(ay);
+        g.az[i] = df_to_double(az);
+    }
+}
+
+// Few-sink kernel: tiles of at most FEW_SINKS_MAX heavy sinks against many sources.
+// grid (source chunks, tiles); a CTA takes DF_FEW_CHUNK sources of one tile, every thread
+// keeps double-float sums for all the tile's sinks, and the CTA's sums go to
+// partial[(comp * rows + row) * pitch + chunk] as FP64; df_few_final adds the chunks.
+constexpr int DF_FEW_CHUNK = 2048;
+
+struct DfFewArgs {
+    GravArgs g;
+    const SplitPos* sp;
+    const int* tile_row0;  // first row of each tile
+    double* partial;
+    int rows;
+    long long pitch;  // >= chunks of the longest row
+};
+
+template <bool SCREEN>
+__global__ void __launch_bounds__(256) grav_df_few(DfFewArgs a)
+{
+    const GravArgs& g = a.g;
+    const Tile tile = g.tiles[blockIdx.y];
+    if (g.sys_active && !g.sys_active[tile.sys]) return;
+    const int nsrc = tile.src_end - tile.src_begin;
+    const int c0 = blockIdx.x * DF_FEW_CHUNK;
+    if (c0 >= nsrc) return;
+    const int ns = tile.sink_end - tile.sink_begin;
+    __shared__ SplitPos s_sink[FEW_SINKS_MAX];
+    __shared__ float s_R[FEW_SINKS_MAX], s_rho[FEW_SINKS_MAX], s_m[FEW_SINKS_MAX];
+    __shared__ int s_act[FEW_SINKS_MAX];
+    __shared__ DF s_red[8][3 * FEW_SINKS_MAX];
+    if (threadIdx.x < ns) {
+        const int i = tile.sink_begin + threadIdx.x;
+        s_sink[threadIdx.x] = a.sp[i];
+        s_act[threadIdx.x] = 0 < g.id[i];
+        s_R[threadIdx.x] = SCREEN ? (float)g.radius[i] : 0.0f;
+        s_rho[threadIdx.x] = (SCREEN && g.hill) ? (float)g.rho[i] : 0.0f;
+        s_m[threadIdx.x] = SCREEN ? (float)g.mass[i] : 0.0f;
+    }
+    __syncthreads();
+    const float inv3M = (SCREEN && g.hill) ? (float)(1.0 / (3.0 * g.mass[tile.base])) : 0.0f;
+    DF acc[FEW_SINKS_MAX][3];
+#pragma unroll
+    for (int s = 0; s < FEW_SINKS_MAX; s++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) acc[s][c] = DF{0.0f, 0.0f};
+    const int c1 = min(nsrc, c0 + DF_FEW_CHUNK);
+    for (int q = c0 + (int)threadIdx.x; q < c1; q += blockDim.x) {
+        const int j = tile.src_begin + q;
+        if (g.id[j] < 0) continue;
+        const SplitPos pj = a.sp[j];
+        float Rj = 0.0f, rhoj = 0.0f;
+        if (SCREEN) {
+            Rj = (float)g.radius[j];
+            rhoj = g.hill ? (float)g.rho[j] : 0.0f;
+        }
+#pragma unroll
+        for (int s = 0; s < FEW_SINKS_MAX; s++) {
+            if (s < ns) {
+                const int i = tile.sink_begin + s;
+                if (s_act[s] && j != i) {
+                    DF tx, ty, tz;
+                    float r2f;
+                    df_term(s_sink[s], pj, tx, ty, tz, r2f);
+                    acc[s][0] = df_add(acc[s][0], tx);
+                    acc[s][1] = df_add(acc[s][1], ty);
+                    acc[s][2] = df_add(acc[s][2], tz);
+                    if (SCREEN) df_screen(g, tile, i, j, r2f, s_R[s], Rj, s_rho[s], rhoj, s_m[s], pj.zm.z, inv3M);
+                }
+            }
+        }
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int s = 0; s < FEW_SINKS_MAX; s++) {
+        if (s < ns) {  // uniform over the CTA
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                DF v = acc[s][c];
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    const DF o{__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off)};
+                    v = df_add(v, o);
+                }
+                if (lane == 0) s_red[warp][3 * s + c] = v;
+            }
+        }
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < 3 * ns) {
+        const int s = threadIdx.x / 3, c = threadIdx.x % 3;
+        DF v = s_red[0][threadIdx.x];
+        for (int w = 1; w < (int)(blockDim.x >> 5); w++) v = df_add(v, s_red[w][threadIdx.x]);
+        const int row = a.tile_row0[blockIdx.y] + s;
+        a.partial[((long long)c * a.rows + row) * a.pitch + blockIdx.x] = df_to_double(v);
+    }
+}
+
+struct DfFinalArgs {
+    const double* partial;
+    int rows, row0, nrows;
+    long long pitch;
+    const int* row_sink;
+    const int* row_nsrc;
+    const int* row_sys;  // nullptr for one disk
+    const int* sys_active;
+    double *ax, *ay, *az;
+};
+
+// one thread per (row, component): the row's chunk sums in order
+__global__ void df_few_final(DfFinalArgs a)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= 3 * a.nrows) return;
+    const int comp = k / a.nrows, row = a.row0 + k % a.nrows;
+    if (a.sys_active && a.row_sys && !a.sys_active[a.row_sys[row]]) return;
+    const int nch = (a.row_nsrc[row] + DF_FEW_CHUNK - 1) / DF_FEW_CHUNK;
+    const double* P = a.partial + ((long long)comp * a.rows + row) * a.pitch;
+    double s = 0.0;
+    for (int c = 0; c < nch; c++) s += P[c];
+    (comp == 0 ? a.ax : (comp == 1 ? a.ay : a.az))[a.row_sink[row]] = s;
+}
+
+int launch_grav_df_rowseq(const GravArgs& g, const void* split, cudaStream_t st)
+{
+    if (g.n_tiles <= 0) return 0;
+    const SplitPos* sp = (const SplitPos*)split;
+    if (g.record || g.hill)
+        grav_df_rowseq<true><<<g.n_tiles, DF_ROW_NT, 0, st>>>(g, sp);
+    else
+        grav_df_rowseq<false><<<g.n_tiles, DF_ROW_NT, 0, st>>>(g, sp);
+    RG_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row0, int max_src, double* partial,
+                       int rows, long long pitch, const int* row_sink, const int* row_nsrc, const int* row_sys,
+                       int group_row0, int group_rows, cudaStream_t st)
+{
+    if (g.n_tiles <= 0 || group_rows <= 0) return 0;
+    const int chunks = std::max(1, (max_src + DF_FEW_CHUNK - 1) / DF_FEW_CHUNK);
+    if ((long long)chunks > pitch) return set_error(RG_ERR_STATE, "few-sink partial buffer too narrow");
+    DfFewArgs a{g, (const SplitPos*)split, tile_row0, partial, rows, pitch};
+    const dim3 grid(chunks, g.n_tiles);
+    if (g.record || g.hill)
+        grav_df_few<true><<<grid, 256, 0, st>>>(a);
+    else
+        grav_df_few<false><<<grid, 256, 0, st>>>(a);
+    RG_CUDA_CHECK(cudaGetLastError());
+    DfFinalArgs f{partial, rows, group_row0, group_rows, pitch, row_sink, row_nsrc, row_sys, g.sys_active,
+                  g.ax, g.ay, g.az};
+    df_few_final<<<(3 * group_rows + 127) / 128, 128, 0, st>>>(f);
+    RG_CUDA_CHECK(cudaGetLastError());
+    return 0;
 }
 
 int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id, int n,

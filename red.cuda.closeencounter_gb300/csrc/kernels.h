@@ -79,6 +79,13 @@ int launch_split_positions(const double* x, const double* y, const double* z, co
                            struct SplitPos* out, cudaStream_t st);
 int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* heavy_end, float near_ratio,
                             int n_chunks, int chunk, double* partial, int n_part, cudaStream_t st);
+// heavy pairs of the mixed-precision mode in double-float arithmetic (gravity_mixed.cu):
+// the row kernel for blocks with a few massive sources, the few-sink kernel for the
+// star's and giants' own rows (partial: 3 x rows x pitch doubles, pitch >= source chunks)
+int launch_grav_df_rowseq(const GravArgs& g, const void* split, cudaStream_t st);
+int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row0, int max_src, double* partial,
+                       int rows, long long pitch, const int* row_sink, const int* row_nsrc, const int* row_sys,
+                       int group_row0, int group_rows, cudaStream_t st);
 int launch_star_distance(const double* x, const double* y, const double* z, const int* base_of, int n, double* rho,
                          cudaStream_t st);
 
