@@ -299,6 +299,17 @@ def run_reference(args, rank, ws):
             "e2e": {"value": value, "unit": "sim-years/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def _compare_events(a, b):
+    """Two event lists of (disk, type, id1, id2): identical, or how many records differ.
+    Over a long interval the trajectories of two precisions part chaotically near the
+    giants, so grazing close encounters may be recorded in one run and not the other;
+    every decision on a given state is taken in FP64 by both."""
+    from collections import Counter
+    ca, cb = Counter(a), Counter(b)
+    return {"identical": a == b, "n": len(a), "n_fp64": len(b),
+            "only_here": sum((ca - cb).values()), "only_fp64": sum((cb - ca).values())}
+
+
 def ensemble_section(args):
     """The batched / mixed / learned forms against the plain FP64 form (module docstring)."""
     import torch
@@ -405,7 +416,8 @@ def ensemble_section(args):
         "speedup_vs_plain_fp64_sequential": learned["sim_years_per_s"] / sequential["sim_years_per_s"],
         "speedup_vs_plain_fp64_batched": learned["sim_years_per_s"] / plain_fp64["sim_years_per_s"],
         "learned_vs_plain_attempts": plain_mixed["attempts"] / max(learned["attempts"], 1),
-        "event_lists_identical": {"learned_vs_fp64": ev_l == ev_f, "mixed_vs_fp64": ev_m == ev_f},
+        "event_lists": {name: _compare_events(ev, ev_f) for name, ev in (("learned_vs_fp64", ev_l),
+                                                                         ("mixed_vs_fp64", ev_m))},
         "proposer": {"train_records": int(len(x)), "train_disks": "seeds 1-64, dither 0.15",
                      "train_years": args.train_years, "loss": loss, "drift_std": float(np.std(y)),
                      "residual_std": net.residual_std, "safety": net.safety, "setup_seconds": train_s},

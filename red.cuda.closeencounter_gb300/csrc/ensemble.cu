@@ -59,20 +59,44 @@ struct EnsStageArgs {
     double* out_hi;       // rows 3..5
 };
 
-// FORM_SUM (stage rows) or FORM_RK8_NP1 (y_{n+1}), one CTA per stage tile
-template <int FORM, int NTERM>
+// FORM_SUM (stage rows) or FORM_RK8_NP1 (y_{n+1}), one CTA per stage tile.
+// FUSED = false: the reference's operation order, y + dt * (c_0 k_0 + c_1 k_1 + ...),
+// without contraction (the bit-exact FP64 mode).  FUSED = true (mixed-precision mode): the
+// per-disk coefficients dt * c_q are formed once per CTA and the sum is contracted,
+// y + fma(dt c_q, k_q, ...), half the FP64 operations -- GB300 retires about two FP64
+// operations per SM and clock, so these kernels are bound by FP64 issue, not by HBM.
+template <int FORM, int NTERM, bool FUSED>
 __global__ void __launch_bounds__(256) ens_combine_kernel(EnsStageArgs a)
 {
     const StageTile t = a.tiles[blockIdx.x];
     if (!a.active[t.sys]) return;
     const double dt = a.dt[t.sys];
+    double w[MAXT];
+    if (FUSED) {
+#pragma unroll
+        for (int q = 0; q < MAXT; q++) w[q] = dt * a.c[q];
+    }
     const int nb = t.b1 - t.b0;
     for (int f = threadIdx.x; f < 6 * nb; f += blockDim.x) {
         const int row = f / nb;
         const long long e = (long long)row * a.stride + t.b0 + (f - row * nb);
         const double y = a.y[e];
         double out;
-        if (FORM == FORM_SUM) {
+        if (FUSED) {
+            double sum;
+            if (FORM == FORM_SUM) {
+                sum = w[0] * a.k[0][e];
+#pragma unroll
+                for (int q = 1; q < NTERM; q++) sum = fma(w[q], a.k[q][e], sum);
+            } else {
+                sum = w[0] * a.k[0][e];
+                sum = fma(w[1], a.k[1][e], sum);
+                sum = fma(w[2], a.k[2][e] + a.k[3][e], sum);
+                sum = fma(w[3], a.k[4][e] + a.k[5][e], sum);
+                sum = fma(w[4], a.k[6][e], sum);
+            }
+            out = y + sum;
+        } else if (FORM == FORM_SUM) {
             double sum = a.c[0] * a.k[0][e];
 #pragma unroll
             for (int q = 1; q < NTERM; q++) sum = sum + a.c[q] * a.k[q][e];
@@ -306,27 +330,30 @@ __global__ void ens_feat_kernel(const StageTile* tiles, const int* mask, const d
                                 const double* mass, const int* id, const int* base_of, const int* nsi_of, int stride,
                                 unsigned int* amax, unsigned int* hill3)
 {
+    // FP32 arithmetic: the features are logarithms fed to an FP32 network, and GB300 spends
+    // about 64 FP32 issue slots per FP64 operation
     const StageTile t = tiles[blockIdx.x];
     if (!mask[t.sys]) return;
     float am = 0.0f, h3 = 3.0e38f;
     for (int i = t.b0 + threadIdx.x; i < t.b1; i += blockDim.x) {
         if (id[i] <= 0) continue;
-        const double ax = k0[3LL * stride + i], ay = k0[4LL * stride + i], az = k0[5LL * stride + i];
-        am = fmaxf(am, (float)sqrt(ax * ax + ay * ay + az * az));
+        const float ax = (float)k0[3LL * stride + i], ay = (float)k0[4LL * stride + i], az = (float)k0[5LL * stride + i];
+        am = fmaxf(am, sqrtf(ax * ax + ay * ay + az * az));
         const int b = base_of[i], ns = nsi_of[i];
-        const double M = mass[b];
-        const double x0 = y[b], y0 = y[stride + b], z0 = y[2LL * stride + b];
-        const double xi = y[i], yi = y[stride + i], zi = y[2LL * stride + i];
-        const double ri = sqrt((xi - x0) * (xi - x0) + (yi - y0) * (yi - y0) + (zi - z0) * (zi - z0));
+        const float M = (float)mass[b];
+        const float x0 = (float)y[b], y0 = (float)y[stride + b], z0 = (float)y[2LL * stride + b];
+        const float xi = (float)y[i] - x0, yi = (float)y[stride + i] - y0, zi = (float)y[2LL * stride + i] - z0;
+        const float ri = sqrtf(xi * xi + yi * yi + zi * zi);
+        const float mi = (float)mass[i];
         for (int j = b + 1; j < b + ns; j++) {
             if (j == i || id[j] <= 0) continue;
-            const double xj = y[j], yj = y[stride + j], zj = y[2LL * stride + j];
-            const double dx = xj - xi, dy = yj - yi, dz = zj - zi;
-            const double d2 = dx * dx + dy * dy + dz * dz;
-            const double rj = sqrt((xj - x0) * (xj - x0) + (yj - y0) * (yj - y0) + (zj - z0) * (zj - z0));
-            const double hh = 0.5 * (ri + rj);
-            const double rh3 = (mass[i] + mass[j]) / (3.0 * M) * hh * hh * hh;
-            if (rh3 > 0.0) h3 = fminf(h3, (float)(d2 * sqrt(d2) / rh3));
+            const float xj = (float)y[j] - x0, yj = (float)y[stride + j] - y0, zj = (float)y[2LL * stride + j] - z0;
+            const float dx = xj - xi, dy = yj - yi, dz = zj - zi;
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const float rj = sqrtf(xj * xj + yj * yj + zj * zj);
+            const float hh = 0.5f * (ri + rj);
+            const float rh3 = (mi + (float)mass[j]) / (3.0f * M) * hh * hh * hh;
+            if (rh3 > 0.0f) h3 = fminf(h3, d2 * sqrtf(d2) / rh3);
         }
     }
     for (int off = 16; off > 0; off >>= 1) {
@@ -873,7 +900,14 @@ int launch_stage(rg_ens* e, int form, int nterm, const int* stages, const double
     a.out_hi = out_hi;
     const int g = (int)e->stiles.size();
     if (g <= 0) return RG_OK;
-#define RG_ENS(F, T) ens_combine_kernel<F, T><<<g, 256, 0, e->st>>>(a)
+    const bool fused = e->gravity_mode == RG_GRAVITY_MIXED;
+#define RG_ENS(F, T)                                                     \
+    do {                                                                 \
+        if (fused)                                                       \
+            ens_combine_kernel<F, T, true><<<g, 256, 0, e->st>>>(a);     \
+        else                                                             \
+            ens_combine_kernel<F, T, false><<<g, 256, 0, e->st>>>(a);    \
+    } while (0)
     if (form == FORM_RK8_NP1) {
         RG_ENS(FORM_RK8_NP1, 7);
     } else {
