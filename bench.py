@@ -361,7 +361,9 @@ def ensemble_section(args):
         e.advance(warm_day)
         E0 = [e.energy(k)[0] for k in range(len(disks))]
         st0 = [e.stats(k) for k in range(len(disks))]
+        _, g0 = e.kernel_count()
         secs, _ = advance_timed(e, warm_day + span_day)
+        _, g1 = e.kernel_count()
         st = [e.stats(k) for k in range(len(disks))]
         dE = max(abs((e.energy(k)[0] - E0[k]) / E0[k]) for k in range(len(disks)))
         sim_years = sum(a["t_day"] - b["t_day"] for a, b in zip(st, st0)) / T.YEAR
@@ -370,7 +372,8 @@ def ensemble_section(args):
         ev, sysv = e.events()
         out = {"sim_years_per_s": sim_years / secs, "seconds": secs, "sim_years": sim_years, "attempts": tried,
                "rejected_frac": failed / max(tried, 1), "max_dE_over_E": dE, "events": int(len(ev)),
-               "all_done": all(a["status"] == T.SYS_DONE for a in st)}
+               "all_done": all(a["status"] == T.SYS_DONE for a in st),
+               "iterations": int(g1 - g0), "ms_per_iteration": 1e3 * secs / max(g1 - g0, 1)}
         if proposer is not None:
             out["proposed"] = sum(a["n_proposed"] for a in st)
             out["proposals_accepted"] = sum(a["n_proposal_accepted"] for a in st)
@@ -437,9 +440,9 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--only-ensemble", action="store_true", help="the ensemble section alone (profiling)")
     ap.add_argument("--ensemble-disks", type=int, default=256)
-    ap.add_argument("--ensemble-years", type=float, default=2.0)
+    ap.add_argument("--ensemble-years", type=float, default=10.0)
     ap.add_argument("--train-years", type=float, default=10.0)
-    ap.add_argument("--sequential-sample", type=int, default=16)
+    ap.add_argument("--sequential-sample", type=int, default=8)
     args = ap.parse_args()
     if args.only_ensemble:
         print(json.dumps({"ensemble": ensemble_section(args)}))

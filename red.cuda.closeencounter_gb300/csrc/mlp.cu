@@ -3,7 +3,7 @@
 // (forward, backward, AdamW) from the attempt logs the ensemble integrator writes.
 //
 // Not in the reference (the reference has no learned component).  Inputs are standardised
-// features of a disk at the start of a step; the output is log(dt_next / dt_last).
+// features of a disk at the start of a step; the output is log(ideal step / last ideal step).
 //
 // Parameter vector (FP32 master copy; the forward passes read its BF16 image):
 //   W1[64][8] b1[64] W2[64][64] b2[64] w3[64] b3
