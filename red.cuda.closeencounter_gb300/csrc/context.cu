@@ -70,6 +70,7 @@ struct rg_ctx {
     unsigned int* d_ev_count = nullptr;
     DevEvent* d_hill = nullptr;
     unsigned int* d_hill_count = nullptr;
+    unsigned int* d_kerr = nullptr;  // set by a gravity kernel whose tile copy timed out
     unsigned int ev_cap = 0;
     EjectRec* d_ej = nullptr;
     unsigned int* d_ej_count = nullptr;
@@ -186,6 +187,7 @@ void free_all(rg_ctx* c)
     cudaFree(c->d_ev_count);
     cudaFree(c->d_hill);
     cudaFree(c->d_hill_count);
+    cudaFree(c->d_kerr);
     cudaFree(c->d_ej);
     cudaFree(c->d_ej_count);
     cudaFree(c->d_maxbits);
@@ -525,7 +527,7 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
                 }
                 if (!rc)
                     rc = launch_grav_mixed_tiles(g, c->d_split, c->d_heavy + gr.off, c->near_ratio, chunks, chunk,
-                                                 c->d_partial, c->cap, c->st);
+                                                 c->d_partial, c->cap, c->d_kerr, c->st);
                 c->n_kernels += chunks > 1;
             }
             c->n_kernels++;
@@ -573,14 +575,25 @@ double stage_c(const rg_ctx* c, int stage)
     }
 }
 
+// a gravity kernel whose bounded wait for a tile copy ran out leaves d_kerr set; the
+// evaluation is then incomplete and the call that read it fails
+int kernel_flag_error(rg_ctx* c, unsigned int flag)
+{
+    if (!flag) return RG_OK;
+    RG_CUDA_CHECK(cudaMemsetAsync(c->d_kerr, 0, sizeof(unsigned int), c->st));
+    return set_error(RG_ERR_CUDA, "a gravity tile copy did not arrive within the wait limit");
+}
+
 // Device candidates -> the reference's raw event records (pp_disk.cu:470-563), in the
 // order its CPU loop creates them: stage by stage, sink i, source j ascending.
 int collect_events(rg_ctx* c)
 {
-    unsigned int counts[2] = {0, 0};
+    unsigned int counts[3] = {0, 0, 0};
     RG_CUDA_CHECK(cudaMemcpyAsync(&counts[0], c->d_ev_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->st));
     RG_CUDA_CHECK(cudaMemcpyAsync(&counts[1], c->d_hill_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&counts[2], c->d_kerr, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->st));
     RG_CUDA_CHECK(cudaStreamSynchronize(c->st));
+    if (int krc = kernel_flag_error(c, counts[2])) return krc;
     const int nsi = c->n_si();
     for (int kind = 0; kind < 2; kind++) {
         unsigned int n = counts[kind];
@@ -1247,6 +1260,9 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
     chk(dalloc(&c->d_ev_count, 1));
     chk(dalloc(&c->d_hill, c->ev_cap));
     chk(dalloc(&c->d_hill_count, 1));
+    chk(dalloc(&c->d_kerr, 1));
+    if (!rc && cudaMemset(c->d_kerr, 0, sizeof(unsigned int)) != cudaSuccess)
+        chk(set_error(RG_ERR_CUDA, "cudaMemset"));
     chk(dalloc(&c->d_ej, nt));
     chk(dalloc(&c->d_ej_count, 1));
     chk(dalloc(&c->d_maxbits, 1));
@@ -1558,7 +1574,10 @@ static int calc_accel_impl(rg_ctx* c, rg_vec_t* a)
     if (n > 0)
         RG_CUDA_CHECK(cudaMemcpy2DAsync(h.data(), n * sizeof(double), c->d_P, cap * sizeof(double), n * sizeof(double),
                                         3, cudaMemcpyDeviceToHost, c->st));
+    unsigned int flag = 0;
+    RG_CUDA_CHECK(cudaMemcpyAsync(&flag, c->d_kerr, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->st));
     RG_CUDA_CHECK(cudaStreamSynchronize(c->st));
+    if ((rc = kernel_flag_error(c, flag))) return rc;
     for (int i = 0; i < n; i++) a[i] = rg_vec_t{h[i], h[(size_t)n + i], h[(size_t)2 * n + i], 0.0};
     return RG_OK;
 }

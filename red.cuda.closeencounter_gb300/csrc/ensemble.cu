@@ -552,6 +552,7 @@ struct rg_ens {
     unsigned int* d_ev_count = nullptr;
     DevEvent* d_hill = nullptr;
     unsigned int* d_hill_count = nullptr;
+    unsigned int* d_kerr = nullptr;  // set by a gravity kernel whose tile copy timed out
     unsigned int ev_cap = 0;
     std::vector<std::pair<int, rg_event_t>> log;
     std::vector<std::vector<int64_t>> hill_prev;
@@ -644,7 +645,7 @@ void free_all(rg_ens* e)
                     e->d_ev, e->d_ev_count, e->d_hill, e->d_hill_count, e->d_part, e->d_base_of, e->d_log,
                     e->d_log_count, e->d_feat, e->d_dt_last, e->d_ideal_last, e->d_hist, e->d_proposed, e->d_step_prop_rej,
                     e->d_prop_rej_steps, e->d_cool, e->d_nprop, e->d_nprop_acc, e->d_nfallback, e->d_amax,
-                    e->d_hill3, e->d_nsi_of};
+                    e->d_hill3, e->d_nsi_of, e->d_kerr};
     for (void* q : ptrs) cudaFree(q);
     for (auto& k : e->d_k) cudaFree(k);
     if (e->st) cudaStreamDestroy(e->st);
@@ -872,7 +873,7 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
                 chunks = 1;  // per-disk source counts differ; one chunk keeps the partial buffer simple
                 (void)src;
                 rc = launch_grav_mixed_tiles(g, e->d_split, e->d_heavy + gr.off, e->near_ratio, chunks,
-                                             MIXED_SOURCE_TILE, nullptr, e->cap, e->st);
+                                             MIXED_SOURCE_TILE, nullptr, e->cap, e->d_kerr, e->st);
                 e->n_kernels++;
             }
             break;
@@ -1353,6 +1354,7 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     chk(dalloc(&e->d_ev_count, 1));
     chk(dalloc(&e->d_hill, e->ev_cap));
     chk(dalloc(&e->d_hill_count, 1));
+    chk(dalloc(&e->d_kerr, 1));
     if (rc) {
         free_all(e);
         delete e;
@@ -1451,6 +1453,7 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     chk(upload(e, e->d_nfallback, zl));
     if (!rc && cudaMemsetAsync(e->d_ev_count, 0, sizeof(unsigned int), e->st) != cudaSuccess) chk(RG_ERR_CUDA);
     if (!rc && cudaMemsetAsync(e->d_hill_count, 0, sizeof(unsigned int), e->st) != cudaSuccess) chk(RG_ERR_CUDA);
+    if (!rc && cudaMemsetAsync(e->d_kerr, 0, sizeof(unsigned int), e->st) != cudaSuccess) chk(RG_ERR_CUDA);
     if (!rc && cudaStreamSynchronize(e->st) != cudaSuccess) chk(set_error(RG_ERR_CUDA, "upload"));
     if (rc) {
         free_all(e);
@@ -1512,15 +1515,20 @@ int drain(rg_ens* e, double stop)
 {
     int lrc = drain_log(e);
     if (lrc) return lrc;
-    unsigned int counts[2];
+    unsigned int counts[3];
     RG_CUDA_CHECK(cudaMemcpyAsync(&counts[0], e->d_ev_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
     RG_CUDA_CHECK(cudaMemcpyAsync(&counts[1], e->d_hill_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&counts[2], e->d_kerr, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
     std::vector<int> status;
     std::vector<unsigned int> nf0;
     int rc = download(e, status, e->d_status, e->n_sys);
     if (!rc) rc = download(e, nf0, e->d_nf0, e->n_sys);
     if (rc) return rc;
     RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    if (counts[2]) {
+        RG_CUDA_CHECK(cudaMemsetAsync(e->d_kerr, 0, sizeof(unsigned int), e->st));
+        return set_error(RG_ERR_CUDA, "a gravity tile copy did not arrive within the wait limit");
+    }
     if (counts[0] > e->ev_cap || counts[1] > e->ev_cap)
         return set_error(RG_ERR_EVENT_OVERFLOW, "ensemble event buffer full between two host synchronisations");
     if (counts[1] > 0) {

@@ -5,26 +5,24 @@
 // FP32 rate, so every FP64 operation per pair costs as much as ~64 FP32 operations.
 //
 //  * Heavy sources (the leading SI bodies: star, giant and rocky planets -- `heavy_end`
-//    per tile) contribute the exact FP64 term of the reference (sqrt, divide), summed in
-//    FP64.  They dominate every force, so their terms stay at FP64 accuracy.
+//    per tile) and near pairs (m_j / r^2 above `near_ratio` times the sink's pull from
+//    the first heavy source) contribute double-float terms (below): FP64-class accuracy
+//    computed on the FP32 pipes, added to the same compensated accumulators.
 //  * Every other pair uses the FP64 positions split into FP32 (hi, lo) pairs once per
 //    force evaluation (split_positions, O(N) FP64 work).  The displacement is
 //    (x_j^hi - x_i^hi) + (x_j^lo - x_i^lo): the hi difference is exact for neighbours
 //    (Sterbenz), so the displacement carries the FP64 positions' information down to
 //    FP32 resolution of the displacement itself.  1/r comes from the FP32 rsqrt refined
-//    by one Newton step, and the terms are summed with compensated (two-sum) FP32
-//    accumulators per component.
-//  * Near pairs (m_j / r^2 above `near_ratio` times the sink's heavy-source pull) fall
-//    back to the FP64 displacement and an FP32 rsqrt seed refined by one FP64 Newton
-//    step, summed in FP64: close approaches keep FP64-quality forces.
+//    by one Newton step, and the terms are summed in groups of 8 folded into compensated
+//    (two-sum) FP32 accumulators per component.
 //  * Event tests (collision radius, Hill sphere) are re-evaluated in FP64 for every pair
 //    whose FP32 distance is within a 1e-3 relative margin of a threshold, so the event
 //    list is decided in FP64 exactly as in the FP64 kernel.
 //
-// Work split: a CTA holds 32 sinks x 2 (lane x register) and 8 warps; warp w walks the
+// Work split: a CTA holds 32 sinks x 4 (lane x register) and 8 warps; warp w walks the
 // w-th slice of each source tile, so all 256 threads work however few sinks a tile has.
-// Sources are staged in shared memory as FP32 (hi, lo) quads; per-warp partial sums are
-// combined with two-sum at the end.
+// Sources are staged in shared memory as FP32 (hi, lo) quads; the per-warp compensated
+// partial sums are added in FP64 at the end.
 #include <algorithm>
 #include <string>
 
@@ -84,6 +82,7 @@ __device__ __forceinline__ Acc2 two_sum_merge(Acc2 a, Acc2 b)
     return a;
 }
 
+
 struct MixedArgs {
     GravArgs g;
     const SplitPos* sp;
@@ -92,6 +91,7 @@ struct MixedArgs {
     int chunk;             // sources per grid.y chunk (multiple of MX_T)
     double* partial;       // n_chunks x 3 x n_part doubles, or nullptr when grid.y == 1
     int n_part;            // row length of `partial`
+    unsigned int* err;     // set to 1 when a tile copy did not arrive within the wait limit
 };
 
 constexpr int MX_WARPS = 8;
@@ -142,272 +142,6 @@ __device__ __forceinline__ void exact_event_tests(const GravArgs& g, const Tile&
             e->r0[0] = g.px[b0]; e->r0[1] = g.py[b0]; e->r0[2] = g.pz[b0];
             e->v0[0] = g.vx[b0]; e->v0[1] = g.vy[b0]; e->v0[2] = g.vz[b0];
         }
-    }
-}
-
-struct SinkD {
-    double x, y, z, R, m, rho;
-};
-
-// FP64 displacement, FP32 rsqrt seed, one FP64 Newton step: a near pair's term
-__device__ __forceinline__ void near_term(const GravArgs& g, const SinkD& sd, int j, double& hx, double& hy,
-                                          double& hz)
-{
-    const double ddx = g.px[j] - sd.x, ddy = g.py[j] - sd.y, ddz = g.pz[j] - sd.z;
-    const double dr2 = ddx * ddx + ddy * ddy + ddz * ddz;
-    const double y0 = (double)rsqrtf((float)dr2);
-    const double y1 = y0 * (1.5 - 0.5 * dr2 * y0 * y0);
-    const double w = g.mass[j] * (y1 * y1 * y1);
-    hx += w * ddx;
-    hy += w * ddy;
-    hz += w * ddz;
-}
-
-constexpr int MX_GROUP = 8;  // sources summed in plain FP32 before each two-sum
-
-// One warp-slice of a source tile for MX_R sinks per lane.  DIAG: the slice may hold the
-// sinks themselves (self pairs are skipped); SCREEN: event screens are on.
-template <bool DIAG, bool SCREEN>
-__device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile, int j0, int q_begin, int q_end,
-                                            const float4* s_xy, const float4* s_zm, const float* s_R,
-                                            const float* s_rho, const SinkD* s_sink, const int* si,
-                                            const float* xh, const float* xl, const float* yh, const float* yl,
-                                            const float* zh, const float* zl, const float* near_lim, Acc2* ax,
-                                            Acc2* ay, Acc2* az, unsigned* near_mask, int lane)
-{
-    const GravArgs& g = a.g;
-    float px[MX_R], py[MX_R], pz[MX_R];
-#pragma unroll
-    for (int r = 0; r < MX_R; r++) {
-        px[r] = py[r] = pz[r] = 0.0f;
-        near_mask[r] = 0u;
-    }
-    for (int q = q_begin; q < q_end; q++) {
-        const float4 pxy = s_xy[q];
-        const float4 pzm = s_zm[q];
-        const float mj = pzm.z;
-        const int j = j0 + q;
-#pragma unroll
-        for (int r = 0; r < MX_R; r++) {
-            const float dx = (pxy.x - xh[r]) + (pxy.y - xl[r]);
-            const float dy = (pxy.z - yh[r]) + (pxy.w - yl[r]);
-            const float dz = (pzm.x - zh[r]) + (pzm.y - zl[r]);
-            // clamp: a merged body parked at 1e20 AU (pp_disk.cu:1184) overflows r^2 in FP32,
-            // and inf * 0 in the Newton step would poison the sum although its mass is 0
-            const float r2 = fminf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), 1.0e30f);
-            bool near = mj > near_lim[r] * r2;
-            if (DIAG) near = near && j != si[r];
-            const float y0 = rsqrt_approx(r2);
-            const float hr2 = 0.5f * r2;
-            const float y = y0 * fmaf(-hr2, y0 * y0, 1.5f);
-            float w = mj * (y * y * y);
-            if (DIAG) w = (j == si[r]) ? 0.0f : w;
-            w = near ? 0.0f : w;
-            px[r] = fmaf(w, dx, px[r]);
-            py[r] = fmaf(w, dy, py[r]);
-            pz[r] = fmaf(w, dz, pz[r]);
-            near_mask[r] |= (unsigned)near << (q - q_begin);
-            if (SCREEN) {
-                const int li = si[r] - tile.base, lj = j - tile.base;
-                if (li > 0 && li > lj && (!DIAG || j != si[r]) && mj >= 0.0f) {
-                    const SinkD& sd = s_sink[lane + 32 * r];
-                    const float margin = 1.001f;
-                    bool cand = false;
-                    if (g.record) {
-                        const float lim = (float)g.f_rad * ((float)sd.R + s_R[q]) * margin;
-                        cand = r2 < lim * lim;
-                    }
-                    if (g.hill && tile.block != 2 && lj > 0) {
-                        const float h = 0.5f * ((float)sd.rho + s_rho[q]);
-                        const float d3 = r2 * sqrtf(r2);
-                        const float inv3M = (float)(1.0 / (3.0 * g.mass[tile.base]));
-                        cand = cand || (d3 < (float)g.hill_f3 * ((float)sd.m + mj) * inv3M * (h * h * h) *
-                                                 (margin * margin * margin));
-                    }
-                    if (cand && 0 <= g.id[j])
-                        exact_event_tests(g, tile, si[r], j, sd.x, sd.y, sd.z, sd.R, sd.m, sd.rho);
-                }
-            }
-        }
-        if (((q - q_begin) & (MX_GROUP - 1)) == MX_GROUP - 1) {
-#pragma unroll
-            for (int r = 0; r < MX_R; r++) {
-                two_sum_add(ax[r], px[r]);
-                two_sum_add(ay[r], py[r]);
-                two_sum_add(az[r], pz[r]);
-                px[r] = py[r] = pz[r] = 0.0f;
-            }
-        }
-    }
-#pragma unroll
-    for (int r = 0; r < MX_R; r++) {
-        two_sum_add(ax[r], px[r]);
-        two_sum_add(ay[r], py[r]);
-        two_sum_add(az[r], pz[r]);
-    }
-}
-
-template <bool SCREEN>
-__global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
-{
-    const GravArgs& g = a.g;
-    __shared__ float4 s_xy[MX_T];
-    __shared__ float4 s_zm[MX_T];
-    __shared__ float s_R[SCREEN ? MX_T : 1];
-    __shared__ float s_rho[SCREEN ? MX_T : 1];
-    __shared__ SinkD s_sink[MX_S];
-    __shared__ double s_h[MX_WARPS][3][MX_S];  // per-warp FP64 sums: heavy sources and near pairs
-
-    const Tile tile = g.tiles[blockIdx.x];
-    if (g.sys_active && !g.sys_active[tile.sys]) return;
-    const int heavy_end = a.heavy_end[blockIdx.x];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int src_lo = tile.src_begin + blockIdx.y * a.chunk;
-    const int src_hi = min(tile.src_end, src_lo + a.chunk);
-
-    for (int s = threadIdx.x; s < MX_S; s += blockDim.x) {
-        const int i = tile.sink_begin + s;
-        SinkD sd{0, 0, 0, 0, 0, 0};
-        if (i < tile.sink_end) {
-            sd.x = g.px[i]; sd.y = g.py[i]; sd.z = g.pz[i];
-            sd.R = g.radius[i]; sd.m = g.mass[i];
-            sd.rho = g.hill ? g.rho[i] : 0.0;
-        }
-        s_sink[s] = sd;
-    }
-    for (int k = threadIdx.x; k < MX_WARPS * 3 * MX_S; k += blockDim.x) (&s_h[0][0][0])[k] = 0.0;
-    __syncthreads();
-
-    int si[MX_R];
-    float xh[MX_R], xl[MX_R], yh[MX_R], yl[MX_R], zh[MX_R], zl[MX_R], near_lim[MX_R];
-    Acc2 ax[MX_R], ay[MX_R], az[MX_R];
-#pragma unroll
-    for (int r = 0; r < MX_R; r++) {
-        const int s = lane + 32 * r;
-        const int i = tile.sink_begin + s;
-        si[r] = i;
-        xh[r] = xl[r] = yh[r] = yl[r] = zh[r] = zl[r] = 0.0f;
-        float pull = 0.0f;
-        if (i < tile.sink_end) {
-            const SplitPos sp = a.sp[i];
-            xh[r] = sp.xy.x; xl[r] = sp.xy.y; yh[r] = sp.xy.z; yl[r] = sp.xy.w;
-            zh[r] = sp.zm.x; zl[r] = sp.zm.y;
-            if (tile.src_begin < heavy_end) {  // m / r^2 of the first heavy source: the near-pair scale
-                const SinkD sd = s_sink[s];
-                const int j = tile.src_begin;
-                const double dx = g.px[j] - sd.x, dy = g.py[j] - sd.y, dz = g.pz[j] - sd.z;
-                pull = (float)(g.mass[j] / (dx * dx + dy * dy + dz * dz));
-            }
-        }
-        // a pair is near when m_j > near_lim * r^2; without a heavy source there is no scale
-        near_lim[r] = pull > 0.0f ? a.near_ratio * pull : 3.0e38f;
-        ax[r] = ay[r] = az[r] = Acc2{0.0f, 0.0f};
-    }
-
-    // heavy sources (first chunk only): exact FP64 terms, split over the warps
-    if (blockIdx.y == 0) {
-        for (int j = tile.src_begin + warp; j < heavy_end; j += MX_WARPS) {
-            const double xj = g.px[j], yj = g.py[j], zj = g.pz[j], mj = g.mass[j];
-            if (0 > g.id[j]) continue;
-#pragma unroll
-            for (int r = 0; r < MX_R; r++) {
-                const int s = lane + 32 * r;
-                if (si[r] >= tile.sink_end || j == si[r]) continue;
-                const SinkD sd = s_sink[s];
-                const double dx = xj - sd.x, dy = yj - sd.y, dz = zj - sd.z;
-                const double r2 = dx * dx + dy * dy + dz * dz;
-                const double d = sqrt(r2);
-                const double w = mj / (d * r2);
-                s_h[warp][0][s] += w * dx;
-                s_h[warp][1][s] += w * dy;
-                s_h[warp][2][s] += w * dz;
-                const int li = si[r] - tile.base, lj = j - tile.base;
-                if ((g.record && li > 0 && li > lj && d < 1.001 * g.f_rad * (sd.R + g.radius[j])) ||
-                    (g.hill && tile.block != 2 && li > 0 && li > lj && lj > 0))
-                    exact_event_tests(g, tile, si[r], j, sd.x, sd.y, sd.z, sd.R, sd.m, sd.rho);
-            }
-        }
-    }
-
-    constexpr int SLICE = MX_T / MX_WARPS;  // 32 sources per warp and tile: one near-mask bit each
-    for (int j0 = max(heavy_end, src_lo); j0 < src_hi; j0 += MX_T) {
-        const int nj = min(MX_T, src_hi - j0);
-        __syncthreads();
-        for (int q = threadIdx.x; q < nj; q += blockDim.x) {
-            const SplitPos sp = a.sp[j0 + q];
-            s_xy[q] = sp.xy;
-            s_zm[q] = sp.zm;
-            if (SCREEN) {
-                s_R[q] = (float)g.radius[j0 + q];
-                s_rho[q] = g.hill ? (float)g.rho[j0 + q] : 0.0f;
-            }
-        }
-        __syncthreads();
-        const int q_begin = warp * SLICE;
-        const int q_end = min(nj, q_begin + SLICE);
-        if (q_begin >= q_end) continue;
-        unsigned near_mask[MX_R];
-        // does this slice hold any of the CTA's sinks?
-        const bool diag = (j0 + q_begin < tile.sink_begin + MX_S) && (j0 + q_end > tile.sink_begin);
-        if (diag)
-            mixed_slice<true, SCREEN>(a, tile, j0, q_begin, q_end, s_xy, s_zm, s_R, s_rho, s_sink, si, xh, xl, yh,
-                                      yl, zh, zl, near_lim, ax, ay, az, near_mask, lane);
-        else
-            mixed_slice<false, SCREEN>(a, tile, j0, q_begin, q_end, s_xy, s_zm, s_R, s_rho, s_sink, si, xh, xl, yh,
-                                       yl, zh, zl, near_lim, ax, ay, az, near_mask, lane);
-        // near pairs of this slice: FP64 displacement, FP32 seed + one FP64 Newton step
-#pragma unroll
-        for (int r = 0; r < MX_R; r++) {
-            unsigned m = near_mask[r];
-            while (m) {
-                const int b = __ffs(m) - 1;
-                m &= m - 1;
-                const int s = lane + 32 * r;
-                double hx = 0.0, hy = 0.0, hz = 0.0;
-                near_term(g, s_sink[s], j0 + q_begin + b, hx, hy, hz);
-                s_h[warp][0][s] += hx;
-                s_h[warp][1][s] += hy;
-                s_h[warp][2][s] += hz;
-            }
-        }
-    }
-
-    // per-sink total: fixed-order sum over the warps of (FP32 compensated + FP64) partials
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < MX_R; r++) {
-        const int s = lane + 32 * r;
-        s_h[warp][0][s] += (double)ax[r].s + (double)ax[r].c;
-        s_h[warp][1][s] += (double)ay[r].s + (double)ay[r].c;
-        s_h[warp][2][s] += (double)az[r].s + (double)az[r].c;
-    }
-    __syncthreads();
-    for (int t = threadIdx.x; t < 3 * MX_S; t += blockDim.x) {
-        const int comp = t / MX_S, s = t % MX_S;
-        const int i = tile.sink_begin + s;
-        if (i >= tile.sink_end) continue;
-        double v = 0.0;
-        for (int w = 0; w < MX_WARPS; w++) v += s_h[w][comp][s];
-        if (!(0 < g.id[i])) v = 0.0;  // inactive sinks feel nothing (pp_disk.cu:235-236)
-        if (a.partial)
-            a.partial[((long long)blockIdx.y * 3 + comp) * a.n_part + i] = v;
-        else
-            (comp == 0 ? g.ax : (comp == 1 ? g.ay : g.az))[i] = v;
-    }
-}
-
-// a_i = sum over source chunks of the partials, in chunk order
-__global__ void mixed_reduce_kernel(const double* __restrict__ partial, int n_chunks, int n_part, const Tile* tiles,
-                                    int n_tiles, const int* sys_active, double* ax, double* ay, double* az)
-{
-    const Tile tile = tiles[blockIdx.x];
-    if (sys_active && !sys_active[tile.sys]) return;
-    const int i = tile.sink_begin + threadIdx.x;
-    if (i >= tile.sink_end) return;
-    for (int comp = 0; comp < 3; comp++) {
-        double v = 0.0;
-        for (int c = 0; c < n_chunks; c++) v += partial[((long long)c * 3 + comp) * n_part + i];
-        (comp == 0 ? ax : (comp == 1 ? ay : az))[i] = v;
     }
 }
 
@@ -477,6 +211,13 @@ __device__ __forceinline__ DF df_diff(float ah, float al, float bh, float bl)
 
 __device__ __forceinline__ double df_to_double(DF a) { return (double)a.hi + (double)a.lo; }
 
+// a double-float term into a compensated FP32 accumulator
+__device__ __forceinline__ void acc_df(Acc2& acc, DF t)
+{
+    two_sum_add(acc, t.hi);
+    acc.c += t.lo;
+}
+
 // the term m_j (r_j - r_i) / |r_j - r_i|^3 of one pair; r2f = |r_j - r_i|^2 in FP32
 __device__ __forceinline__ void df_term(const SplitPos& si, const SplitPos& pj, DF& tx, DF& ty, DF& tz, float& r2f)
 {
@@ -517,6 +258,361 @@ __device__ __forceinline__ void df_screen(const GravArgs& g, const Tile& tile, i
     }
     if (cand)
         exact_event_tests(g, tile, i, j, g.px[i], g.py[i], g.pz[i], g.radius[i], g.mass[i], g.hill ? g.rho[i] : 0.0);
+}
+
+struct SinkD {
+    double x, y, z, R, m, rho;
+};
+
+constexpr int MX_GROUP = 8;  // sources summed in plain FP32 before each two-sum
+
+// One warp-slice of a source tile for MX_R sinks per lane.  DIAG: the slice may hold the
+// sinks themselves (self pairs are skipped); SCREEN: event screens are on.
+template <bool DIAG, bool SCREEN>
+__device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile, int j0, int q_begin, int q_end,
+                                            const SplitPos* s_sp, const float* s_R,
+                                            const float* s_rho, const SinkD* s_sink, const int* si,
+                                            const float* xh, const float* xl, const float* yh, const float* yl,
+                                            const float* zh, const float* zl, const float* near_lim, Acc2* ax,
+                                            Acc2* ay, Acc2* az, unsigned* near_mask, int lane)
+{
+    const GravArgs& g = a.g;
+    float px[MX_R], py[MX_R], pz[MX_R];
+#pragma unroll
+    for (int r = 0; r < MX_R; r++) {
+        px[r] = py[r] = pz[r] = 0.0f;
+        near_mask[r] = 0u;
+    }
+    for (int q = q_begin; q < q_end; q++) {
+        const float4 pxy = s_sp[q].xy;
+        const float4 pzm = s_sp[q].zm;
+        const float mj = pzm.z;
+        const int j = j0 + q;
+#pragma unroll
+        for (int r = 0; r < MX_R; r++) {
+            const float dx = (pxy.x - xh[r]) + (pxy.y - xl[r]);
+            const float dy = (pxy.z - yh[r]) + (pxy.w - yl[r]);
+            const float dz = (pzm.x - zh[r]) + (pzm.y - zl[r]);
+            // clamp: a merged body parked at 1e20 AU (pp_disk.cu:1184) overflows r^2 in FP32,
+            // and inf * 0 in the Newton step would poison the sum although its mass is 0
+            const float r2 = fminf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), 1.0e30f);
+            bool near = mj > near_lim[r] * r2;
+            if (DIAG) near = near && j != si[r];
+            const float y0 = rsqrt_approx(r2);
+            const float hr2 = 0.5f * r2;
+            const float y = y0 * fmaf(-hr2, y0 * y0, 1.5f);
+            float w = mj * (y * y * y);
+            if (DIAG) w = (j == si[r]) ? 0.0f : w;
+            w = near ? 0.0f : w;
+            px[r] = fmaf(w, dx, px[r]);
+            py[r] = fmaf(w, dy, py[r]);
+            pz[r] = fmaf(w, dz, pz[r]);
+            near_mask[r] |= (unsigned)near << (q - q_begin);
+            if (SCREEN) {
+                const int li = si[r] - tile.base, lj = j - tile.base;
+                if (li > 0 && li > lj && (!DIAG || j != si[r]) && mj >= 0.0f) {
+                    const SinkD& sd = s_sink[lane + 32 * r];
+                    const float margin = 1.001f;
+                    bool cand = false;
+                    if (g.record) {
+                        const float lim = (float)g.f_rad * ((float)sd.R + s_R[q]) * margin;
+                        cand = r2 < lim * lim;
+                    }
+                    if (g.hill && tile.block != 2 && lj > 0) {
+                        const float h = 0.5f * ((float)sd.rho + s_rho[q]);
+                        const float d3 = r2 * sqrtf(r2);
+                        const float inv3M = (float)(1.0 / (3.0 * g.mass[tile.base]));
+                        cand = cand || (d3 < (float)g.hill_f3 * ((float)sd.m + mj) * inv3M * (h * h * h) *
+                                                 (margin * margin * margin));
+                    }
+                    if (cand && 0 <= g.id[j])
+                        exact_event_tests(g, tile, si[r], j, sd.x, sd.y, sd.z, sd.R, sd.m, sd.rho);
+                }
+            }
+        }
+        if (((q - q_begin) & (MX_GROUP - 1)) == MX_GROUP - 1) {
+#pragma unroll
+            for (int r = 0; r < MX_R; r++) {
+                two_sum_add(ax[r], px[r]);
+                two_sum_add(ay[r], py[r]);
+                two_sum_add(az[r], pz[r]);
+                px[r] = py[r] = pz[r] = 0.0f;
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < MX_R; r++) {
+        two_sum_add(ax[r], px[r]);
+        two_sum_add(ay[r], py[r]);
+        two_sum_add(az[r], pz[r]);
+    }
+}
+
+// Source tiles reach shared memory by TMA bulk copies (cp.async.bulk, one thread issues an
+// 8 KB copy of MX_T split positions), double-buffered: tile t + 2 is requested while tile t
+// is computed, each buffer's arrival is signalled on its own mbarrier (transaction bytes),
+// and one CTA barrier per tile releases the buffer for reuse.  Every wait on a copy is
+// bounded (MX_WAIT_POLLS polls); a CTA whose copy does not arrive sets a.err, waits (again
+// bounded) for the copies it issued, and returns.
+constexpr unsigned MX_WAIT_POLLS = 1u << 24;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned phase)
+{
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned phase)
+{
+    for (unsigned k = 0; k < MX_WAIT_POLLS; k++)
+        if (mbar_try_wait(bar, phase)) return true;
+    return false;
+}
+
+// one thread: expect `bytes` on `bar` and start the bulk copy global -> shared
+__device__ __forceinline__ void tma_tile(void* dst, const void* src, unsigned bytes, unsigned long long* bar)
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// dynamic shared memory of grav_mixed_kernel
+struct MixedSmem {
+    SplitPos sp[2][MX_T];              // double-buffered source tiles (TMA destination)
+    SinkD sink[MX_S];
+    Acc2 part[MX_WARPS][3][MX_S];      // per-warp compensated partial sums
+    float R[2][MX_T], rho[2][MX_T];    // screening data of the tiles (SCREEN only)
+    unsigned long long bar[2];
+    int fail;
+};
+
+template <bool SCREEN>
+__global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
+{
+    const GravArgs& g = a.g;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    MixedSmem& S = *reinterpret_cast<MixedSmem*>(smem_raw);
+
+    const Tile tile = g.tiles[blockIdx.x];
+    if (g.sys_active && !g.sys_active[tile.sys]) return;
+    const int heavy_end = a.heavy_end[blockIdx.x];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int src_lo = tile.src_begin + blockIdx.y * a.chunk;
+    const int src_hi = min(tile.src_end, src_lo + a.chunk);
+    const int first = max(heavy_end, src_lo);
+    const int n_tiles = first < src_hi ? (src_hi - first + MX_T - 1) / MX_T : 0;
+
+    auto issue = [&](int t) {  // one thread
+        const int j0 = first + t * MX_T;
+        const int nj = min(MX_T, src_hi - j0);
+        tma_tile(&S.sp[t & 1][0], a.sp + j0, (unsigned)(nj * sizeof(SplitPos)), &S.bar[t & 1]);
+    };
+    auto stage_screen = [&](int t) {  // all threads
+        const int j0 = first + t * MX_T;
+        const int nj = min(MX_T, src_hi - j0);
+        for (int q = threadIdx.x; q < nj; q += blockDim.x) {
+            S.R[t & 1][q] = (float)g.radius[j0 + q];
+            S.rho[t & 1][q] = g.hill ? (float)g.rho[j0 + q] : 0.0f;
+        }
+    };
+
+    if (threadIdx.x == 0) {
+        mbar_init(&S.bar[0], 1);
+        mbar_init(&S.bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        S.fail = 0;
+    }
+    for (int s = threadIdx.x; s < MX_S; s += blockDim.x) {
+        const int i = tile.sink_begin + s;
+        SinkD sd{0, 0, 0, 0, 0, 0};
+        if (i < tile.sink_end) {
+            sd.x = g.px[i]; sd.y = g.py[i]; sd.z = g.pz[i];
+            sd.R = g.radius[i]; sd.m = g.mass[i];
+            sd.rho = g.hill ? g.rho[i] : 0.0;
+        }
+        S.sink[s] = sd;
+    }
+    __syncthreads();
+    // the first two tiles travel while the heavy sources are summed
+    if (threadIdx.x == 0) {
+        if (n_tiles > 0) issue(0);
+        if (n_tiles > 1) issue(1);
+    }
+    if (SCREEN) {
+        if (n_tiles > 0) stage_screen(0);
+        if (n_tiles > 1) stage_screen(1);
+    }
+
+    int si[MX_R];
+    float xh[MX_R], xl[MX_R], yh[MX_R], yl[MX_R], zh[MX_R], zl[MX_R], near_lim[MX_R];
+    Acc2 ax[MX_R], ay[MX_R], az[MX_R];
+#pragma unroll
+    for (int r = 0; r < MX_R; r++) {
+        const int s = lane + 32 * r;
+        const int i = tile.sink_begin + s;
+        si[r] = i;
+        xh[r] = xl[r] = yh[r] = yl[r] = zh[r] = zl[r] = 0.0f;
+        float pull = 0.0f;
+        if (i < tile.sink_end) {
+            const SplitPos sp = a.sp[i];
+            xh[r] = sp.xy.x; xl[r] = sp.xy.y; yh[r] = sp.xy.z; yl[r] = sp.xy.w;
+            zh[r] = sp.zm.x; zl[r] = sp.zm.y;
+            if (tile.src_begin < heavy_end) {  // m / r^2 of the first heavy source: the near-pair scale
+                const SinkD sd = S.sink[s];
+                const int j = tile.src_begin;
+                const double dx = g.px[j] - sd.x, dy = g.py[j] - sd.y, dz = g.pz[j] - sd.z;
+                pull = (float)(g.mass[j] / (dx * dx + dy * dy + dz * dz));
+            }
+        }
+        // a pair is near when m_j > near_lim * r^2; without a heavy source there is no scale
+        near_lim[r] = pull > 0.0f ? a.near_ratio * pull : 3.0e38f;
+        ax[r] = ay[r] = az[r] = Acc2{0.0f, 0.0f};
+    }
+
+    // heavy sources (first chunk only): double-float terms, split over the warps
+    if (blockIdx.y == 0) {
+        for (int j = tile.src_begin + warp; j < heavy_end; j += MX_WARPS) {
+            if (0 > g.id[j]) continue;
+            const SplitPos pj = a.sp[j];
+            float Rj = 0.0f, rhoj = 0.0f;
+            if (SCREEN) {
+                Rj = (float)g.radius[j];
+                rhoj = g.hill ? (float)g.rho[j] : 0.0f;
+            }
+#pragma unroll
+            for (int r = 0; r < MX_R; r++) {
+                const int s = lane + 32 * r;
+                if (si[r] >= tile.sink_end || j == si[r]) continue;
+                SplitPos sp;
+                sp.xy = make_float4(xh[r], xl[r], yh[r], yl[r]);
+                sp.zm = make_float4(zh[r], zl[r], 0.0f, 0.0f);
+                DF tx, ty, tz;
+                float r2f;
+                df_term(sp, pj, tx, ty, tz, r2f);
+                acc_df(ax[r], tx);
+                acc_df(ay[r], ty);
+                acc_df(az[r], tz);
+                if (SCREEN) {
+                    const SinkD& sd = S.sink[s];
+                    df_screen(g, tile, si[r], j, r2f, (float)sd.R, Rj, (float)sd.rho, rhoj, (float)sd.m, pj.zm.z,
+                              (float)(1.0 / (3.0 * g.mass[tile.base])));
+                }
+            }
+        }
+    }
+    if (SCREEN) __syncthreads();  // the screening data of tiles 0 and 1 are visible
+
+    constexpr int SLICE = MX_T / MX_WARPS;  // 32 sources per warp and tile: one near-mask bit each
+    int t = 0;
+    for (; t < n_tiles; t++) {
+        const int b = t & 1;
+        const int j0 = first + t * MX_T;
+        const int nj = min(MX_T, src_hi - j0);
+        const bool arrived = mbar_wait(&S.bar[b], (unsigned)((t >> 1) & 1));
+        if (!arrived) S.fail = 1;
+        const int q_begin = warp * SLICE;
+        const int q_end = min(nj, q_begin + SLICE);
+        if (arrived && q_begin < q_end) {
+            unsigned near_mask[MX_R];
+            // does this slice hold any of the CTA's sinks?
+            const bool diag = (j0 + q_begin < tile.sink_begin + MX_S) && (j0 + q_end > tile.sink_begin);
+            if (diag)
+                mixed_slice<true, SCREEN>(a, tile, j0, q_begin, q_end, S.sp[b], S.R[b], S.rho[b], S.sink, si, xh, xl,
+                                          yh, yl, zh, zl, near_lim, ax, ay, az, near_mask, lane);
+            else
+                mixed_slice<false, SCREEN>(a, tile, j0, q_begin, q_end, S.sp[b], S.R[b], S.rho[b], S.sink, si, xh,
+                                           xl, yh, yl, zh, zl, near_lim, ax, ay, az, near_mask, lane);
+            // near pairs of this slice: the double-float term (FP64-class accuracy on the FP32 pipes)
+#pragma unroll
+            for (int r = 0; r < MX_R; r++) {
+                unsigned m = near_mask[r];
+                if (!m) continue;
+                SplitPos sp;
+                sp.xy = make_float4(xh[r], xl[r], yh[r], yl[r]);
+                sp.zm = make_float4(zh[r], zl[r], 0.0f, 0.0f);
+                while (m) {
+                    const int bit = __ffs(m) - 1;
+                    m &= m - 1;
+                    DF tx, ty, tz;
+                    float r2f;
+                    df_term(sp, S.sp[b][q_begin + bit], tx, ty, tz, r2f);
+                    acc_df(ax[r], tx);
+                    acc_df(ay[r], ty);
+                    acc_df(az[r], tz);
+                }
+            }
+        }
+        __syncthreads();  // buffer b is free; the fail flag is visible
+        if (S.fail) break;
+        // tile t + 2 into buffer b; its screening data become visible at the next iteration's barrier
+        if (t + 2 < n_tiles) {
+            if (threadIdx.x == 0) issue(t + 2);
+            if (SCREEN) stage_screen(t + 2);
+        }
+    }
+    if (S.fail) {
+        if (threadIdx.x == 0) {
+            atomicExch(a.err, 1u);
+            // the copies this CTA issued and did not consume: tiles t and t + 1
+            for (int u = t; u < min(t + 2, n_tiles); u++) mbar_wait(&S.bar[u & 1], (unsigned)((u >> 1) & 1));
+        }
+        return;
+    }
+
+    // per-sink total: fixed-order sum over the warps of the compensated partials
+#pragma unroll
+    for (int r = 0; r < MX_R; r++) {
+        const int s = lane + 32 * r;
+        S.part[warp][0][s] = ax[r];
+        S.part[warp][1][s] = ay[r];
+        S.part[warp][2][s] = az[r];
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 3 * MX_S; k += blockDim.x) {
+        const int comp = k / MX_S, s = k % MX_S;
+        const int i = tile.sink_begin + s;
+        if (i >= tile.sink_end) continue;
+        double v = 0.0;
+        for (int w = 0; w < MX_WARPS; w++) v += (double)S.part[w][comp][s].s + (double)S.part[w][comp][s].c;
+        if (!(0 < g.id[i])) v = 0.0;  // inactive sinks feel nothing (pp_disk.cu:235-236)
+        if (a.partial)
+            a.partial[((long long)blockIdx.y * 3 + comp) * a.n_part + i] = v;
+        else
+            (comp == 0 ? g.ax : (comp == 1 ? g.ay : g.az))[i] = v;
+    }
+}
+
+// a_i = sum over source chunks of the partials, in chunk order
+__global__ void mixed_reduce_kernel(const double* __restrict__ partial, int n_chunks, int n_part, const Tile* tiles,
+                                    int n_tiles, const int* sys_active, double* ax, double* ay, double* az)
+{
+    const Tile tile = tiles[blockIdx.x];
+    if (sys_active && !sys_active[tile.sys]) return;
+    const int i = tile.sink_begin + threadIdx.x;
+    if (i >= tile.sink_end) return;
+    for (int comp = 0; comp < 3; comp++) {
+        double v = 0.0;
+        for (int c = 0; c < n_chunks; c++) v += partial[((long long)c * 3 + comp) * n_part + i];
+        (comp == 0 ? ax : (comp == 1 ? ay : az))[i] = v;
+    }
 }
 
 // Row kernel: one thread per sink, the tile's sources (a few massive bodies) staged in
@@ -745,10 +841,18 @@ int launch_split_positions(const double* x, const double* y, const double* z, co
 }
 
 int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* heavy_end, float near_ratio,
-                            int n_chunks, int chunk, double* partial, int n_part, cudaStream_t st)
+                            int n_chunks, int chunk, double* partial, int n_part, unsigned int* err, cudaStream_t st)
 {
     if (g.n_tiles <= 0) return 0;
+    constexpr int smem = (int)sizeof(MixedSmem);
+    static bool attr_set = false;
+    if (!attr_set) {
+        RG_CUDA_CHECK(cudaFuncSetAttribute(grav_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        RG_CUDA_CHECK(cudaFuncSetAttribute(grav_mixed_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr_set = true;
+    }
     MixedArgs a;
+    a.err = err;
     a.g = g;
     a.sp = (const SplitPos*)split;
     a.heavy_end = heavy_end;
@@ -758,9 +862,9 @@ int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* hea
     a.n_part = n_part;
     const dim3 grid(g.n_tiles, n_chunks > 1 ? n_chunks : 1);
     if (g.record || g.hill)
-        grav_mixed_kernel<true><<<grid, 256, 0, st>>>(a);
+        grav_mixed_kernel<true><<<grid, 256, smem, st>>>(a);
     else
-        grav_mixed_kernel<false><<<grid, 256, 0, st>>>(a);
+        grav_mixed_kernel<false><<<grid, 256, smem, st>>>(a);
     RG_CUDA_CHECK(cudaGetLastError());
     if (n_chunks > 1) {
         mixed_reduce_kernel<<<g.n_tiles, MX_S, 0, st>>>(partial, n_chunks, n_part, g.tiles, g.n_tiles, g.sys_active,

@@ -78,7 +78,8 @@ constexpr size_t SPLIT_POS_BYTES = 32;  // per body
 int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id, int n,
                            struct SplitPos* out, cudaStream_t st);
 int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* heavy_end, float near_ratio,
-                            int n_chunks, int chunk, double* partial, int n_part, cudaStream_t st);
+                            int n_chunks, int chunk, double* partial, int n_part, unsigned int* err,
+                            cudaStream_t st);
 // heavy pairs of the mixed-precision mode in double-float arithmetic (gravity_mixed.cu):
 // the row kernel for blocks with a few massive sources, the few-sink kernel for the
 // star's and giants' own rows (partial: 3 x rows x pitch doubles, pitch >= source chunks)
