@@ -40,18 +40,33 @@ struct SplitPos {
 };
 
 // inactive bodies (id < 0, pp_disk.cu:242) get mass 0 here, so the pair loop needs no
-// per-pair activity test: their terms vanish
+// per-pair activity test: their terms vanish.  Coordinates beyond 1e15 AU are clamped
+// there (a merged body is parked at 1e20 AU, pp_disk.cu:1184, and a hit-star merger stays
+// active with m = 0 until the next ejection check): |r|^2 then stays finite in FP32, so
+// the pair loop needs no clamp either, and such a body's zero mass gives a zero term.
+__device__ __forceinline__ void split_coord(double v, float& hi, float& lo)
+{
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+    if (fabsf(hi) > 1.0e15f) {
+        hi = copysignf(1.0e15f, hi);
+        lo = 0.0f;
+    }
+}
+
 __global__ void split_positions_kernel(const double* __restrict__ x, const double* __restrict__ y,
                                        const double* __restrict__ z, const double* __restrict__ m,
                                        const int* __restrict__ id, int n, SplitPos* __restrict__ out)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    const double xd = x[i], yd = y[i], zd = z[i];
-    const float xh = (float)xd, yh = (float)yd, zh = (float)zd;
-    out[i].xy = make_float4(xh, (float)(xd - (double)xh), yh, (float)(yd - (double)yh));
+    float xh, xl, yh, yl, zh, zl;
+    split_coord(x[i], xh, xl);
+    split_coord(y[i], yh, yl);
+    split_coord(z[i], zh, zl);
+    out[i].xy = make_float4(xh, xl, yh, yl);
     const float mh = id[i] < 0 ? 0.0f : (float)m[i];
-    out[i].zm = make_float4(zh, (float)(zd - (double)zh), mh, id[i] < 0 ? 0.0f : (float)(m[i] - (double)mh));
+    out[i].zm = make_float4(zh, zl, mh, id[i] < 0 ? 0.0f : (float)(m[i] - (double)mh));
 }
 
 __device__ __forceinline__ float rsqrt_approx(float x)
@@ -264,7 +279,7 @@ struct SinkD {
     double x, y, z, R, m, rho;
 };
 
-constexpr int MX_GROUP = 8;  // sources summed in plain FP32 before each two-sum
+constexpr int MX_GROUP = 16;  // sources summed in plain FP32 before each two-sum
 
 // One warp-slice of a source tile for MX_R sinks per lane.  DIAG: the slice may hold the
 // sinks themselves (self pairs are skipped); SCREEN: event screens are on.
@@ -293,9 +308,8 @@ __device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile
             const float dx = (pxy.x - xh[r]) + (pxy.y - xl[r]);
             const float dy = (pxy.z - yh[r]) + (pxy.w - yl[r]);
             const float dz = (pzm.x - zh[r]) + (pzm.y - zl[r]);
-            // clamp: a merged body parked at 1e20 AU (pp_disk.cu:1184) overflows r^2 in FP32,
-            // and inf * 0 in the Newton step would poison the sum although its mass is 0
-            const float r2 = fminf(fmaf(dx, dx, fmaf(dy, dy, dz * dz)), 1.0e30f);
+            // finite: split_positions clamps coordinates to 1e15 AU
+            const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             bool near = mj > near_lim[r] * r2;
             if (DIAG) near = near && j != si[r];
             const float y0 = rsqrt_approx(r2);
@@ -340,11 +354,13 @@ __device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile
             }
         }
     }
+    if (((q_end - q_begin) & (MX_GROUP - 1)) != 0) {  // a partial last group (uniform over the warp)
 #pragma unroll
-    for (int r = 0; r < MX_R; r++) {
-        two_sum_add(ax[r], px[r]);
-        two_sum_add(ay[r], py[r]);
-        two_sum_add(az[r], pz[r]);
+        for (int r = 0; r < MX_R; r++) {
+            two_sum_add(ax[r], px[r]);
+            two_sum_add(ay[r], py[r]);
+            two_sum_add(az[r], pz[r]);
+        }
     }
 }
 
