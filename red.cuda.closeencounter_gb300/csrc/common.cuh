@@ -53,6 +53,7 @@ struct GravArgs {
     const double* __restrict__ radius;
     const int* __restrict__ id;
     const double* __restrict__ rho;  // |r_i - r_0| of the step-start state (Hill test)
+    const float* __restrict__ rf;    // mixed mode: radii in FP32 (event screens), else nullptr
     double* ax;  // output rows
     double* ay;
     double* az;

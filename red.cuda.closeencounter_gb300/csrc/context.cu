@@ -66,6 +66,7 @@ struct rg_ctx {
     int* d_heavy = nullptr;  // per mixed tile: end of its heavy sources
     int tiles_cap = 0;
     void* d_split = nullptr;  // FP32 (hi, lo) positions of the mixed kernel
+    float* d_rf = nullptr;    // FP32 radii of the mixed kernels' event screens
     DevEvent* d_ev = nullptr;
     unsigned int* d_ev_count = nullptr;
     DevEvent* d_hill = nullptr;
@@ -119,6 +120,7 @@ struct rg_ctx {
         int row_base;   // few-sink groups: first row in the terms buffer
         int rows;       // few-sink groups: rows
         int max_src;    // few-sink groups: largest source count of a tile
+        int max_sinks;  // few-sink groups: widest tile
     };
     std::vector<Group> plan[2];
     std::vector<Tile> tiles;       // all groups' tiles, uploaded to d_tiles
@@ -178,6 +180,7 @@ void free_all(rg_ctx* c)
     cudaFree(c->d_tiles);
     cudaFree(c->d_heavy);
     cudaFree(c->d_split);
+    cudaFree(c->d_rf);
     cudaFree(c->d_terms);
     cudaFree(c->d_partial);
     cudaFree(c->d_row_sink);
@@ -331,7 +334,7 @@ void build_tiles(rg_ctx* c)
 
     auto add_group = [&](int mode, int kind, int s0, int s1, int src1, int block, int step) {
         if (s1 <= s0) return;
-        rg_ctx::Group gr{kind, c->tiles.size(), 0, c->few_rows, 0, src1};
+        rg_ctx::Group gr{kind, c->tiles.size(), 0, c->few_rows, 0, src1, std::min(step, s1 - s0)};
         for (int s = s0; s < s1; s += step) {
             c->tiles.push_back(Tile{s, std::min(s + step, s1), 0, src1, 0, 0, block, 0});
             c->heavy_mx.push_back(kind == GROUP_MIXED ? std::min(n_heavy, src1) : 0);
@@ -449,6 +452,7 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
     g.radius = c->d_radius;
     g.id = c->d_id;
     g.rho = c->d_rho;
+    g.rf = c->gravity_mode == RG_GRAVITY_MIXED ? c->d_rf : nullptr;
     g.ax = acc;
     g.ay = acc + cap;
     g.az = acc + 2 * cap;
@@ -490,7 +494,8 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
         case GROUP_DF_ROWSEQ:
         case GROUP_DF_FEW:
             if (!split_done) {
-                rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, c->n_total(), (SplitPos*)c->d_split, c->st);
+                rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, c->d_radius, c->n_total(),
+                                            (SplitPos*)c->d_split, c->d_rf, c->st);
                 split_done = true;
                 c->n_kernels++;
             }
@@ -499,7 +504,8 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
                 rc = launch_grav_df_rowseq(g, c->d_split, c->st);
                 c->n_kernels++;
             } else {
-                rc = launch_grav_df_few(g, c->d_split, c->d_few_row0 + gr.off, gr.max_src, c->d_terms, c->few_rows,
+                rc = launch_grav_df_few(g, c->d_split, c->d_few_row0 + gr.off, gr.max_src, gr.max_sinks, c->d_terms,
+                                        c->few_rows,
                                         c->few_pitch, c->d_row_sink, c->d_row_nsrc, nullptr, gr.row_base, gr.rows,
                                         c->st);
                 c->n_kernels += 2;
@@ -507,7 +513,8 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
             break;
         case GROUP_MIXED:
             if (!split_done) {
-                rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, c->n_total(), (SplitPos*)c->d_split, c->st);
+                rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, c->d_radius, c->n_total(),
+                                            (SplitPos*)c->d_split, c->d_rf, c->st);
                 split_done = true;
                 c->n_kernels++;
             }
@@ -1269,6 +1276,7 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
     chk(dalloc(&c->d_dt, 1));
     chk(dalloc(&c->d_part, (size_t)5 * nt));
     chk(dalloc((char**)&c->d_split, SPLIT_POS_BYTES * (size_t)nt));
+    chk(dalloc(&c->d_rf, nt));
     if (!rc && cudaMallocHost((void**)&c->h_pin, 8 * sizeof(double)) != cudaSuccess)
         chk(set_error(RG_ERR_NOMEM, "pinned host buffer"));
     if (rc) {

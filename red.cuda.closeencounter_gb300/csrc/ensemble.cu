@@ -516,6 +516,7 @@ struct rg_ens {
     int* d_id = nullptr;
     int* d_type = nullptr;
     void* d_split = nullptr;
+    float* d_rf = nullptr;  // FP32 radii of the mixed kernels' event screens
     double* d_partial = nullptr;
     size_t partial_cap = 0;
     double* d_thr = nullptr;
@@ -535,6 +536,7 @@ struct rg_ens {
         size_t off;
         int n;
         int row_base, rows, max_src;
+        int max_sinks = 0;  // few-sink groups: widest tile
     };
     std::vector<Group> plan[2];
     std::vector<Tile> tiles;
@@ -645,7 +647,7 @@ void free_all(rg_ens* e)
                     e->d_ev, e->d_ev_count, e->d_hill, e->d_hill_count, e->d_part, e->d_base_of, e->d_log,
                     e->d_log_count, e->d_feat, e->d_dt_last, e->d_ideal_last, e->d_hist, e->d_proposed, e->d_step_prop_rej,
                     e->d_prop_rej_steps, e->d_cool, e->d_nprop, e->d_nprop_acc, e->d_nfallback, e->d_amax,
-                    e->d_hill3, e->d_nsi_of, e->d_kerr};
+                    e->d_hill3, e->d_nsi_of, e->d_kerr, e->d_rf};
     for (void* q : ptrs) cudaFree(q);
     for (auto& k : e->d_k) cudaFree(k);
     if (e->st) cudaStreamDestroy(e->st);
@@ -734,6 +736,7 @@ void build_gravity_plan(rg_ens* e)
                         gr.rows++;
                     }
                     gr.max_src = std::max(gr.max_src, nsrc);
+                    gr.max_sinks = std::max(gr.max_sinks, T[k].sink_end - T[k].sink_begin);
                     e->few_pitch = std::max<long long>(e->few_pitch, nsrc);
                 } else {
                     e->few_row0.push_back(0);
@@ -806,6 +809,7 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
     g.radius = e->d_radius;
     g.id = e->d_id;
     g.rho = e->d_rho;
+    g.rf = e->gravity_mode == RG_GRAVITY_MIXED ? e->d_rf : nullptr;
     g.ax = acc;
     g.ay = acc + cap;
     g.az = acc + 2 * cap;
@@ -846,7 +850,8 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
         case GROUP_DF_ROWSEQ:
         case GROUP_DF_FEW:
             if (!split_done) {
-                rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->cap, (SplitPos*)e->d_split, e->st);
+                rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->d_radius, e->cap,
+                                            (SplitPos*)e->d_split, e->d_rf, e->st);
                 split_done = true;
                 e->n_kernels++;
             }
@@ -855,7 +860,8 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
                 rc = launch_grav_df_rowseq(g, e->d_split, e->st);
                 e->n_kernels++;
             } else {
-                rc = launch_grav_df_few(g, e->d_split, e->d_few_row0 + gr.off, gr.max_src, e->d_terms, e->few_rows,
+                rc = launch_grav_df_few(g, e->d_split, e->d_few_row0 + gr.off, gr.max_src, gr.max_sinks, e->d_terms,
+                                        e->few_rows,
                                         e->few_pitch, e->d_row_sink, e->d_row_nsrc, e->d_row_sys, gr.row_base, gr.rows,
                                         e->st);
                 e->n_kernels += 2;
@@ -863,7 +869,8 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
             break;
         case GROUP_MIXED:
             if (!split_done) {
-                rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->cap, (SplitPos*)e->d_split, e->st);
+                rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->d_radius, e->cap,
+                                            (SplitPos*)e->d_split, e->d_rf, e->st);
                 split_done = true;
                 e->n_kernels++;
             }
@@ -1317,6 +1324,7 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     chk(dalloc(&e->d_type, nt));
     chk(dalloc(&e->d_base_of, nt));
     chk(dalloc((char**)&e->d_split, SPLIT_POS_BYTES * nt));
+    chk(dalloc(&e->d_rf, nt));
     chk(dalloc(&e->d_thr, 5 * ns));
     chk(dalloc(&e->d_status, ns));
     chk(dalloc(&e->d_active, ns));

@@ -44,29 +44,69 @@ struct SplitPos {
 // there (a merged body is parked at 1e20 AU, pp_disk.cu:1184, and a hit-star merger stays
 // active with m = 0 until the next ejection check): |r|^2 then stays finite in FP32, so
 // the pair loop needs no clamp either, and such a body's zero mass gives a zero term.
+//
+// The split is done on the bit patterns, with integer operations only (a conversion
+// FP64 -> FP32 runs on GB300's scarce FP64 pipe): hi = v rounded to 24 significant bits
+// (round half up on the dropped 29 bits; a carry into the exponent is the correct next
+// value), lo = the signed remainder rounded to FP32, so |v - (hi + lo)| <= 2^-48 |v| and hi
+// carries no bias.  |v| < 2^-74 gives lo = 0 and |v| < 2^-126 gives hi = lo = 0.
+__device__ __forceinline__ void split_bits(double v, float& hi, float& lo)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7ffu);
+    const int ef = e - 896;  // FP32 biased exponent
+    if (ef <= 0) {
+        hi = lo = 0.0f;
+        return;
+    }
+    if (ef >= 254) {  // at or beyond FP32's largest binade, or inf / NaN
+        hi = (float)v;
+        lo = 0.0f;
+        return;
+    }
+    const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+    unsigned hb = sign | ((unsigned)ef << 23) | (unsigned)(mant >> 29);
+    int r = (int)(mant & 0x1FFFFFFFu);  // the dropped bits, in units of 2^(e - 1075)
+    if (r >= (1 << 28)) {
+        hb += 1u;
+        r -= 1 << 29;
+    }
+    hi = __uint_as_float(hb);
+    const int es = e - 948;  // FP32 biased exponent of 2^(e - 1075)
+    const float l = es > 0 ? __int2float_rn(r) * __uint_as_float((unsigned)es << 23) : 0.0f;
+    lo = sign ? -l : l;
+}
+
 __device__ __forceinline__ void split_coord(double v, float& hi, float& lo)
 {
-    hi = (float)v;
-    lo = (float)(v - (double)hi);
+    split_bits(v, hi, lo);
     if (fabsf(hi) > 1.0e15f) {
         hi = copysignf(1.0e15f, hi);
         lo = 0.0f;
     }
 }
 
+// rf (optional): the radii rounded to FP32, for the event screens
 __global__ void split_positions_kernel(const double* __restrict__ x, const double* __restrict__ y,
                                        const double* __restrict__ z, const double* __restrict__ m,
-                                       const int* __restrict__ id, int n, SplitPos* __restrict__ out)
+                                       const int* __restrict__ id, const double* __restrict__ radius, int n,
+                                       SplitPos* __restrict__ out, float* __restrict__ rf)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    float xh, xl, yh, yl, zh, zl;
+    float xh, xl, yh, yl, zh, zl, mh = 0.0f, ml = 0.0f;
     split_coord(x[i], xh, xl);
     split_coord(y[i], yh, yl);
     split_coord(z[i], zh, zl);
+    if (id[i] >= 0) split_bits(m[i], mh, ml);
     out[i].xy = make_float4(xh, xl, yh, yl);
-    const float mh = id[i] < 0 ? 0.0f : (float)m[i];
-    out[i].zm = make_float4(zh, zl, mh, id[i] < 0 ? 0.0f : (float)(m[i] - (double)mh));
+    out[i].zm = make_float4(zh, zl, mh, ml);
+    if (rf) {
+        float rh, rl;
+        split_bits(radius[i], rh, rl);
+        rf[i] = rh;
+    }
 }
 
 __device__ __forceinline__ float rsqrt_approx(float x)
@@ -224,7 +264,26 @@ __device__ __forceinline__ DF df_diff(float ah, float al, float bh, float bl)
     return df_two_sum(s.hi, (al - bl) + s.lo);
 }
 
-__device__ __forceinline__ double df_to_double(DF a) { return (double)a.hi + (double)a.lo; }
+// FP32 -> FP64 on the bit pattern (exact; no FP64-pipe conversion); FP32 denormals -> 0
+__device__ __forceinline__ double f2d_bits(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned ef = (u >> 23) & 0xffu;
+    if (ef == 0) return 0.0;
+    if (ef == 255) return (double)f;
+    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
+                                 ((unsigned long long)(ef + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)b);
+}
+
+__device__ __forceinline__ double df_to_double(DF a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
+
+// |r_i - r_base| in FP32 from the split positions' leading parts (event screens)
+__device__ __forceinline__ float star_dist_f(const SplitPos& pi, const SplitPos& p0)
+{
+    const float dx = pi.xy.x - p0.xy.x, dy = pi.xy.z - p0.xy.z, dz = pi.zm.x - p0.zm.x;
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+}
 
 // a double-float term into a compensated FP32 accumulator
 __device__ __forceinline__ void acc_df(Acc2& acc, DF t)
@@ -445,8 +504,8 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
         const int j0 = first + t * MX_T;
         const int nj = min(MX_T, src_hi - j0);
         for (int q = threadIdx.x; q < nj; q += blockDim.x) {
-            S.R[t & 1][q] = (float)g.radius[j0 + q];
-            S.rho[t & 1][q] = g.hill ? (float)g.rho[j0 + q] : 0.0f;
+            S.R[t & 1][q] = g.rf[j0 + q];
+            S.rho[t & 1][q] = g.hill ? star_dist_f(a.sp[j0 + q], a.sp[tile.base]) : 0.0f;
         }
     };
 
@@ -648,16 +707,20 @@ __global__ void __launch_bounds__(DF_ROW_NT) grav_df_rowseq(GravArgs g, const Sp
     const bool sink_ok = i < tile.sink_end;
     const bool active = sink_ok && 0 < g.id[i];
     SplitPos si{};
-    float Ri = 0.0f, rhoi = 0.0f, mi = 0.0f;
+    float Ri = 0.0f, rhoi = 0.0f, mi = 0.0f, inv3M = 0.0f;
+    SplitPos p0{};
+    if (SCREEN && g.hill) {
+        p0 = sp[tile.base];
+        inv3M = 1.0f / (3.0f * p0.zm.z);
+    }
     if (active) {
         si = sp[i];
         if (SCREEN) {
-            Ri = (float)g.radius[i];
-            rhoi = g.hill ? (float)g.rho[i] : 0.0f;
-            mi = (float)g.mass[i];
+            Ri = g.rf[i];
+            rhoi = g.hill ? star_dist_f(si, p0) : 0.0f;
+            mi = si.zm.z;
         }
     }
-    const float inv3M = (SCREEN && g.hill) ? (float)(1.0 / (3.0 * g.mass[tile.base])) : 0.0f;
     DF ax{0.0f, 0.0f}, ay{0.0f, 0.0f}, az{0.0f, 0.0f};
     for (int j0 = tile.src_begin; j0 < tile.src_end; j0 += DF_ROW_NT) {
         const int nj = min(DF_ROW_NT, tile.src_end - j0);
@@ -666,8 +729,8 @@ __global__ void __launch_bounds__(DF_ROW_NT) grav_df_rowseq(GravArgs g, const Sp
             s_p[t] = sp[j];
             s_id[t] = g.id[j];
             if (SCREEN) {
-                s_R[t] = (float)g.radius[j];
-                s_rho[t] = g.hill ? (float)g.rho[j] : 0.0f;
+                s_R[t] = g.rf[j];
+                s_rho[t] = g.hill ? star_dist_f(s_p[t], p0) : 0.0f;
             }
         }
         __syncthreads();
@@ -708,7 +771,7 @@ struct DfFewArgs {
     long long pitch;  // >= chunks of the longest row
 };
 
-template <bool SCREEN>
+template <bool SCREEN, int SMAX>
 __global__ void __launch_bounds__(256) grav_df_few(DfFewArgs a)
 {
     const GravArgs& g = a.g;
@@ -717,24 +780,30 @@ __global__ void __launch_bounds__(256) grav_df_few(DfFewArgs a)
     const int nsrc = tile.src_end - tile.src_begin;
     const int c0 = blockIdx.x * DF_FEW_CHUNK;
     if (c0 >= nsrc) return;
-    const int ns = tile.sink_end - tile.sink_begin;
-    __shared__ SplitPos s_sink[FEW_SINKS_MAX];
-    __shared__ float s_R[FEW_SINKS_MAX], s_rho[FEW_SINKS_MAX], s_m[FEW_SINKS_MAX];
-    __shared__ int s_act[FEW_SINKS_MAX];
-    __shared__ DF s_red[8][3 * FEW_SINKS_MAX];
+    const int ns = tile.sink_end - tile.sink_begin;  // <= SMAX
+    __shared__ SplitPos s_sink[SMAX];
+    __shared__ float s_R[SMAX], s_rho[SMAX], s_m[SMAX];
+    __shared__ int s_act[SMAX];
+    __shared__ DF s_red[8][3 * SMAX];
+    SplitPos p0{};
+    float inv3M = 0.0f;
+    if (SCREEN && g.hill) {
+        p0 = a.sp[tile.base];
+        inv3M = 1.0f / (3.0f * p0.zm.z);
+    }
     if (threadIdx.x < ns) {
         const int i = tile.sink_begin + threadIdx.x;
-        s_sink[threadIdx.x] = a.sp[i];
+        const SplitPos pi = a.sp[i];
+        s_sink[threadIdx.x] = pi;
         s_act[threadIdx.x] = 0 < g.id[i];
-        s_R[threadIdx.x] = SCREEN ? (float)g.radius[i] : 0.0f;
-        s_rho[threadIdx.x] = (SCREEN && g.hill) ? (float)g.rho[i] : 0.0f;
-        s_m[threadIdx.x] = SCREEN ? (float)g.mass[i] : 0.0f;
+        s_R[threadIdx.x] = SCREEN ? g.rf[i] : 0.0f;
+        s_rho[threadIdx.x] = (SCREEN && g.hill) ? star_dist_f(pi, p0) : 0.0f;
+        s_m[threadIdx.x] = pi.zm.z;
     }
     __syncthreads();
-    const float inv3M = (SCREEN && g.hill) ? (float)(1.0 / (3.0 * g.mass[tile.base])) : 0.0f;
-    DF acc[FEW_SINKS_MAX][3];
+    DF acc[SMAX][3];
 #pragma unroll
-    for (int s = 0; s < FEW_SINKS_MAX; s++)
+    for (int s = 0; s < SMAX; s++)
 #pragma unroll
         for (int c = 0; c < 3; c++) acc[s][c] = DF{0.0f, 0.0f};
     const int c1 = min(nsrc, c0 + DF_FEW_CHUNK);
@@ -744,11 +813,11 @@ __global__ void __launch_bounds__(256) grav_df_few(DfFewArgs a)
         const SplitPos pj = a.sp[j];
         float Rj = 0.0f, rhoj = 0.0f;
         if (SCREEN) {
-            Rj = (float)g.radius[j];
-            rhoj = g.hill ? (float)g.rho[j] : 0.0f;
+            Rj = g.rf[j];
+            rhoj = g.hill ? star_dist_f(pj, p0) : 0.0f;
         }
 #pragma unroll
-        for (int s = 0; s < FEW_SINKS_MAX; s++) {
+        for (int s = 0; s < SMAX; s++) {
             if (s < ns) {
                 const int i = tile.sink_begin + s;
                 if (s_act[s] && j != i) {
@@ -765,7 +834,7 @@ __global__ void __launch_bounds__(256) grav_df_few(DfFewArgs a)
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-    for (int s = 0; s < FEW_SINKS_MAX; s++) {
+    for (int s = 0; s < SMAX; s++) {
         if (s < ns) {  // uniform over the CTA
 #pragma unroll
             for (int c = 0; c < 3; c++) {
@@ -826,19 +895,28 @@ int launch_grav_df_rowseq(const GravArgs& g, const void* split, cudaStream_t st)
     return 0;
 }
 
-int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row0, int max_src, double* partial,
-                       int rows, long long pitch, const int* row_sink, const int* row_nsrc, const int* row_sys,
-                       int group_row0, int group_rows, cudaStream_t st)
+int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row0, int max_src, int max_sinks,
+                       double* partial, int rows, long long pitch, const int* row_sink, const int* row_nsrc,
+                       const int* row_sys, int group_row0, int group_rows, cudaStream_t st)
 {
     if (g.n_tiles <= 0 || group_rows <= 0) return 0;
+    if (max_sinks > FEW_SINKS_MAX) return set_error(RG_ERR_STATE, "few-sink tile wider than FEW_SINKS_MAX");
     const int chunks = std::max(1, (max_src + DF_FEW_CHUNK - 1) / DF_FEW_CHUNK);
     if ((long long)chunks > pitch) return set_error(RG_ERR_STATE, "few-sink partial buffer too narrow");
     DfFewArgs a{g, (const SplitPos*)split, tile_row0, partial, rows, pitch};
     const dim3 grid(chunks, g.n_tiles);
-    if (g.record || g.hill)
-        grav_df_few<true><<<grid, 256, 0, st>>>(a);
-    else
-        grav_df_few<false><<<grid, 256, 0, st>>>(a);
+    const bool screen = g.record || g.hill;
+    if (max_sinks <= 4) {
+        if (screen)
+            grav_df_few<true, 4><<<grid, 256, 0, st>>>(a);
+        else
+            grav_df_few<false, 4><<<grid, 256, 0, st>>>(a);
+    } else {
+        if (screen)
+            grav_df_few<true, FEW_SINKS_MAX><<<grid, 256, 0, st>>>(a);
+        else
+            grav_df_few<false, FEW_SINKS_MAX><<<grid, 256, 0, st>>>(a);
+    }
     RG_CUDA_CHECK(cudaGetLastError());
     DfFinalArgs f{partial, rows, group_row0, group_rows, pitch, row_sink, row_nsrc, row_sys, g.sys_active,
                   g.ax, g.ay, g.az};
@@ -847,11 +925,11 @@ int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row
     return 0;
 }
 
-int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id, int n,
-                           SplitPos* out, cudaStream_t st)
+int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id,
+                           const double* radius, int n, SplitPos* out, float* rf, cudaStream_t st)
 {
     if (n <= 0) return 0;
-    split_positions_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, m, id, n, out);
+    split_positions_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, m, id, radius, n, out, rf);
     RG_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

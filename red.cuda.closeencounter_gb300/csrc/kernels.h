@@ -72,11 +72,12 @@ int launch_grav_fp64_few(const GravArgs& g, const int* tile_row0, int max_src, d
                          long long pitch, const int* dev_row_sink, const int* dev_row_nsrc, const int* dev_row_sys,
                          int group_row0, int group_rows, bool serial, cudaStream_t st);
 // mixed precision (gravity_mixed.cu): positions split into FP32 (hi, lo) once per evaluation
+struct SplitPos;
 constexpr int MIXED_SINKS_PER_TILE = 128;
 constexpr int MIXED_SOURCE_TILE = 256;  // source-chunk lengths are multiples of this
 constexpr size_t SPLIT_POS_BYTES = 32;  // per body
-int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id, int n,
-                           struct SplitPos* out, cudaStream_t st);
+int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id,
+                           const double* radius, int n, SplitPos* out, float* rf, cudaStream_t st);
 int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* heavy_end, float near_ratio,
                             int n_chunks, int chunk, double* partial, int n_part, unsigned int* err,
                             cudaStream_t st);
@@ -84,9 +85,9 @@ int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* hea
 // the row kernel for blocks with a few massive sources, the few-sink kernel for the
 // star's and giants' own rows (partial: 3 x rows x pitch doubles, pitch >= source chunks)
 int launch_grav_df_rowseq(const GravArgs& g, const void* split, cudaStream_t st);
-int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row0, int max_src, double* partial,
-                       int rows, long long pitch, const int* row_sink, const int* row_nsrc, const int* row_sys,
-                       int group_row0, int group_rows, cudaStream_t st);
+int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row0, int max_src, int max_sinks,
+                       double* partial, int rows, long long pitch, const int* row_sink, const int* row_nsrc,
+                       const int* row_sys, int group_row0, int group_rows, cudaStream_t st);
 int launch_star_distance(const double* x, const double* y, const double* z, const int* base_of, int n, double* rho,
                          cudaStream_t st);
 
