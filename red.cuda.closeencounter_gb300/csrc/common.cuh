@@ -61,6 +61,8 @@ struct GravArgs {
     int n_tiles;
     double f_rad;      // THRESHOLD_RADII_ENHANCE_FACTOR
     double hill_f3;    // hill_factor^3
+    float f_rad_f;     // the same in FP32 (the mixed kernels' event screens)
+    float hill_f3_f;
     int record;        // record radius-criterion candidates
     int hill;          // record Hill candidates
     uint32_t seq;

@@ -458,6 +458,8 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
     g.az = acc + 2 * cap;
     g.f_rad = c->thr[RG_THRESHOLD_RADII_ENHANCE_FACTOR];
     g.hill_f3 = c->hill_factor * c->hill_factor * c->hill_factor;
+    g.f_rad_f = (float)g.f_rad;
+    g.hill_f3_f = (float)g.hill_f3;
     g.record = (record && c->inner_steps && g.f_rad > 0.0) ? 1 : 0;
     g.hill = hill ? 1 : 0;
     g.seq = ((uint32_t)attempt << 8) | (uint32_t)stage;

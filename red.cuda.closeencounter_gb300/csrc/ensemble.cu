@@ -816,6 +816,8 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
     // one collision factor for the ensemble (the first disk's): the kernels take a scalar
     g.f_rad = e->thr[RG_THRESHOLD_RADII_ENHANCE_FACTOR];
     g.hill_f3 = e->hill_factor * e->hill_factor * e->hill_factor;
+    g.f_rad_f = (float)g.f_rad;
+    g.hill_f3_f = (float)g.hill_f3;
     g.record = (stage > 0 && g.f_rad > 0.0) ? 1 : 0;
     g.hill = hill ? 1 : 0;
     g.seq = (uint32_t)stage;

@@ -322,13 +322,13 @@ __device__ __forceinline__ void df_screen(const GravArgs& g, const Tile& tile, i
     const float margin = 1.001f;
     bool cand = false;
     if (g.record) {
-        const float lim = (float)g.f_rad * (Ri + Rj) * margin;
+        const float lim = g.f_rad_f * (Ri + Rj) * margin;
         cand = r2f < lim * lim;
     }
     if (g.hill && tile.block != 2 && lj > 0) {
         const float h = 0.5f * (rhoi + rhoj);
         const float d3 = r2f * sqrtf(r2f);
-        cand = cand || d3 < (float)g.hill_f3 * (mi + mj) * inv3M * (h * h * h) * (margin * margin * margin);
+        cand = cand || d3 < g.hill_f3_f * (mi + mj) * inv3M * (h * h * h) * (margin * margin * margin);
     }
     if (cand)
         exact_event_tests(g, tile, i, j, g.px[i], g.py[i], g.pz[i], g.radius[i], g.mass[i], g.hill ? g.rho[i] : 0.0);
@@ -344,7 +344,7 @@ constexpr int MX_GROUP = 16;  // sources summed in plain FP32 before each two-su
 // sinks themselves (self pairs are skipped); SCREEN: event screens are on.
 template <bool DIAG, bool SCREEN>
 __device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile, int j0, int q_begin, int q_end,
-                                            const SplitPos* s_sp, const float* s_R,
+                                            const SplitPos* s_sp, const float4* s_sinkf, float inv3M, const float* s_R,
                                             const float* s_rho, const SinkD* s_sink, const int* si,
                                             const float* xh, const float* xl, const float* yh, const float* yl,
                                             const float* zh, const float* zl, const float* near_lim, Acc2* ax,
@@ -384,22 +384,23 @@ __device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile
             if (SCREEN) {
                 const int li = si[r] - tile.base, lj = j - tile.base;
                 if (li > 0 && li > lj && (!DIAG || j != si[r]) && mj >= 0.0f) {
-                    const SinkD& sd = s_sink[lane + 32 * r];
+                    const float4 sf = s_sinkf[lane + 32 * r];  // R, m, rho of the sink in FP32
                     const float margin = 1.001f;
                     bool cand = false;
                     if (g.record) {
-                        const float lim = (float)g.f_rad * ((float)sd.R + s_R[q]) * margin;
+                        const float lim = g.f_rad_f * (sf.x + s_R[q]) * margin;
                         cand = r2 < lim * lim;
                     }
                     if (g.hill && tile.block != 2 && lj > 0) {
-                        const float h = 0.5f * ((float)sd.rho + s_rho[q]);
+                        const float h = 0.5f * (sf.z + s_rho[q]);
                         const float d3 = r2 * sqrtf(r2);
-                        const float inv3M = (float)(1.0 / (3.0 * g.mass[tile.base]));
-                        cand = cand || (d3 < (float)g.hill_f3 * ((float)sd.m + mj) * inv3M * (h * h * h) *
+                        cand = cand || (d3 < g.hill_f3_f * (sf.y + mj) * inv3M * (h * h * h) *
                                                  (margin * margin * margin));
                     }
-                    if (cand && 0 <= g.id[j])
+                    if (cand && 0 <= g.id[j]) {
+                        const SinkD& sd = s_sink[lane + 32 * r];
                         exact_event_tests(g, tile, si[r], j, sd.x, sd.y, sd.z, sd.R, sd.m, sd.rho);
+                    }
                 }
             }
         }
@@ -473,6 +474,7 @@ __device__ __forceinline__ void tma_tile(void* dst, const void* src, unsigned by
 struct MixedSmem {
     SplitPos sp[2][MX_T];              // double-buffered source tiles (TMA destination)
     SinkD sink[MX_S];
+    float4 sinkf[MX_S];                // R, m, rho of the sinks in FP32 (event screens)
     Acc2 part[MX_WARPS][3][MX_S];      // per-warp compensated partial sums
     float R[2][MX_T], rho[2][MX_T];    // screening data of the tiles (SCREEN only)
     unsigned long long bar[2];
@@ -524,7 +526,9 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
             sd.rho = g.hill ? g.rho[i] : 0.0;
         }
         S.sink[s] = sd;
+        S.sinkf[s] = make_float4((float)sd.R, (float)sd.m, (float)sd.rho, 0.0f);
     }
+    const float inv3M = (SCREEN && g.hill) ? (float)(1.0 / (3.0 * g.mass[tile.base])) : 0.0f;
     __syncthreads();
     // the first two tiles travel while the heavy sources are summed
     if (threadIdx.x == 0) {
@@ -586,9 +590,8 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
                 acc_df(ay[r], ty);
                 acc_df(az[r], tz);
                 if (SCREEN) {
-                    const SinkD& sd = S.sink[s];
-                    df_screen(g, tile, si[r], j, r2f, (float)sd.R, Rj, (float)sd.rho, rhoj, (float)sd.m, pj.zm.z,
-                              (float)(1.0 / (3.0 * g.mass[tile.base])));
+                    const float4 sf = S.sinkf[s];
+                    df_screen(g, tile, si[r], j, r2f, sf.x, Rj, sf.z, rhoj, sf.y, pj.zm.z, inv3M);
                 }
             }
         }
@@ -610,10 +613,10 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
             // does this slice hold any of the CTA's sinks?
             const bool diag = (j0 + q_begin < tile.sink_begin + MX_S) && (j0 + q_end > tile.sink_begin);
             if (diag)
-                mixed_slice<true, SCREEN>(a, tile, j0, q_begin, q_end, S.sp[b], S.R[b], S.rho[b], S.sink, si, xh, xl,
+                mixed_slice<true, SCREEN>(a, tile, j0, q_begin, q_end, S.sp[b], S.sinkf, inv3M, S.R[b], S.rho[b], S.sink, si, xh, xl,
                                           yh, yl, zh, zl, near_lim, ax, ay, az, near_mask, lane);
             else
-                mixed_slice<false, SCREEN>(a, tile, j0, q_begin, q_end, S.sp[b], S.R[b], S.rho[b], S.sink, si, xh,
+                mixed_slice<false, SCREEN>(a, tile, j0, q_begin, q_end, S.sp[b], S.sinkf, inv3M, S.R[b], S.rho[b], S.sink, si, xh,
                                            xl, yh, yl, zh, zl, near_lim, ax, ay, az, near_mask, lane);
             // near pairs of this slice: the double-float term (FP64-class accuracy on the FP32 pipes)
 #pragma unroll
@@ -695,7 +698,7 @@ __global__ void mixed_reduce_kernel(const double* __restrict__ partial, int n_ch
 constexpr int DF_ROW_NT = 128;
 
 template <bool SCREEN>
-__global__ void __launch_bounds__(DF_ROW_NT) grav_df_rowseq(GravArgs g, const SplitPos* __restrict__ sp)
+__global__ void __launch_bounds__(DF_ROW_NT, 8) grav_df_rowseq(GravArgs g, const SplitPos* __restrict__ sp)
 {
     __shared__ SplitPos s_p[DF_ROW_NT];
     __shared__ float s_R[DF_ROW_NT], s_rho[DF_ROW_NT];
@@ -772,7 +775,7 @@ struct DfFewArgs {
 };
 
 template <bool SCREEN, int SMAX>
-__global__ void __launch_bounds__(256) grav_df_few(DfFewArgs a)
+__global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs a)
 {
     const GravArgs& g = a.g;
     const Tile tile = g.tiles[blockIdx.y];
