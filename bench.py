@@ -35,6 +35,7 @@ sys.path.insert(0, os.path.join(ROOT, "red.cuda.closeencounter_gb300"))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 from redgb import bodies, types as T  # noqa: E402
+from redgb.replicas import max_over_ranks  # noqa: E402
 
 WORKLOADS = {
     # name: (config, n, integrator, dt_day, adaptive)
@@ -175,10 +176,8 @@ def run_ours(args, rank, ws, dist):
     torch.cuda.synchronize()
     clk = clocks.stop()
     if dist:
-        t = torch.tensor([secs], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        secs = max_over_ranks(secs, dist, device="cuda")
         dist.barrier()
-        secs = float(t.item())
     launches = sysm.counters()["n_kernels"] - k0
     E1, _ = sysm.energy()
     years = days / T.YEAR
@@ -199,9 +198,7 @@ def run_ours(args, rank, ws, dist):
         r_h, v_h = sysm.state()[:2]
         t_e2e += time.perf_counter() - t0
     if dist:
-        t = torch.tensor([t_e2e], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+        t_e2e = max_over_ranks(t_e2e, dist, device="cuda")
     e2e = {"value": ws * (e2e_days / T.YEAR) / t_e2e, "unit": "sim-years/s", "h2d_bytes_per_step": nbytes,
            "d2h_bytes_per_step": nbytes}
 
@@ -297,6 +294,32 @@ def run_reference(args, rank, ws):
                              "sample": f"{args.steps} full integrator steps, single thread (the reference's "
                                        "CPU path is serial)"},
             "e2e": {"value": value, "unit": "sim-years/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def _oracle_disk(task):
+    """One disk through the oracle on one host core (a spawned worker: no CUDA)."""
+    import pyoracle
+    seed, years, hill = task
+    disk = bodies.config_disk("ensemble_member", seed=seed)
+    o = pyoracle.OracleSystem(disk, bodies.thresholds(ejection=100.0, hit_centrum=0.05, collision_factor=1.0))
+    o.set_integrator(T.INT_RKF78, 0.001, True, 1e-10)
+    o.set_event_options(close_encounter=False, hill_factor=hill)
+    t0 = time.perf_counter()
+    o.advance(years * T.YEAR)
+    return years, time.perf_counter() - t0
+
+
+def cpu_ensemble(seeds, years, hill, processes):
+    """The reference's CPU path (oracle) on `processes` host cores, one disk per process,
+    all running at once: aggregate simulated years over the slowest process's time."""
+    import multiprocessing as mp
+    with mp.get_context("spawn").Pool(processes) as pool:
+        res = pool.map(_oracle_disk, [(s, years, hill) for s in seeds], chunksize=1)
+    yrs = sum(r[0] for r in res)
+    slowest = max(r[1] for r in res)
+    return {"value": yrs / slowest, "unit": "sim-years/s", "cores": processes, "kind": "port",
+            "sample": f"{len(seeds)} disks of the same ensemble (seeds {seeds[0]}-{seeds[-1]}), {years} yr each, "
+                      f"one process per core, all at once; slowest process {slowest:.2f} s"}
 
 
 def _compare_events(a, b):
@@ -408,7 +431,11 @@ def ensemble_section(args):
     sequential = {"sim_years_per_s": seq_years / seq_s, "seconds": seq_s, "sim_years": seq_years,
                   "max_dE_over_E": seq_dE, "sample": f"{len(sample)} of {len(disks)} disks (every "
                   f"{max(1, len(disks) // args.sequential_sample)}th), the rate applies to all of them"}
+    procs = max(1, min(os.cpu_count() or 1, 32))
+    cpu = cpu_ensemble([65 + k for k in range(procs)], args.cpu_ensemble_years, hill, procs)
     return {
+        "cpu_baseline": cpu,
+        "speedup_vs_cpu_cores": learned["sim_years_per_s"] / cpu["value"],
         "workload": f"{len(disks)} disks, {n_bodies} bodies (N ~ U[512, 8192]), RKF7(8) tol 1e-10, "
                     f"{args.ensemble_years} yr per disk after a {warm_day:g}-day warm-up; CE at {hill:g} mutual "
                     "Hill radii, collisions at R1+R2, ejection 100 AU, hit-star 0.05 AU",
@@ -443,6 +470,7 @@ def main():
     ap.add_argument("--ensemble-years", type=float, default=10.0)
     ap.add_argument("--train-years", type=float, default=10.0)
     ap.add_argument("--sequential-sample", type=int, default=8)
+    ap.add_argument("--cpu-ensemble-years", type=float, default=1.0)
     args = ap.parse_args()
     if args.only_ensemble:
         print(json.dumps({"ensemble": ensemble_section(args)}))
