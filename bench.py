@@ -163,6 +163,7 @@ def run_ours(args, rank, ws, dist):
         return tot / 1e3, days, p
 
     sysm = make(mode)
+    tune = sysm.autotune(3) if not args.no_autotune else None
     for _ in range(args.warmup):
         sysm.step()
     E0, _ = sysm.energy()
@@ -211,6 +212,7 @@ def run_ours(args, rank, ws, dist):
         achieved = pairs * FLOP_PER_PAIR / (avg_ms * 1e-3) / 1e12
         # the FP64 form of the same step, for the mixed/FP64 comparison
         fp = make(T.GRAVITY_FP64)
+        tune_fp = fp.autotune(1) if not args.no_autotune else None
         for _ in range(min(args.warmup, 3)):
             fp.step()
         k_fp = max(2, min(args.steps, 5))
@@ -245,6 +247,7 @@ def run_ours(args, rank, ws, dist):
                           "fp64_peak_tflops": L.measure_pipe_peak(1),
                           "achieved_tflops": k_fp * evals_per_step * pairs * FLOP_PER_PAIR / s_fp / 1e12},
             "mixed_force_error": {"max_rel": float(rel.max()), "rms_rel": float(np.sqrt(np.mean(rel ** 2)))},
+            "autotune": {"timed_form": tune, "fp64_form": tune_fp},
             "clocks": clk,
         }
         if ws == 1 and not args.no_cpu_baseline:
@@ -465,6 +468,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--only-ensemble", action="store_true", help="the ensemble section alone (profiling)")
     ap.add_argument("--ensemble-disks", type=int, default=256)
     ap.add_argument("--ensemble-years", type=float, default=10.0)

@@ -191,6 +191,16 @@ RG_API int rg_set_state(rg_ctx* ctx, const rg_vec_t* r, const rg_vec_t* v);
  * pp_disk.cu:998-1041) in internal units; events it finds are discarded. */
 RG_API int rg_calc_accel(rg_ctx* ctx, rg_vec_t* a);
 
+/*
+ * Autotuner (not in the reference): times every candidate launch shape of the force
+ * evaluation in the current gravity mode on the current state (`reps` evaluations each,
+ * CUDA events on the context's stream) and keeps the fastest.  FP64 mode: sinks per
+ * pair-parallel CTA x the row-kernel source limit -- every candidate sums in the same
+ * order, so results stay bit-exact; mixed mode: source chunks x the row-kernel limit.
+ * Counters are left as they were.  `out` (may be NULL) receives the choice.
+ */
+RG_API int rg_autotune(rg_ctx* ctx, int reps, rg_tune_t* out);
+
 /* Integrator and event counters (integrator.cu:258-278, pp_disk.h:129-133). */
 RG_API int rg_get_counters(rg_ctx* ctx, rg_counters_t* c);
 

@@ -72,6 +72,16 @@ typedef struct rg_profile {
     double  stage_ms;
 } rg_profile_t;
 
+/* launch shape of a context's force evaluation (rg_autotune) */
+typedef struct rg_tune {
+    int32_t pairpar_sinks;   /* FP64 mode: sinks per pair-parallel CTA (8, 16 or 32)             */
+    int32_t rowseq_max_src;  /* blocks with at most this many sources use the row kernel         */
+    int32_t mixed_chunks;    /* mixed mode: source chunks over grid.y (0: chosen from the SM count) */
+    int32_t candidates;      /* configurations timed                                             */
+    double  ms_per_eval;     /* the chosen configuration: CUDA-event time of one evaluation       */
+    double  ms_before;       /* the configuration in place before tuning                         */
+} rg_tune_t;
+
 /* per-system statistics of an ensemble (rg_ens_get_stats) */
 typedef struct rg_ens_stats {
     double  t_day;          /* simulation clock of the system            */

@@ -90,6 +90,7 @@ struct rg_ctx {
     int gravity_mode = RG_GRAVITY_FP64;
     int pairpar_S = 16;
     int rowseq_max_src = 64;
+    int mixed_chunks = 0;  // source chunks of the mixed kernel (0: from the SM count)
     float near_ratio = 1.0e-5f;
     // integrator
     int has_int = 0, int_type = 0, adaptive = 0, ectp = 0, r_max = 0, order = 0;
@@ -523,7 +524,9 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
             if (!rc) {
                 // split the sources over grid.y so that about 4 CTAs per SM are in flight
                 const int src = c->tiles[gr.off].src_end - c->tiles[gr.off].src_begin;
-                int chunks = std::max(1, std::min((4 * c->n_sm + gr.n - 1) / gr.n, src / (4 * MIXED_SOURCE_TILE)));
+                int chunks = c->mixed_chunks > 0
+                                 ? std::min(c->mixed_chunks, std::max(1, src / MIXED_SOURCE_TILE))
+                                 : std::max(1, std::min((4 * c->n_sm + gr.n - 1) / gr.n, src / (4 * MIXED_SOURCE_TILE)));
                 const int chunk = ((src + chunks - 1) / chunks + MIXED_SOURCE_TILE - 1) / MIXED_SOURCE_TILE *
                                   MIXED_SOURCE_TILE;
                 chunks = (src + chunk - 1) / chunk;
@@ -1574,6 +1577,87 @@ int rg_set_state(rg_ctx* c, const rg_vec_t* r, const rg_vec_t* v)
     RG_GUARD(upload_state(c, h));
 }
 
+// CUDA-event time of one force evaluation (stage-0 form, no event recording) over `reps`
+static int time_evaluations(rg_ctx* c, int reps, double* ms)
+{
+    const size_t cap = (size_t)c->cap;
+    int rc = gravity(c, c->d_y, c->d_y + 3 * cap, c->d_P, 0, 0, false, false);  // warm-up (plan upload)
+    if (rc) return rc;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    RG_CUDA_CHECK(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return set_error(RG_ERR_CUDA, "cudaEventCreate");
+    }
+    cudaEventRecord(e0, c->st);
+    for (int k = 0; k < reps && !rc; k++) rc = gravity(c, c->d_y, c->d_y + 3 * cap, c->d_P, 0, 0, false, false);
+    cudaEventRecord(e1, c->st);
+    cudaError_t err = cudaEventSynchronize(e1);
+    float t = 0.0f;
+    if (!rc && err == cudaSuccess) err = cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (err != cudaSuccess) return cuda_fail(err, "autotune timing", __FILE__, __LINE__);
+    *ms = (double)t / reps;
+    return RG_OK;
+}
+
+static int autotune_impl(rg_ctx* c, int reps, rg_tune_t* out)
+{
+    struct Shape {
+        int S, rowseq, chunks;
+    };
+    std::vector<Shape> cand;
+    const int rows[3] = {32, 64, 128};
+    if (c->gravity_mode == RG_GRAVITY_MIXED) {
+        const int ch[5] = {0, 1, 2, 4, 8};
+        for (int r : rows)
+            for (int k : ch) cand.push_back({c->pairpar_S, r, k});
+    } else {
+        const int ss[3] = {8, 16, 32};
+        for (int r : rows)
+            for (int S : ss) cand.push_back({S, r, c->mixed_chunks});
+    }
+    // tuning evaluations leave the counters as they were
+    const int64_t evals = c->n_gravity_evals, pairs = c->n_pairs, kernels = c->n_kernels;
+    const Shape before{c->pairpar_S, c->rowseq_max_src, c->mixed_chunks};
+    double ms_before = 0.0, best_ms = 0.0;
+    int rc = time_evaluations(c, reps, &ms_before);
+    Shape best = before;
+    best_ms = ms_before;
+    for (const Shape& sh : cand) {
+        if (rc) break;
+        c->pairpar_S = sh.S;
+        c->rowseq_max_src = sh.rowseq;
+        c->mixed_chunks = sh.chunks;
+        build_tiles(c);
+        double ms = 0.0;
+        rc = time_evaluations(c, reps, &ms);
+        if (!rc && ms < best_ms) {
+            best_ms = ms;
+            best = sh;
+        }
+    }
+    c->pairpar_S = best.S;
+    c->rowseq_max_src = best.rowseq;
+    c->mixed_chunks = best.chunks;
+    build_tiles(c);
+    c->n_gravity_evals = evals;
+    c->n_pairs = pairs;
+    c->n_kernels = kernels;
+    if (rc) return rc;
+    if (out) {
+        out->pairpar_sinks = best.S;
+        out->rowseq_max_src = best.rowseq;
+        out->mixed_chunks = best.chunks;
+        out->candidates = (int32_t)cand.size();
+        out->ms_per_eval = best_ms;
+        out->ms_before = ms_before;
+    }
+    return RG_OK;
+}
+
 static int calc_accel_impl(rg_ctx* c, rg_vec_t* a)
 {
     const size_t cap = (size_t)c->cap;
@@ -1596,6 +1680,12 @@ int rg_calc_accel(rg_ctx* c, rg_vec_t* a)
 {
     if (!c || !a) return set_error(RG_ERR_ARG, "bad argument");
     RG_GUARD(calc_accel_impl(c, a));
+}
+
+int rg_autotune(rg_ctx* c, int reps, rg_tune_t* out)
+{
+    if (!c || reps <= 0) return set_error(RG_ERR_ARG, "bad argument");
+    RG_GUARD(autotune_impl(c, reps, out));
 }
 
 int rg_get_counters(rg_ctx* c, rg_counters_t* o)

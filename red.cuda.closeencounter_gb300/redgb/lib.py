@@ -35,6 +35,7 @@ def load(auto_build=True):
     L.rg_set_profiling.argtypes = [vp, ci]
     L.rg_get_profile.argtypes = [vp, ctypes.POINTER(T.Profile)]
     L.rg_measure_pipe_peak.argtypes = [ci, ctypes.POINTER(ctypes.c_double)]
+    L.rg_autotune.argtypes = [vp, ci, ctypes.POINTER(T.Tune)]
     _lib = L
     return L
 
@@ -67,6 +68,13 @@ class System(api.System):
         prof = T.Profile()
         self._call("get_profile", self.handle, ctypes.byref(prof))
         return {f: getattr(prof, f) for f, _ in prof._fields_}
+
+    def autotune(self, reps=3):
+        """Time the candidate launch shapes of the current gravity mode and keep the fastest
+        (rg_autotune); returns the choice."""
+        t = T.Tune()
+        self._call("autotune", self.handle, int(reps), ctypes.byref(t))
+        return {f: getattr(t, f) for f, _ in t._fields_}
 
 
 def measure_pipe_peak(kind):

@@ -96,6 +96,13 @@ class Profile(ctypes.Structure):
                 ("stage_launches", ctypes.c_int64), ("stage_ms", ctypes.c_double)]
 
 
+class Tune(ctypes.Structure):
+    """rg_tune_t: the launch shape rg_autotune chose."""
+    _fields_ = [("pairpar_sinks", ctypes.c_int32), ("rowseq_max_src", ctypes.c_int32),
+                ("mixed_chunks", ctypes.c_int32), ("candidates", ctypes.c_int32),
+                ("ms_per_eval", ctypes.c_double), ("ms_before", ctypes.c_double)]
+
+
 STEP_REC = np.dtype([("sys", "<i4"), ("accepted", "<i4"), ("proposed", "<i4"), ("step", "<i4"), ("dt", "<f8"),
                      ("err", "<f8"), ("feat", "<f4", 8)], align=True)
 assert STEP_REC.itemsize == 64
