@@ -254,6 +254,8 @@ def run_ours(args, rank, ws, dist):
             out["cpu_baseline"] = cpu_baseline(args, disk, int_type, dt_day, adaptive, samples=args.cpu_steps)
         if not args.no_ensemble:
             out["ensemble"] = ensemble_section(args)
+        if not args.no_dense_ring:
+            out["dense_ring"] = dense_ring_section(args)
     return out
 
 
@@ -323,6 +325,67 @@ def cpu_ensemble(seeds, years, hill, processes):
     return {"value": yrs / slowest, "unit": "sim-years/s", "cores": processes, "kind": "port",
             "sample": f"{len(seeds)} disks of the same ensemble (seeds {seeds[0]}-{seeds[-1]}), {years} yr each, "
                       f"one process per core, all at once; slowest process {slowest:.2f} s"}
+
+
+def dense_ring_section(args):
+    """BASELINE config 4: 131 072 self-gravitating bodies in a narrow ring (a in [0.9, 1.1]
+    AU, e, i ~ R(0.002)) around a 1 Msun star plus a 3e-6 Msun embryo at 1 AU, masses
+    log-uniform in [1e-11, 1e-9] Msun; RKF5 adaptive at tolerance 1e-9, collisions at R1 + R2,
+    close encounters at 3 mutual Hill radii.  A bounded sample of the 10-year run: mixed
+    precision over `--dense-ring-steps` steps, and the first `--dense-ring-fp64-steps` steps
+    in both precisions from the same state, whose event lists (type, pair, step) must agree."""
+    import torch
+
+    from redgb import lib
+
+    disk = bodies.config_disk("dense_ring")
+    thr = bodies.thresholds(ejection=100.0, hit_centrum=0.05, collision_factor=1.0)
+
+    def make(mode):
+        s = lib.System(disk, thr)
+        s.set_integrator(T.INT_RK5, 0.001, True, 1e-9)
+        s.set_event_options(close_encounter=False, hill_factor=3.0)
+        s.set_gravity_mode(mode)
+        return s
+
+    def run(s, steps):
+        events = []
+        E0 = s.energy()[0]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        days = 0.0
+        for k in range(steps):  # the main loop's order (main.cu:201-251)
+            s.check_for_ejection_hit_centrum()
+            days += s.step()
+            for name in ("check_for_collision", "check_for_close_encounter"):
+                getattr(s, name)()
+            for e in s.events():
+                events.append((k, int(e["event_name"]), int(e["id1"]), int(e["id2"])))
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        return days, secs, events, abs((s.energy()[0] - E0) / E0)
+
+    mixed = make(T.GRAVITY_MIXED)
+    tune = mixed.autotune(1)
+    days, secs, ev_m, dE = run(mixed, args.dense_ring_steps)
+    evals = 6 * args.dense_ring_steps
+    pairs = disk.pairs_per_eval()
+    cmp_m = make(T.GRAVITY_MIXED)
+    _, _, ev_a, _ = run(cmp_m, args.dense_ring_fp64_steps)
+    fp = make(T.GRAVITY_FP64)
+    d_fp, s_fp, ev_f, dE_fp = run(fp, args.dense_ring_fp64_steps)
+    return {
+        "workload": f"dense ring, {disk.n_total} bodies, RKF5 tol 1e-9, {args.dense_ring_steps} steps "
+                    "(a sample of the 10-year run)",
+        "mixed": {"sim_years_per_s": (days / T.YEAR) / secs, "steps": args.dense_ring_steps,
+                  "ms_per_step": 1e3 * secs / args.dense_ring_steps, "simulated_days": days,
+                  "pairs_per_s_lower_bound": evals * pairs / secs, "events": len(ev_m), "dE_over_E": dE,
+                  "autotune": tune},
+        "fp64": {"sim_years_per_s": (d_fp / T.YEAR) / s_fp, "steps": args.dense_ring_fp64_steps,
+                 "ms_per_step": 1e3 * s_fp / args.dense_ring_fp64_steps, "dE_over_E": dE_fp},
+        "event_list_vs_fp64": {"steps": args.dense_ring_fp64_steps, "identical": ev_a == ev_f,
+                               "n_mixed": len(ev_a), "n_fp64": len(ev_f)},
+    }
 
 
 def _compare_events(a, b):
@@ -475,6 +538,9 @@ def main():
     ap.add_argument("--train-years", type=float, default=10.0)
     ap.add_argument("--sequential-sample", type=int, default=8)
     ap.add_argument("--cpu-ensemble-years", type=float, default=1.0)
+    ap.add_argument("--no-dense-ring", action="store_true")
+    ap.add_argument("--dense-ring-steps", type=int, default=20)
+    ap.add_argument("--dense-ring-fp64-steps", type=int, default=2)
     args = ap.parse_args()
     if args.only_ensemble:
         print(json.dumps({"ensemble": ensemble_section(args)}))
