@@ -116,7 +116,7 @@ def read_body_file(path) -> Disk:
 
 def write_parameter_file(path, *, integrator="rkf8", tolerance=None, length_yr=1.0, output_interval_yr=None,
                          ejection=None, hit_centrum=None, collision_factor=None, error_check_for_tp=False,
-                         close_encounter=False, name="synthetic"):
+                         close_encounter=False, name="synthetic", output_type=None):
     """key = value parameter file read by parameter::parse (parameter.cpp:55-285)."""
     lines = [f"name = {name}", "description = seeded synthetic disk", "frame_center = bary",
              f"integrator = {integrator}"]
@@ -133,6 +133,8 @@ def write_parameter_file(path, *, integrator="rkf8", tolerance=None, length_yr=1
         lines.append(f"hit_centrum = {hit_centrum!r}")
     if collision_factor is not None:
         lines.append(f"collision_factor = {collision_factor!r}")
+    if output_type is not None:  # "text" or "binary" (parameter.cpp:242-256)
+        lines.append(f"output_type = {output_type}")
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")
 

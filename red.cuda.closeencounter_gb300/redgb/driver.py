@@ -12,8 +12,10 @@ from . import types as T
 
 
 def run_main_loop(system, stop_day, output_interval_day, *, radii_enhance_factor, close_encounter=False,
-                  inner_steps=True, start_day=0.0, max_steps=0):
-    """Returns (snapshots, events, n_steps); a snapshot is (t_day, r, v, p, md) in file units."""
+                  inner_steps=True, start_day=0.0, max_steps=0, keep_inactive=False):
+    """Returns (snapshots, events, n_steps); a snapshot is (t_day, r, v, p, md) in file units,
+    the active records only, or the whole storage (inactive records until the next
+    compaction included, storage order) with keep_inactive."""
     snaps = []
     events = []
     stop = stop_day * T.GAUSS
@@ -22,6 +24,9 @@ def run_main_loop(system, stop_day, output_interval_day, *, radii_enhance_factor
 
     def snap():
         r, v, p, md, t = system.state()
+        if keep_inactive:
+            snaps.append((t, r.copy(), v.copy(), p.copy(), md.copy()))
+            return
         active = (md["id"] > 0) & (md["body_type"] < T.BODY_PADDINGPARTICLE)
         snaps.append((t, r[active].copy(), v[active].copy(), p[active].copy(), md[active].copy()))
 

@@ -83,6 +83,30 @@ def run_case(name, disk, params, workdir, timeout=600):
     return result, events
 
 
+def save_text(name, disk, params, workdir, events_only=False):
+    """The reference's own output files of one case, kept verbatim (gzip) to pin the
+    writers of redgb.io byte for byte: text result, binary result, event lines."""
+    import gzip
+    for out_type in (("text",) if events_only else ("text", "binary")):
+        d = os.path.join(workdir, name + "_" + out_type)
+        os.makedirs(d, exist_ok=True)
+        bodies.write_body_file(os.path.join(d, "bodies.txt"), disk)
+        bodies.write_parameter_file(os.path.join(d, "parameters.txt"), output_type=out_type, **params)
+        subprocess.run([RED, "-cpu", "-ef", "-iDir", d, "-p", "parameters.txt", "-ic", "bodies.txt"], cwd=d,
+                       check=True, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, timeout=600)
+        prefix = os.path.join(d, "R_cpu_ns_" + ("as" if params.get("tolerance") is not None else "fs") + "_")
+        short = {"e": "E", "rk4": "RK4", "rkf8": "RKF8"}[params["integrator"]]
+        files = [("_event.txt", "_event.txt")] if events_only else []
+        if not events_only:
+            files += [("_result.txt", "_result.txt")] if out_type == "text" else [("_result.bin", "_result.bin")]
+            if out_type == "text":
+                files.append(("_event.txt", "_event.txt"))
+        for src, dst in files:
+            with open(prefix + short + src, "rb") as fi, gzip.open(os.path.join(HERE, name + dst + ".gz"), "wb") as fo:
+                fo.write(fi.read())
+            print(f"{name}{dst}.gz")
+
+
 def save(name, disk, params, result, events):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), counts=np.array(disk.counts, np.int32), r=disk.r,
                         v=disk.v, p=disk.p, md=disk.md, epoch=disk.epoch, params=json.dumps(params),
@@ -148,6 +172,11 @@ def main():
                 continue
             result, events = run_case(name, disk, params, work)
             save(name, disk, params, result, events)
+            # verbatim output files for the format tests of redgb.io
+            if name == "disk_eject_hit":
+                save_text(name, disk, params, work)
+            elif name == "disk_si_rkf78_ce":
+                save_text(name, disk, params, work, events_only=True)
     finally:
         shutil.rmtree(work, ignore_errors=True)
 
