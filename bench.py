@@ -338,7 +338,7 @@ def dense_ring_section(args):
 
     from redgb import lib
 
-    disk = bodies.config_disk("dense_ring")
+    disk = bodies.config_disk("dense_ring", n=args.dense_ring_n)
     thr = bodies.thresholds(ejection=100.0, hit_centrum=0.05, collision_factor=1.0)
 
     def make(mode):
@@ -363,23 +363,25 @@ def dense_ring_section(args):
                 events.append((k, int(e["event_name"]), int(e["id1"]), int(e["id2"])))
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
-        return days, secs, events, abs((s.energy()[0] - E0) / E0)
+        c = s.counters()
+        return days, secs, events, abs((s.energy()[0] - E0) / E0), (c["n_passed_step"], c["n_tried_step"])
 
     mixed = make(T.GRAVITY_MIXED)
     tune = mixed.autotune(1)
-    days, secs, ev_m, dE = run(mixed, args.dense_ring_steps)
+    days, secs, ev_m, dE, att = run(mixed, args.dense_ring_steps)
     evals = 6 * args.dense_ring_steps
     pairs = disk.pairs_per_eval()
     cmp_m = make(T.GRAVITY_MIXED)
-    _, _, ev_a, _ = run(cmp_m, args.dense_ring_fp64_steps)
+    _, _, ev_a, _, _ = run(cmp_m, args.dense_ring_fp64_steps)
     fp = make(T.GRAVITY_FP64)
-    d_fp, s_fp, ev_f, dE_fp = run(fp, args.dense_ring_fp64_steps)
+    d_fp, s_fp, ev_f, dE_fp, _ = run(fp, args.dense_ring_fp64_steps)
     return {
         "workload": f"dense ring, {disk.n_total} bodies, RKF5 tol 1e-9, {args.dense_ring_steps} steps "
                     "(a sample of the 10-year run)",
         "mixed": {"sim_years_per_s": (days / T.YEAR) / secs, "steps": args.dense_ring_steps,
                   "ms_per_step": 1e3 * secs / args.dense_ring_steps, "simulated_days": days,
                   "pairs_per_s_lower_bound": evals * pairs / secs, "events": len(ev_m), "dE_over_E": dE,
+                  "steps_passed_tried": att,
                   "autotune": tune},
         "fp64": {"sim_years_per_s": (d_fp / T.YEAR) / s_fp, "steps": args.dense_ring_fp64_steps,
                  "ms_per_step": 1e3 * s_fp / args.dense_ring_fp64_steps, "dE_over_E": dE_fp},
@@ -533,6 +535,7 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--only-ensemble", action="store_true", help="the ensemble section alone (profiling)")
+    ap.add_argument("--only-dense-ring", action="store_true", help="the dense-ring section alone (profiling)")
     ap.add_argument("--ensemble-disks", type=int, default=256)
     ap.add_argument("--ensemble-years", type=float, default=10.0)
     ap.add_argument("--train-years", type=float, default=10.0)
@@ -540,10 +543,14 @@ def main():
     ap.add_argument("--cpu-ensemble-years", type=float, default=1.0)
     ap.add_argument("--no-dense-ring", action="store_true")
     ap.add_argument("--dense-ring-steps", type=int, default=20)
+    ap.add_argument("--dense-ring-n", type=int, default=None, help="planetesimals of the ring (default 131072)")
     ap.add_argument("--dense-ring-fp64-steps", type=int, default=2)
     args = ap.parse_args()
     if args.only_ensemble:
         print(json.dumps({"ensemble": ensemble_section(args)}))
+        return
+    if args.only_dense_ring:
+        print(json.dumps({"dense_ring": dense_ring_section(args)}))
         return
     if args.impl == "reference":
         rank, ws = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))

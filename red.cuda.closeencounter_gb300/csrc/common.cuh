@@ -54,6 +54,9 @@ struct GravArgs {
     const int* __restrict__ id;
     const double* __restrict__ rho;  // |r_i - r_0| of the step-start state (Hill test)
     const float* __restrict__ rf;    // mixed mode: radii in FP32 (event screens), else nullptr
+    const unsigned int* smax;        // mixed mode with screens: per system (4 words each), FP32 bits
+                                     // of the largest radius, mass and |r - r_0| of its light bodies
+                                     // (split_positions), else nullptr
     double* ax;  // output rows
     double* ay;
     double* az;

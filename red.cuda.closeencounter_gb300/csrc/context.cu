@@ -67,6 +67,8 @@ struct rg_ctx {
     int tiles_cap = 0;
     void* d_split = nullptr;  // FP32 (hi, lo) positions of the mixed kernel
     float* d_rf = nullptr;    // FP32 radii of the mixed kernels' event screens
+    unsigned int* d_smax = nullptr;  // the screens' maxima (split_positions)
+    int* d_screen_slot = nullptr;    // per body: 0 for a light body, -1 for a heavy one
     DevEvent* d_ev = nullptr;
     unsigned int* d_ev_count = nullptr;
     DevEvent* d_hill = nullptr;
@@ -126,6 +128,7 @@ struct rg_ctx {
     std::vector<Group> plan[2];
     std::vector<Tile> tiles;       // all groups' tiles, uploaded to d_tiles
     std::vector<int> heavy_mx;     // per tile (mixed groups): end of the heavy sources
+    std::vector<int> screen_slot;  // per body: 0 light, -1 heavy (the mixed kernels' screen cutoffs)
     std::vector<int> few_row0, few_nsrc;  // per tile (few-sink groups)
     std::vector<int> row_sink, row_nsrc;  // per terms-buffer row
     int few_rows = 0;
@@ -182,6 +185,8 @@ void free_all(rg_ctx* c)
     cudaFree(c->d_heavy);
     cudaFree(c->d_split);
     cudaFree(c->d_rf);
+    cudaFree(c->d_smax);
+    cudaFree(c->d_screen_slot);
     cudaFree(c->d_terms);
     cudaFree(c->d_partial);
     cudaFree(c->d_row_sink);
@@ -379,6 +384,8 @@ void build_tiles(rg_ctx* c)
         add_group(1, GROUP_DF_FEW, b.s0, light0, b.src1, b.block, FEW_SINKS_MAX);
         add_group(1, GROUP_MIXED, light0, b.s1, b.src1, b.block, MIXED_SINKS_PER_TILE);
     }
+    c->screen_slot.assign(nt, 0);
+    for (int i = 0; i < n_heavy; i++) c->screen_slot[i] = -1;
     c->tiles_dirty = true;
 }
 
@@ -421,6 +428,9 @@ int sync_tiles(rg_ctx* c)
         RG_CUDA_CHECK(cudaMemcpyAsync(c->d_heavy, c->heavy_mx.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->st));
         RG_CUDA_CHECK(cudaMemcpyAsync(c->d_few_row0, c->few_row0.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->st));
     }
+    if (!c->screen_slot.empty())
+        RG_CUDA_CHECK(cudaMemcpyAsync(c->d_screen_slot, c->screen_slot.data(), c->screen_slot.size() * sizeof(int),
+                                      cudaMemcpyHostToDevice, c->st));
     if (c->few_rows > 0) {
         RG_CUDA_CHECK(cudaMemcpyAsync(c->d_row_sink, c->row_sink.data(), c->few_rows * sizeof(int),
                                       cudaMemcpyHostToDevice, c->st));
@@ -471,6 +481,13 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
         if (rc) return rc;
         c->n_kernels++;
     }
+    // the screens' maxima serve the mixed kernel's per-sink cutoffs (light sinks x light sources)
+    bool mixed_tiles = false;
+    for (const auto& gr : c->plan[1]) mixed_tiles = mixed_tiles || gr.kind == GROUP_MIXED;
+    if (c->gravity_mode == RG_GRAVITY_MIXED && (g.record || g.hill) && mixed_tiles) {
+        RG_CUDA_CHECK(cudaMemsetAsync(c->d_smax, 0, SCREEN_MAX_WORDS * sizeof(unsigned int), c->st));
+        g.smax = c->d_smax;
+    }
     c->n_gravity_evals++;
     c->n_pairs += c->pairs_per_eval;
     const long prof = prof_begin(c, 0);
@@ -497,8 +514,9 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
         case GROUP_DF_ROWSEQ:
         case GROUP_DF_FEW:
             if (!split_done) {
-                rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, c->d_radius, c->n_total(),
-                                            (SplitPos*)c->d_split, c->d_rf, c->st);
+                rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, nullptr, c->d_screen_slot,
+                                            c->d_radius, c->n_total(), (SplitPos*)c->d_split, c->d_rf,
+                                            g.smax ? c->d_smax : nullptr, g.hill != 0, c->st);
                 split_done = true;
                 c->n_kernels++;
             }
@@ -516,8 +534,9 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
             break;
         case GROUP_MIXED:
             if (!split_done) {
-                rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, c->d_radius, c->n_total(),
-                                            (SplitPos*)c->d_split, c->d_rf, c->st);
+                rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, nullptr, c->d_screen_slot,
+                                            c->d_radius, c->n_total(), (SplitPos*)c->d_split, c->d_rf,
+                                            g.smax ? c->d_smax : nullptr, g.hill != 0, c->st);
                 split_done = true;
                 c->n_kernels++;
             }
@@ -1282,6 +1301,8 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
     chk(dalloc(&c->d_part, (size_t)5 * nt));
     chk(dalloc((char**)&c->d_split, SPLIT_POS_BYTES * (size_t)nt));
     chk(dalloc(&c->d_rf, nt));
+    chk(dalloc(&c->d_smax, SCREEN_MAX_WORDS));
+    chk(dalloc(&c->d_screen_slot, nt));
     if (!rc && cudaMallocHost((void**)&c->h_pin, 8 * sizeof(double)) != cudaSuccess)
         chk(set_error(RG_ERR_NOMEM, "pinned host buffer"));
     if (rc) {

@@ -517,6 +517,9 @@ struct rg_ens {
     int* d_type = nullptr;
     void* d_split = nullptr;
     float* d_rf = nullptr;  // FP32 radii of the mixed kernels' event screens
+    unsigned int* d_smax = nullptr;  // the screens' maxima per disk (split_positions)
+    int* d_screen_slot = nullptr;    // per body: its disk for a light body, -1 for a heavy one
+    std::vector<int> screen_slot;
     double* d_partial = nullptr;
     size_t partial_cap = 0;
     double* d_thr = nullptr;
@@ -647,7 +650,7 @@ void free_all(rg_ens* e)
                     e->d_ev, e->d_ev_count, e->d_hill, e->d_hill_count, e->d_part, e->d_base_of, e->d_log,
                     e->d_log_count, e->d_feat, e->d_dt_last, e->d_ideal_last, e->d_hist, e->d_proposed, e->d_step_prop_rej,
                     e->d_prop_rej_steps, e->d_cool, e->d_nprop, e->d_nprop_acc, e->d_nfallback, e->d_amax,
-                    e->d_hill3, e->d_nsi_of, e->d_kerr, e->d_rf};
+                    e->d_hill3, e->d_nsi_of, e->d_kerr, e->d_rf, e->d_smax, e->d_screen_slot};
     for (void* q : ptrs) cudaFree(q);
     for (auto& k : e->d_k) cudaFree(k);
     if (e->st) cudaStreamDestroy(e->st);
@@ -686,10 +689,12 @@ void build_gravity_plan(rg_ens* e)
     // group tiles of all disks by (mode, kind)
     std::vector<Tile> by[2][GROUP_KINDS];
     std::vector<int> hv[2][GROUP_KINDS];
+    e->screen_slot.assign(e->cap, -1);
     for (int s = 0; s < e->n_sys; s++) {
         const int b = e->base[s];
         const int nsi = e->n_si(s), nm = e->n_massive(s), nt = e->ntot[s];
         const int n_heavy = std::min(nsi, e->cnt[s][0] + e->cnt[s][1] + e->cnt[s][2]);
+        for (int q = n_heavy; q < nt; q++) e->screen_slot[b + q] = s;
         e->pairs_per_eval += (int64_t)nsi * (nm > 0 ? nm - 1 : 0) + (int64_t)(nm - nsi) * nsi + (int64_t)(nt - nm) * nm;
         struct Blk {
             int s0, s1, src1, block;
@@ -784,6 +789,7 @@ int upload_plans(rg_ens* e)
     up(e->d_stiles, e->stiles.data(), e->stiles.size() * sizeof(StageTile));
     up(e->d_tiles, e->tiles.data(), nt * sizeof(Tile));
     up(e->d_heavy, e->heavy.data(), nt * sizeof(int));
+    up(e->d_screen_slot, e->screen_slot.data(), e->screen_slot.size() * sizeof(int));
     up(e->d_few_row0, e->few_row0.data(), nt * sizeof(int));
     up(e->d_row_sink, e->row_sink.data(), e->row_sink.size() * sizeof(int));
     up(e->d_row_nsrc, e->row_nsrc.data(), e->row_nsrc.size() * sizeof(int));
@@ -835,6 +841,14 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
         if (rc) return rc;
         e->n_kernels++;
     }
+    // the screens' maxima serve the mixed kernel's per-sink cutoffs (light sinks x light sources)
+    bool mixed_tiles = false;
+    for (const auto& gr : e->plan[1]) mixed_tiles = mixed_tiles || gr.kind == GROUP_MIXED;
+    if (e->gravity_mode == RG_GRAVITY_MIXED && (g.record || g.hill) && mixed_tiles) {
+        RG_CUDA_CHECK(cudaMemsetAsync(e->d_smax, 0, (size_t)SCREEN_MAX_WORDS * e->n_sys * sizeof(unsigned int),
+                                      e->st));
+        g.smax = e->d_smax;
+    }
     bool split_done = false;
     for (const auto& gr : e->plan[e->gravity_mode == RG_GRAVITY_MIXED ? 1 : 0]) {
         g.tiles = e->d_tiles + gr.off;
@@ -852,8 +866,9 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
         case GROUP_DF_ROWSEQ:
         case GROUP_DF_FEW:
             if (!split_done) {
-                rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->d_radius, e->cap,
-                                            (SplitPos*)e->d_split, e->d_rf, e->st);
+                rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->d_base_of, e->d_screen_slot,
+                                            e->d_radius, e->cap, (SplitPos*)e->d_split, e->d_rf,
+                                            g.smax ? e->d_smax : nullptr, g.hill != 0, e->st);
                 split_done = true;
                 e->n_kernels++;
             }
@@ -871,8 +886,9 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
             break;
         case GROUP_MIXED:
             if (!split_done) {
-                rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->d_radius, e->cap,
-                                            (SplitPos*)e->d_split, e->d_rf, e->st);
+                rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->d_base_of, e->d_screen_slot,
+                                            e->d_radius, e->cap, (SplitPos*)e->d_split, e->d_rf,
+                                            g.smax ? e->d_smax : nullptr, g.hill != 0, e->st);
                 split_done = true;
                 e->n_kernels++;
             }
@@ -1327,6 +1343,8 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     chk(dalloc(&e->d_base_of, nt));
     chk(dalloc((char**)&e->d_split, SPLIT_POS_BYTES * nt));
     chk(dalloc(&e->d_rf, nt));
+    chk(dalloc(&e->d_smax, (size_t)SCREEN_MAX_WORDS * ns));
+    chk(dalloc(&e->d_screen_slot, nt));
     chk(dalloc(&e->d_thr, 5 * ns));
     chk(dalloc(&e->d_status, ns));
     chk(dalloc(&e->d_active, ns));

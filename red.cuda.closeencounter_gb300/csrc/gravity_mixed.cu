@@ -9,11 +9,11 @@
 //    the first heavy source) contribute double-float terms (below): FP64-class accuracy
 //    computed on the FP32 pipes, added to the same compensated accumulators.
 //  * Every other pair uses the FP64 positions split into FP32 (hi, lo) pairs once per
-//    force evaluation (split_positions, O(N) FP64 work).  The displacement is
+//    force evaluation (split_positions, O(N) integer work).  The displacement is
 //    (x_j^hi - x_i^hi) + (x_j^lo - x_i^lo): the hi difference is exact for neighbours
 //    (Sterbenz), so the displacement carries the FP64 positions' information down to
 //    FP32 resolution of the displacement itself.  1/r comes from the FP32 rsqrt refined
-//    by one Newton step, and the terms are summed in groups of 8 folded into compensated
+//    by one Newton step, and the terms are summed in groups of 16 folded into compensated
 //    (two-sum) FP32 accumulators per component.
 //  * Event tests (collision radius, Hill sphere) are re-evaluated in FP64 for every pair
 //    whose FP32 distance is within a 1e-3 relative margin of a threshold, so the event
@@ -87,25 +87,74 @@ __device__ __forceinline__ void split_coord(double v, float& hi, float& lo)
     }
 }
 
-// rf (optional): the radii rounded to FP32, for the event screens
+// |r_i - r_base| in FP32 from the split positions' leading parts (event screens)
+__device__ __forceinline__ float star_dist_f(const SplitPos& pi, const SplitPos& p0)
+{
+    const float dx = pi.xy.x - p0.xy.x, dy = pi.xy.z - p0.xy.z, dz = pi.zm.x - p0.zm.x;
+    return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
+// rf (optional): the radii rounded to FP32, for the event screens.  smax (optional, reset to
+// zero before the launch): per system k, FP32 bits of the largest screened value over its
+// light bodies that can be the source of an event test (screen_slot[i] = k, id >= 0) --
+// smax[4k] the radius, smax[4k + 1] the mass and smax[4k + 2] the star distance (with hill),
+// each the same FP32 value the screens read (base_of: each body's body 0, or nullptr for
+// index 0).  Heavy bodies (screen_slot -1: stars, giant and rocky planets) are screened
+// without a cutoff.
 __global__ void split_positions_kernel(const double* __restrict__ x, const double* __restrict__ y,
                                        const double* __restrict__ z, const double* __restrict__ m,
-                                       const int* __restrict__ id, const double* __restrict__ radius, int n,
-                                       SplitPos* __restrict__ out, float* __restrict__ rf)
+                                       const int* __restrict__ id, const int* __restrict__ base_of,
+                                       const int* __restrict__ screen_slot, const double* __restrict__ radius,
+                                       int n, SplitPos* __restrict__ out, float* __restrict__ rf,
+                                       unsigned int* smax, bool hill)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float xh, xl, yh, yl, zh, zl, mh = 0.0f, ml = 0.0f;
-    split_coord(x[i], xh, xl);
-    split_coord(y[i], yh, yl);
-    split_coord(z[i], zh, zl);
-    if (id[i] >= 0) split_bits(m[i], mh, ml);
-    out[i].xy = make_float4(xh, xl, yh, yl);
-    out[i].zm = make_float4(zh, zl, mh, ml);
-    if (rf) {
-        float rh, rl;
-        split_bits(radius[i], rh, rl);
-        rf[i] = rh;
+    float rmax = 0.0f, mmax = 0.0f, dmax = 0.0f;
+    int slot = -1;
+    if (i < n) {
+        SplitPos sp;
+        split_coord(x[i], sp.xy.x, sp.xy.y);
+        split_coord(y[i], sp.xy.z, sp.xy.w);
+        split_coord(z[i], sp.zm.x, sp.zm.y);
+        sp.zm.z = sp.zm.w = 0.0f;
+        if (id[i] >= 0) split_bits(m[i], sp.zm.z, sp.zm.w);
+        out[i] = sp;
+        if (rf) {
+            float rh, rl;
+            split_bits(radius[i], rh, rl);
+            rf[i] = rh;
+            if (smax && id[i] >= 0) slot = screen_slot[i];
+            if (slot >= 0) {
+                rmax = rh;
+                const int b = base_of ? base_of[i] : 0;
+                if (hill) {
+                    SplitPos p0;
+                    split_coord(x[b], p0.xy.x, p0.xy.y);
+                    split_coord(y[b], p0.xy.z, p0.xy.w);
+                    split_coord(z[b], p0.zm.x, p0.zm.y);
+                    mmax = sp.zm.z;
+                    dmax = star_dist_f(sp, p0);
+                }
+            }
+        }
+    }
+    if (!smax) return;
+    // lanes of one system: one atomic per value and warp (non-negative floats order as their
+    // bit patterns); a warp that spans systems or holds heavy bodies: one per lane
+    const int slot0 = __shfl_sync(0xffffffffu, slot, 0);
+    if (__all_sync(0xffffffffu, slot == slot0)) {
+        for (int off = 16; off > 0; off >>= 1) {
+            rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, off));
+            mmax = fmaxf(mmax, __shfl_xor_sync(0xffffffffu, mmax, off));
+            dmax = fmaxf(dmax, __shfl_xor_sync(0xffffffffu, dmax, off));
+        }
+        if ((threadIdx.x & 31) != 0) slot = -1;
+    }
+    if (slot >= 0) {
+        unsigned int* s = smax + SCREEN_MAX_WORDS * slot;
+        if (rmax > 0.0f) atomicMax(&s[0], __float_as_uint(rmax));
+        if (mmax > 0.0f) atomicMax(&s[1], __float_as_uint(mmax));
+        if (dmax > 0.0f) atomicMax(&s[2], __float_as_uint(dmax));
     }
 }
 
@@ -278,13 +327,6 @@ __device__ __forceinline__ double f2d_bits(float f)
 
 __device__ __forceinline__ double df_to_double(DF a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
 
-// |r_i - r_base| in FP32 from the split positions' leading parts (event screens)
-__device__ __forceinline__ float star_dist_f(const SplitPos& pi, const SplitPos& p0)
-{
-    const float dx = pi.xy.x - p0.xy.x, dy = pi.xy.z - p0.xy.z, dz = pi.zm.x - p0.zm.x;
-    return sqrtf(dx * dx + dy * dy + dz * dz);
-}
-
 // a double-float term into a compensated FP32 accumulator
 __device__ __forceinline__ void acc_df(Acc2& acc, DF t)
 {
@@ -334,6 +376,36 @@ __device__ __forceinline__ void df_screen(const GravArgs& g, const Tile& tile, i
         exact_event_tests(g, tile, i, j, g.px[i], g.py[i], g.pz[i], g.radius[i], g.mass[i], g.hill ? g.rho[i] : 0.0);
 }
 
+// A sink's cutoff on the FP32 r^2 beyond which no pair of it with a light source passes the
+// screens: each screen's limit grows with the source's radius, mass and star distance (FP32
+// sums and products of non-negative factors round monotonically), so the limit computed, in
+// the screens' own operation order, from the maxima over the system's light bodies (g.smax,
+// split_positions) bounds it (heavy sources are screened by the heavy-source loop, without
+// a cutoff).  The star-distance maximum gets a 1e-4 relative allowance for the rounding of
+// its own evaluation; the Hill limit on r^2 is (the limit on r^3)^(2/3) x 1.001.  An
+// undefined Hill limit (0 x inf) only arises where no Hill test can pass.  Without the
+// maxima every pair is screened.
+__device__ __forceinline__ float screen_cut2(const GravArgs& g, const Tile& tile, float Ri, float mi, float rhoi,
+                                             float inv3M)
+{
+    if (!g.smax) return 3.0e38f;
+    const unsigned int* sm = g.smax + SCREEN_MAX_WORDS * tile.sys;
+    const float margin = 1.001f;
+    float c = 0.0f;
+    if (g.record) {
+        const float lim = g.f_rad_f * (Ri + __uint_as_float(sm[0])) * margin;
+        c = lim * lim;
+    }
+    if (g.hill) {
+        const float h = 0.5f * (rhoi + __uint_as_float(sm[2]) * 1.0001f);
+        const float d3 = g.hill_f3_f * (mi + __uint_as_float(sm[1])) * inv3M * (h * h * h) *
+                         (margin * margin * margin);
+        const float cr = cbrtf(d3);
+        c = fmaxf(c, cr * cr * 1.001f);
+    }
+    return c;
+}
+
 struct SinkD {
     double x, y, z, R, m, rho;
 };
@@ -381,7 +453,8 @@ __device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile
             py[r] = fmaf(w, dy, py[r]);
             pz[r] = fmaf(w, dz, pz[r]);
             near_mask[r] |= (unsigned)near << (q - q_begin);
-            if (SCREEN) {
+            // one compare per pair: beyond its cutoff no pair of this sink can pass the screens
+            if (SCREEN && r2 < s_sinkf[lane + 32 * r].w) {
                 const int li = si[r] - tile.base, lj = j - tile.base;
                 if (li > 0 && li > lj && (!DIAG || j != si[r]) && mj >= 0.0f) {
                     const float4 sf = s_sinkf[lane + 32 * r];  // R, m, rho of the sink in FP32
@@ -474,7 +547,7 @@ __device__ __forceinline__ void tma_tile(void* dst, const void* src, unsigned by
 struct MixedSmem {
     SplitPos sp[2][MX_T];              // double-buffered source tiles (TMA destination)
     SinkD sink[MX_S];
-    float4 sinkf[MX_S];                // R, m, rho of the sinks in FP32 (event screens)
+    float4 sinkf[MX_S];                // R, m, rho, r^2 cutoff of the sinks in FP32 (screens)
     Acc2 part[MX_WARPS][3][MX_S];      // per-warp compensated partial sums
     float R[2][MX_T], rho[2][MX_T];    // screening data of the tiles (SCREEN only)
     unsigned long long bar[2];
@@ -529,6 +602,12 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
         S.sinkf[s] = make_float4((float)sd.R, (float)sd.m, (float)sd.rho, 0.0f);
     }
     const float inv3M = (SCREEN && g.hill) ? (float)(1.0 / (3.0 * g.mass[tile.base])) : 0.0f;
+    // .w: the sink's cutoff on r^2 (screen_cut2); padding sinks get none
+    for (int s = threadIdx.x; s < MX_S; s += blockDim.x) {
+        float4& sf = S.sinkf[s];
+        sf.w = (SCREEN && tile.sink_begin + s < tile.sink_end) ? screen_cut2(g, tile, sf.x, sf.y, sf.z, inv3M)
+                                                               : -1.0f;
+    }
     __syncthreads();
     // the first two tiles travel while the heavy sources are summed
     if (threadIdx.x == 0) {
@@ -929,10 +1008,12 @@ int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row
 }
 
 int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id,
-                           const double* radius, int n, SplitPos* out, float* rf, cudaStream_t st)
+                           const int* base_of, const int* screen_slot, const double* radius, int n,
+                           SplitPos* out, float* rf, unsigned int* smax, bool hill, cudaStream_t st)
 {
     if (n <= 0) return 0;
-    split_positions_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, m, id, radius, n, out, rf);
+    split_positions_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, m, id, base_of, screen_slot, radius, n, out,
+                                                            rf, smax, hill);
     RG_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

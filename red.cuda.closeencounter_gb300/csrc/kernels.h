@@ -77,7 +77,9 @@ constexpr int MIXED_SINKS_PER_TILE = 128;
 constexpr int MIXED_SOURCE_TILE = 256;  // source-chunk lengths are multiples of this
 constexpr size_t SPLIT_POS_BYTES = 32;  // per body
 int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id,
-                           const double* radius, int n, SplitPos* out, float* rf, cudaStream_t st);
+                           const int* base_of, const int* screen_slot, const double* radius, int n,
+                           SplitPos* out, float* rf, unsigned int* smax, bool hill, cudaStream_t st);
+constexpr int SCREEN_MAX_WORDS = 4;  // GravArgs::smax per system: radius, mass, star distance, spare
 int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* heavy_end, float near_ratio,
                             int n_chunks, int chunk, double* partial, int n_part, unsigned int* err,
                             cudaStream_t st);

@@ -99,3 +99,31 @@ def test_ensemble_mixed_and_energy(gpulib):
         assert ens.stats(s)["status"] == T.SYS_DONE
     n_k, n_g = ens.kernel_count()
     assert n_g > 0 and n_k > n_g
+
+
+def test_ensemble_mixed_screen_cutoffs_keep_every_event(gpulib):
+    """Three crowded disks (3000 protoplanets with radii x 300 and a giant; Hill factor 3:
+    about 20 overlapping and 50 Hill pairs each at the start).  The mixed kernels skip the
+    detailed screens beyond each sink's cutoff from its own disk's largest light-body
+    radius, mass and star distance, screen the star and the giant always, and record the
+    FP64 ensemble's events.  One step (the first trial step, 0.001 day): the next step sizes
+    follow error estimates far below the tolerance, i.e. rounding noise, which differs
+    between the two arithmetics."""
+    disks = []
+    for seed in (51, 52, 53):
+        d = bodies.make_disk(n_pl=3000, pl_type=T.BODY_PROTOPLANET, seed=seed, m_range=(1e-9, 1e-7),
+                             giants=((9.55e-4, 5.2, 0.05),), a_range=(1.0, 1.3), sigma_e=0.05, sigma_i=0.02)
+        d.p["radius"][2:] *= 300.0
+        disks.append(d)
+    thr = bodies.thresholds(collision_factor=1.0)
+    out = {}
+    for mode in (T.GRAVITY_FP64, T.GRAVITY_MIXED):
+        ens = Ensemble(disks, thr)
+        ens.set_integrator(0.001, 1e-10)
+        ens.set_options(gravity_mode=mode, hill_factor=3.0)
+        ens.advance(0.0005)  # runs while t <= t_stop: one step of the first trial size
+        ev, sysv = ens.events()
+        out[mode] = [(int(s), int(e["event_name"]), int(e["id1"]), int(e["id2"])) for e, s in zip(ev, sysv)]
+        assert all(ens.stats(s)["n_tried_step"] == 1 for s in range(len(disks)))
+    assert len(out[T.GRAVITY_FP64]) > 60 and len({k for _, k, _, _ in out[T.GRAVITY_FP64]}) >= 2
+    assert out[T.GRAVITY_MIXED] == out[T.GRAVITY_FP64]

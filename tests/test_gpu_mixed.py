@@ -71,3 +71,24 @@ def test_mixed_event_list_identical(gpulib):
     k = min(len(mine), len(ref))
     assert [(int(e["event_name"]), int(e["id1"]), int(e["id2"])) for e in mine[:k]] == \
            [(int(e["name"]), int(e["id1"]), int(e["id2"])) for e in ref[:k]]
+
+
+def test_mixed_screen_cutoffs_keep_every_event(gpulib):
+    """A crowded ring (planetesimal radii x 300, Hill factor 3: about 150 overlapping and
+    250 Hill pairs at the start, masses spread over a factor of 100): the mixed kernels
+    skip the detailed screens beyond each sink's cutoff from the evaluation's largest
+    radius, mass and star distance, and still find exactly the FP64 path's events."""
+    disk = bodies.config_disk("dense_ring", n=16384)
+    disk.p["radius"][1:] *= 300.0
+    thr = bodies.thresholds(collision_factor=1.0)
+    lists = {}
+    for mode in (T.GRAVITY_FP64, T.GRAVITY_MIXED):
+        s = lib.System(disk, thr, event_capacity=1 << 16)
+        s.set_gravity_mode(mode)
+        s.set_integrator(T.INT_RKF78, 0.02, False)
+        s.set_event_options(hill_factor=3.0)
+        s.advance(0.04)
+        lists[mode] = [(int(e["event_name"]), int(e["id1"]), int(e["id2"])) for e in s.events()]
+    names = {k for k, _, _ in lists[T.GRAVITY_FP64]}
+    assert len(lists[T.GRAVITY_FP64]) > 100 and len(names) >= 2, (len(lists[T.GRAVITY_FP64]), names)
+    assert lists[T.GRAVITY_MIXED] == lists[T.GRAVITY_FP64]
