@@ -7,7 +7,9 @@
 //  * Heavy sources (the leading SI bodies: star, giant and rocky planets -- `heavy_end`
 //    per tile) and near pairs (m_j / r^2 above `near_ratio` times the sink's pull from
 //    the first heavy source) contribute double-float terms (below): FP64-class accuracy
-//    computed on the FP32 pipes, added to the same compensated accumulators.
+//    computed on the FP32 pipes, added to the same compensated accumulators.  Their
+//    displacement comes from the FP64 positions where the split positions would not
+//    resolve it (heavy sources always; others closer than |x| / 256: close_r2).
 //  * Every other pair uses the FP64 positions split into FP32 (hi, lo) pairs once per
 //    force evaluation (split_positions, O(N) integer work).  The displacement is
 //    (x_j^hi - x_i^hi) + (x_j^lo - x_i^lo): the hi difference is exact for neighbours
@@ -335,11 +337,10 @@ __device__ __forceinline__ void acc_df(Acc2& acc, DF t)
 }
 
 // the term m_j (r_j - r_i) / |r_j - r_i|^3 of one pair; r2f = |r_j - r_i|^2 in FP32
-__device__ __forceinline__ void df_term(const SplitPos& si, const SplitPos& pj, DF& tx, DF& ty, DF& tz, float& r2f)
+// the term from a double-float displacement r_j - r_i and the source's split mass
+__device__ __forceinline__ void df_term_disp(DF dx, DF dy, DF dz, float mh, float ml, DF& tx, DF& ty, DF& tz,
+                                             float& r2f)
 {
-    const DF dx = df_diff(pj.xy.x, pj.xy.y, si.xy.x, si.xy.y);
-    const DF dy = df_diff(pj.xy.z, pj.xy.w, si.xy.z, si.xy.w);
-    const DF dz = df_diff(pj.zm.x, pj.zm.y, si.zm.x, si.zm.y);
     DF r2 = df_add(df_add(df_mul(dx, dx), df_mul(dy, dy)), df_mul(dz, dz));
     // a merged body parked at 1e20 AU (pp_disk.cu:1184) overflows r^2 in FP32; its mass is 0
     if (!(r2.hi < 1.0e30f)) r2 = DF{1.0e30f, 0.0f};
@@ -347,11 +348,44 @@ __device__ __forceinline__ void df_term(const SplitPos& si, const SplitPos& pj, 
     const DF p = df_mul(r2, df_two_prod(y0, y0));
     const float h = (1.0f - p.hi) - p.lo;  // 1 - r^2 y0^2, small: FP32 suffices
     const DF y = df_fast_sum(y0, 0.5f * y0 * h);
-    const DF w = df_mul(df_mul(df_mul(y, y), y), DF{pj.zm.z, pj.zm.w});
+    const DF w = df_mul(df_mul(df_mul(y, y), y), DF{mh, ml});
     tx = df_mul(w, dx);
     ty = df_mul(w, dy);
     tz = df_mul(w, dz);
     r2f = r2.hi;
+}
+
+// the term from the split positions: the displacement (x_j^hi - x_i^hi) + (x_j^lo - x_i^lo)
+// carries the positions to 2^-48 |x| (the split keeps 48 of FP64's 53 significant bits)
+__device__ __forceinline__ void df_term(const SplitPos& si, const SplitPos& pj, DF& tx, DF& ty, DF& tz, float& r2f)
+{
+    df_term_disp(df_diff(pj.xy.x, pj.xy.y, si.xy.x, si.xy.y), df_diff(pj.xy.z, pj.xy.w, si.xy.z, si.xy.w),
+                 df_diff(pj.zm.x, pj.zm.y, si.zm.x, si.zm.y), pj.zm.z, pj.zm.w, tx, ty, tz, r2f);
+}
+
+__device__ __forceinline__ DF split_df(double v)
+{
+    DF d;
+    split_bits(v, d.hi, d.lo);
+    return d;
+}
+
+// r^2 below which a pair of this sink takes the FP64 displacement: beyond it the split
+// positions' error, 2^-48 (|x_i| + |x_j|) per component, stays below ~1e-12 of |r_j - r_i|
+__device__ __forceinline__ float close_r2(const SplitPos& p)
+{
+    const float m = fmaxf(fabsf(p.xy.x), fmaxf(fabsf(p.xy.z), fabsf(p.zm.x))) * (1.0f / 256.0f);
+    return m * m;
+}
+
+// the term from the FP64 positions: the displacement is one FP64 subtraction per component
+// (exact for neighbours, Sterbenz), kept to 2^-48 of itself -- for close pairs, where the
+// split positions' 2^-48 |x| would be a large part of |r_j - r_i|
+__device__ __forceinline__ void df_term_fp64(double xi, double yi, double zi, double xj, double yj, double zj,
+                                             float mh, float ml, DF& tx, DF& ty, DF& tz, float& r2f)
+{
+    df_term_disp(split_df(__dadd_rn(xj, -xi)), split_df(__dadd_rn(yj, -yi)), split_df(__dadd_rn(zj, -zi)), mh, ml,
+                 tx, ty, tz, r2f);
 }
 
 // FP32 screen of the event tests of pair_term (pp_disk.cu:262-280) with a 1e-3 margin;
@@ -650,6 +684,7 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
         for (int j = tile.src_begin + warp; j < heavy_end; j += MX_WARPS) {
             if (0 > g.id[j]) continue;
             const SplitPos pj = a.sp[j];
+            const double xj = g.px[j], yj = g.py[j], zj = g.pz[j];
             float Rj = 0.0f, rhoj = 0.0f;
             if (SCREEN) {
                 Rj = (float)g.radius[j];
@@ -659,12 +694,10 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
             for (int r = 0; r < MX_R; r++) {
                 const int s = lane + 32 * r;
                 if (si[r] >= tile.sink_end || j == si[r]) continue;
-                SplitPos sp;
-                sp.xy = make_float4(xh[r], xl[r], yh[r], yl[r]);
-                sp.zm = make_float4(zh[r], zl[r], 0.0f, 0.0f);
+                const SinkD& sd = S.sink[s];
                 DF tx, ty, tz;
                 float r2f;
-                df_term(sp, pj, tx, ty, tz, r2f);
+                df_term_fp64(sd.x, sd.y, sd.z, xj, yj, zj, pj.zm.z, pj.zm.w, tx, ty, tz, r2f);
                 acc_df(ax[r], tx);
                 acc_df(ay[r], ty);
                 acc_df(az[r], tz);
@@ -697,7 +730,8 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
             else
                 mixed_slice<false, SCREEN>(a, tile, j0, q_begin, q_end, S.sp[b], S.sinkf, inv3M, S.R[b], S.rho[b], S.sink, si, xh,
                                            xl, yh, yl, zh, zl, near_lim, ax, ay, az, near_mask, lane);
-            // near pairs of this slice: the double-float term (FP64-class accuracy on the FP32 pipes)
+            // near pairs of this slice: the double-float term (FP64-class accuracy on the FP32
+            // pipes), from the FP64 displacement for pairs closer than the split positions resolve
 #pragma unroll
             for (int r = 0; r < MX_R; r++) {
                 unsigned m = near_mask[r];
@@ -705,12 +739,19 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
                 SplitPos sp;
                 sp.xy = make_float4(xh[r], xl[r], yh[r], yl[r]);
                 sp.zm = make_float4(zh[r], zl[r], 0.0f, 0.0f);
+                const float close2 = close_r2(sp);
                 while (m) {
                     const int bit = __ffs(m) - 1;
                     m &= m - 1;
+                    const SplitPos pj = S.sp[b][q_begin + bit];
                     DF tx, ty, tz;
                     float r2f;
-                    df_term(sp, S.sp[b][q_begin + bit], tx, ty, tz, r2f);
+                    df_term(sp, pj, tx, ty, tz, r2f);
+                    if (r2f < close2) {
+                        const int j = j0 + q_begin + bit;
+                        const SinkD& sd = S.sink[lane + 32 * r];
+                        df_term_fp64(sd.x, sd.y, sd.z, g.px[j], g.py[j], g.pz[j], pj.zm.z, pj.zm.w, tx, ty, tz, r2f);
+                    }
                     acc_df(ax[r], tx);
                     acc_df(ay[r], ty);
                     acc_df(az[r], tz);
@@ -803,6 +844,7 @@ __global__ void __launch_bounds__(DF_ROW_NT, 8) grav_df_rowseq(GravArgs g, const
             mi = si.zm.z;
         }
     }
+    const float close2 = close_r2(si);
     DF ax{0.0f, 0.0f}, ay{0.0f, 0.0f}, az{0.0f, 0.0f};
     for (int j0 = tile.src_begin; j0 < tile.src_end; j0 += DF_ROW_NT) {
         const int nj = min(DF_ROW_NT, tile.src_end - j0);
@@ -823,6 +865,9 @@ __global__ void __launch_bounds__(DF_ROW_NT, 8) grav_df_rowseq(GravArgs g, const
                 DF tx, ty, tz;
                 float r2f;
                 df_term(si, s_p[q], tx, ty, tz, r2f);
+                if (r2f < close2)
+                    df_term_fp64(g.px[i], g.py[i], g.pz[i], g.px[j], g.py[j], g.pz[j], s_p[q].zm.z, s_p[q].zm.w, tx,
+                                 ty, tz, r2f);
                 ax = df_add(ax, tx);
                 ay = df_add(ay, ty);
                 az = df_add(az, tz);
@@ -864,7 +909,7 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
     if (c0 >= nsrc) return;
     const int ns = tile.sink_end - tile.sink_begin;  // <= SMAX
     __shared__ SplitPos s_sink[SMAX];
-    __shared__ float s_R[SMAX], s_rho[SMAX], s_m[SMAX];
+    __shared__ float s_R[SMAX], s_rho[SMAX], s_m[SMAX], s_close2[SMAX];
     __shared__ int s_act[SMAX];
     __shared__ DF s_red[8][3 * SMAX];
     SplitPos p0{};
@@ -881,6 +926,7 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
         s_R[threadIdx.x] = SCREEN ? g.rf[i] : 0.0f;
         s_rho[threadIdx.x] = (SCREEN && g.hill) ? star_dist_f(pi, p0) : 0.0f;
         s_m[threadIdx.x] = pi.zm.z;
+        s_close2[threadIdx.x] = close_r2(pi);
     }
     __syncthreads();
     DF acc[SMAX][3];
@@ -906,6 +952,9 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
                     DF tx, ty, tz;
                     float r2f;
                     df_term(s_sink[s], pj, tx, ty, tz, r2f);
+                    if (r2f < s_close2[s])
+                        df_term_fp64(g.px[i], g.py[i], g.pz[i], g.px[j], g.py[j], g.pz[j], pj.zm.z, pj.zm.w, tx, ty,
+                                     tz, r2f);
                     acc[s][0] = df_add(acc[s][0], tx);
                     acc[s][1] = df_add(acc[s][1], ty);
                     acc[s][2] = df_add(acc[s][2], tz);

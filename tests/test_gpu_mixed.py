@@ -47,6 +47,28 @@ def test_mixed_force_error(gpulib, config, n):
     assert mx < MAX_REL and rms < RMS_REL
 
 
+def test_mixed_close_pairs_force_error(gpulib):
+    """Pairs closer than the split positions resolve (2^-48 |x| ~ 4e-15 AU at 1 AU): light
+    pairs 1e-7 to 1e-5 AU apart (near pairs of the mixed kernel) and planetesimals within
+    0.002 AU of a giant (double-float kernels).  Their displacements come from the FP64
+    positions, so the force error stays within the same bounds."""
+    disk = bodies.config_disk("self_gravitating", n=4096)
+    for k in range(8):
+        a, b = 10 + k, 2000 + k
+        for f, c in zip("xyz", (1.0, 2.0, -1.0)):
+            disk.r[f][b] = disk.r[f][a] + c * 10.0 ** (-7 + 2 * (k % 2)) * (k + 1)
+    mx, rms, _, _ = force_error(disk)
+    print(f"close light pairs: max rel {mx:.3e} rms rel {rms:.3e}")
+    assert mx < MAX_REL and rms < RMS_REL
+    disk = bodies.config_disk("planetesimal_disk")
+    for k, off in enumerate(((2e-3, 1e-3, 0.0), (0.0, -5e-4, 1e-4), (1e-4, 1e-4, 1e-4))):
+        for f, c in zip("xyz", off):
+            disk.r[f][3 + k] = disk.r[f][1] + c
+    mx, rms, _, _ = force_error(disk)
+    print(f"planetesimals near a giant: max rel {mx:.3e} rms rel {rms:.3e}")
+    assert mx < MAX_REL and rms < RMS_REL
+
+
 def test_mixed_fp64_reference_matches_oracle_rows(gpulib):
     """The FP64 accelerations used as the yardstick above are the oracle's."""
     disk = bodies.config_disk("self_gravitating", n=2048)
