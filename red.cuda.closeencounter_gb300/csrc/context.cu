@@ -80,6 +80,7 @@ struct rg_ctx {
     unsigned long long* d_maxbits = nullptr;
     double* d_dt = nullptr;
     double* d_part = nullptr;
+    double* d_records = nullptr;  // r and v as vec_t records (state in / out): 8 doubles per body
     double* h_pin = nullptr;  // pinned: [0] dt, [1] max bits, [2..3] counts
     // host mirrors of the body parameters (authoritative; the state lives on the device)
     std::vector<rg_param_t> p;
@@ -202,6 +203,7 @@ void free_all(rg_ctx* c)
     cudaFree(c->d_maxbits);
     cudaFree(c->d_dt);
     cudaFree(c->d_part);
+    cudaFree(c->d_records);
     if (c->h_pin) cudaFreeHost(c->h_pin);
     for (auto e : c->ev_pool) cudaEventDestroy(e);
     if (c->st) cudaStreamDestroy(c->st);
@@ -1299,6 +1301,7 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
     chk(dalloc(&c->d_maxbits, 1));
     chk(dalloc(&c->d_dt, 1));
     chk(dalloc(&c->d_part, (size_t)5 * nt));
+    chk(dalloc(&c->d_records, (size_t)8 * nt));
     chk(dalloc((char**)&c->d_split, SPLIT_POS_BYTES * (size_t)nt));
     chk(dalloc(&c->d_rf, nt));
     chk(dalloc(&c->d_smax, SCREEN_MAX_WORDS));
@@ -1547,21 +1550,14 @@ int rg_get_n_total(rg_ctx* c, rg_counts_t* n, int* n_total)
 static int get_state_impl(rg_ctx* c, rg_vec_t* r, rg_vec_t* v, rg_param_t* p, rg_body_metadata_t* md, bool file_units)
 {
     const int n = c->n_total();
-    if (r || v) {
-        std::vector<double> h;
-        int rc = download_state(c, h);
+    if ((r || v) && n > 0) {  // records built on the device, one copy per array
+        double* dr = c->d_records;
+        double* dv = c->d_records + (size_t)4 * n;
+        int rc = launch_rows_to_records(c->d_y, n, c->cap, GAUSS, file_units, dr, dv, c->st);  // pp_disk.cu:1720-1722
         if (rc) return rc;
-        for (int i = 0; i < n; i++) {
-            if (r) r[i] = rg_vec_t{h[i], h[(size_t)n + i], h[(size_t)2 * n + i], 0.0};
-            if (v) {
-                v[i] = rg_vec_t{h[(size_t)3 * n + i], h[(size_t)4 * n + i], h[(size_t)5 * n + i], 0.0};
-                if (file_units) {  // pp_disk.cu:1720-1722
-                    v[i].x = v[i].x * GAUSS;
-                    v[i].y = v[i].y * GAUSS;
-                    v[i].z = v[i].z * GAUSS;
-                }
-            }
-        }
+        if (r) RG_CUDA_CHECK(cudaMemcpyAsync(r, dr, (size_t)n * sizeof(rg_vec_t), cudaMemcpyDeviceToHost, c->st));
+        if (v) RG_CUDA_CHECK(cudaMemcpyAsync(v, dv, (size_t)n * sizeof(rg_vec_t), cudaMemcpyDeviceToHost, c->st));
+        RG_CUDA_CHECK(cudaStreamSynchronize(c->st));
     }
     if (p) std::memcpy(p, c->p.data(), (size_t)n * sizeof(rg_param_t));
     if (md) std::memcpy(md, c->md.data(), (size_t)n * sizeof(rg_body_metadata_t));
@@ -1582,20 +1578,25 @@ int rg_get_state_internal(rg_ctx* c, rg_vec_t* r, rg_vec_t* v, rg_param_t* p, rg
     RG_GUARD(get_state_impl(c, r, v, p, md, false));
 }
 
+static int set_state_impl(rg_ctx* c, const rg_vec_t* r, const rg_vec_t* v)
+{
+    const int n = c->n_total();
+    if (n > 0) {  // one copy per array, the rows built on the device (v / k as the host would)
+        double* dr = c->d_records;
+        double* dv = c->d_records + (size_t)4 * n;
+        RG_CUDA_CHECK(cudaMemcpyAsync(dr, r, (size_t)n * sizeof(rg_vec_t), cudaMemcpyHostToDevice, c->st));
+        RG_CUDA_CHECK(cudaMemcpyAsync(dv, v, (size_t)n * sizeof(rg_vec_t), cudaMemcpyHostToDevice, c->st));
+        const int rc = launch_records_to_rows(dr, dv, n, c->cap, GAUSS, c->d_y, c->st);
+        if (rc) return rc;
+        RG_CUDA_CHECK(cudaStreamSynchronize(c->st));
+    }
+    return RG_OK;
+}
+
 int rg_set_state(rg_ctx* c, const rg_vec_t* r, const rg_vec_t* v)
 {
     if (!c || !r || !v) return set_error(RG_ERR_ARG, "bad argument");
-    const int n = c->n_total();
-    std::vector<double> h((size_t)6 * n);
-    for (int i = 0; i < n; i++) {
-        h[i] = r[i].x;
-        h[(size_t)n + i] = r[i].y;
-        h[(size_t)2 * n + i] = r[i].z;
-        h[(size_t)3 * n + i] = v[i].x / GAUSS;
-        h[(size_t)4 * n + i] = v[i].y / GAUSS;
-        h[(size_t)5 * n + i] = v[i].z / GAUSS;
-    }
-    RG_GUARD(upload_state(c, h));
+    RG_GUARD(set_state_impl(c, r, v));
 }
 
 // CUDA-event time of one force evaluation (stage-0 form, no event recording) over `reps`

@@ -55,6 +55,12 @@ struct EjectRec {
 int launch_ejection(const double* x, const double* y, const double* z, const int* id, const int* type, int n,
                     const double* thr, EjectRec* rec, unsigned int* count, unsigned int cap, cudaStream_t st);
 
+// vec_t records (r, v: 4 doubles per body) <-> the 6 state rows of `stride`; v / k on the way
+// in, v * k on the way out when `scale`
+int launch_records_to_rows(const double* r, const double* v, int n, int stride, double k, double* y, cudaStream_t st);
+int launch_rows_to_records(const double* y, int n, int stride, double k, bool scale, double* r, double* v,
+                           cudaStream_t st);
+
 struct EnergyArgs {
     const double* y;  // 6 rows of stride
     const double* mass;

@@ -211,6 +211,57 @@ int launch_ejection(const double* x, const double* y, const double* z, const int
 }
 
 // ---------------------------------------------------------------------------------------
+// State records <-> the state rows.  Records are the reference's vec_t {x, y, z, w} (4
+// doubles; r in AU, v in AU/day, w = 0), rows the integrator's SoA (v in AU per k-scaled
+// day).  On the way in velocities are divided by k (the load transform, pp_disk.cu:1498-1551),
+// on the way out multiplied by it (print_result_ascii, pp_disk.cu:1720-1722) when `scale`:
+// single IEEE operations, as the host loops round them.
+
+__global__ void records_to_rows_kernel(const double* __restrict__ r, const double* __restrict__ v, int n,
+                                       int stride, double k, double* __restrict__ y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t s = (size_t)stride;
+    for (int c = 0; c < 3; c++) {
+        y[c * s + i] = r[4 * (size_t)i + c];
+        y[(3 + c) * s + i] = __ddiv_rn(v[4 * (size_t)i + c], k);
+    }
+}
+
+__global__ void rows_to_records_kernel(const double* __restrict__ y, int n, int stride, double k, bool scale,
+                                       double* __restrict__ r, double* __restrict__ v)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const size_t s = (size_t)stride;
+    for (int c = 0; c < 3; c++) {
+        r[4 * (size_t)i + c] = y[c * s + i];
+        const double vc = y[(3 + c) * s + i];
+        v[4 * (size_t)i + c] = scale ? __dmul_rn(vc, k) : vc;
+    }
+    r[4 * (size_t)i + 3] = 0.0;
+    v[4 * (size_t)i + 3] = 0.0;
+}
+
+int launch_records_to_rows(const double* r, const double* v, int n, int stride, double k, double* y, cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    records_to_rows_kernel<<<(n + 255) / 256, 256, 0, st>>>(r, v, n, stride, k, y);
+    RG_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int launch_rows_to_records(const double* y, int n, int stride, double k, bool scale, double* r, double* v,
+                           cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    rows_to_records_kernel<<<(n + 255) / 256, 256, 0, st>>>(y, n, stride, k, scale, r, v);
+    RG_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+// ---------------------------------------------------------------------------------------
 // Energy and angular momentum partials (not in the reference).  Per body i: kinetic
 // energy, the potential of the pairs (i, j < i) the force model couples (all j < i for a
 // self-interacting body, j < n_si for a planetesimal), and m r x v, each summed with a

@@ -176,10 +176,20 @@ class System:
         self._call("get_n_total", self.handle, ctypes.byref(c), ctypes.byref(n))
         return c, n.value
 
-    def state(self, internal=False):
+    def state(self, internal=False, out=None, params=True):
+        """(r, v, p, md, t): positions and velocities as vec_t records (AU, AU/day; internal
+        units with `internal`), parameters, metadata and the time.  `out`: two vec_t arrays of
+        n_total records to fill instead of new ones (e.g. pinned host buffers); with
+        params=False, p and md are not copied and come back as None."""
         _, n = self.n_total()
-        r, v = np.zeros(n, T.VEC), np.zeros(n, T.VEC)
-        p, md = np.zeros(n, T.PARAM), np.zeros(n, T.BODY_MD)
+        if out is None:
+            r, v = np.zeros(n, T.VEC), np.zeros(n, T.VEC)
+        else:
+            r, v = out
+            for a in (r, v):
+                if a.dtype != T.VEC or a.shape != (n,) or not a.flags["C_CONTIGUOUS"]:
+                    raise ValueError("out: two contiguous vec_t arrays of n_total records")
+        p, md = (np.zeros(n, T.PARAM), np.zeros(n, T.BODY_MD)) if params else (None, None)
         t = ctypes.c_double()
         self._call("get_state_internal" if internal else "get_state", self.handle, T.ptr(r), T.ptr(v), T.ptr(p),
                    T.ptr(md), ctypes.byref(t))

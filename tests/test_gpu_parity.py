@@ -141,6 +141,36 @@ def test_hill_close_encounters_match_oracle(gpulib):
     _assert_same_state(g, o)
 
 
+def test_state_records_in_and_out(gpulib):
+    """rg_set_state / rg_get_state: vec_t records in file units, converted on the device
+    (v / k in, v * k out: the reference's load and print transforms, one IEEE operation
+    each); pinned host buffers through out= give the same records as fresh arrays."""
+    import torch
+    disk = bodies.make_disk(n_pl=300, seed=12)
+    s = gpu_system(disk, bodies.thresholds())
+    r, v = s.state()[:2]
+    rng = np.random.RandomState(4)
+    for f in "xyz":
+        r[f] *= 1.0 + 1e-3 * rng.standard_normal(len(r))
+        v[f] *= 1.0 + 1e-3 * rng.standard_normal(len(v))
+    s.set_state(r, v)
+    ri, vi = s.state(internal=True)[:2]
+    for f in "xyz":
+        assert H.same(ri[f], r[f])
+        assert H.same(vi[f], v[f] / T.GAUSS)
+    rf, vf, p, md, _ = s.state()
+    for f in "xyz":
+        assert H.same(vf[f], vi[f] * T.GAUSS)
+    assert np.all(rf["w"] == 0.0) and np.all(vf["w"] == 0.0)
+    n = len(r)
+    pin = [torch.empty(4 * n, dtype=torch.float64, pin_memory=True).numpy().view(T.VEC) for _ in range(2)]
+    r2, v2, p2, md2, _ = s.state(out=pin, params=False)
+    assert p2 is None and md2 is None and r2 is pin[0]
+    assert r2.tobytes() == rf.tobytes() and v2.tobytes() == vf.tobytes()
+    with pytest.raises(ValueError):
+        s.state(out=(np.zeros(n - 1, T.VEC), np.zeros(n, T.VEC)))
+
+
 def test_energy_matches_oracle(gpulib):
     disk = bodies.make_disk(n_pl=500, seed=3, n_tp=10, embryos=((1e-6, 1.5, 0.0),))
     g = gpu_system(disk, bodies.thresholds())
