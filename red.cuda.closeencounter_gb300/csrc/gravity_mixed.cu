@@ -884,10 +884,15 @@ __global__ void __launch_bounds__(DF_ROW_NT, 8) grav_df_rowseq(GravArgs g, const
 }
 
 // Few-sink kernel: tiles of at most FEW_SINKS_MAX heavy sinks against many sources.
-// grid (source chunks, tiles); a CTA takes DF_FEW_CHUNK sources of one tile, every thread
-// keeps double-float sums for all the tile's sinks, and the CTA's sums go to
-// partial[(comp * rows + row) * pitch + chunk] as FP64; df_few_final adds the chunks.
-constexpr int DF_FEW_CHUNK = 2048;
+// grid (source chunks, tiles); a CTA takes `chunk` sources of one tile, every thread keeps
+// double-float sums for all the tile's sinks, and the CTA's sums go to
+// partial[(comp * rows + row) * pitch + chunk index] as FP64; df_few_final adds the chunks.
+// The chunk is DF_FEW_CHUNK_MAX sources (the per-CTA reduction of the sums is then a small
+// part of the work), halved -- down to one source per thread -- while the grid has fewer
+// than DF_FEW_GRID_MIN CTAs (two per SM of a 152-SM GB300), e.g. for a single star row.
+constexpr int DF_FEW_CHUNK_MAX = 2048;
+constexpr int DF_FEW_CHUNK_MIN = 256;
+constexpr int DF_FEW_GRID_MIN = 304;
 
 struct DfFewArgs {
     GravArgs g;
@@ -896,6 +901,7 @@ struct DfFewArgs {
     double* partial;
     int rows;
     long long pitch;  // >= chunks of the longest row
+    int chunk;        // sources per CTA
 };
 
 template <bool SCREEN, int SMAX>
@@ -905,7 +911,7 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
     const Tile tile = g.tiles[blockIdx.y];
     if (g.sys_active && !g.sys_active[tile.sys]) return;
     const int nsrc = tile.src_end - tile.src_begin;
-    const int c0 = blockIdx.x * DF_FEW_CHUNK;
+    const int c0 = blockIdx.x * a.chunk;
     if (c0 >= nsrc) return;
     const int ns = tile.sink_end - tile.sink_begin;  // <= SMAX
     __shared__ SplitPos s_sink[SMAX];
@@ -934,7 +940,7 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
     for (int s = 0; s < SMAX; s++)
 #pragma unroll
         for (int c = 0; c < 3; c++) acc[s][c] = DF{0.0f, 0.0f};
-    const int c1 = min(nsrc, c0 + DF_FEW_CHUNK);
+    const int c1 = min(nsrc, c0 + a.chunk);
     for (int q = c0 + (int)threadIdx.x; q < c1; q += blockDim.x) {
         const int j = tile.src_begin + q;
         if (g.id[j] < 0) continue;
@@ -998,6 +1004,7 @@ struct DfFinalArgs {
     const int* row_sys;  // nullptr for one disk
     const int* sys_active;
     double *ax, *ay, *az;
+    int chunk;
 };
 
 // one thread per (row, component): the row's chunk sums in order
@@ -1007,7 +1014,7 @@ __global__ void df_few_final(DfFinalArgs a)
     if (k >= 3 * a.nrows) return;
     const int comp = k / a.nrows, row = a.row0 + k % a.nrows;
     if (a.sys_active && a.row_sys && !a.sys_active[a.row_sys[row]]) return;
-    const int nch = (a.row_nsrc[row] + DF_FEW_CHUNK - 1) / DF_FEW_CHUNK;
+    const int nch = (a.row_nsrc[row] + a.chunk - 1) / a.chunk;
     const double* P = a.partial + ((long long)comp * a.rows + row) * a.pitch;
     double s = 0.0;
     for (int c = 0; c < nch; c++) s += P[c];
@@ -1032,9 +1039,12 @@ int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row
 {
     if (g.n_tiles <= 0 || group_rows <= 0) return 0;
     if (max_sinks > FEW_SINKS_MAX) return set_error(RG_ERR_STATE, "few-sink tile wider than FEW_SINKS_MAX");
-    const int chunks = std::max(1, (max_src + DF_FEW_CHUNK - 1) / DF_FEW_CHUNK);
+    int chunk = DF_FEW_CHUNK_MAX;
+    while (chunk > DF_FEW_CHUNK_MIN && (long long)g.n_tiles * ((max_src + chunk - 1) / chunk) < DF_FEW_GRID_MIN)
+        chunk /= 2;
+    const int chunks = std::max(1, (max_src + chunk - 1) / chunk);
     if ((long long)chunks > pitch) return set_error(RG_ERR_STATE, "few-sink partial buffer too narrow");
-    DfFewArgs a{g, (const SplitPos*)split, tile_row0, partial, rows, pitch};
+    DfFewArgs a{g, (const SplitPos*)split, tile_row0, partial, rows, pitch, chunk};
     const dim3 grid(chunks, g.n_tiles);
     const bool screen = g.record || g.hill;
     if (max_sinks <= 4) {
@@ -1050,7 +1060,7 @@ int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row
     }
     RG_CUDA_CHECK(cudaGetLastError());
     DfFinalArgs f{partial, rows, group_row0, group_rows, pitch, row_sink, row_nsrc, row_sys, g.sys_active,
-                  g.ax, g.ay, g.az};
+                  g.ax, g.ay, g.az, chunk};
     df_few_final<<<(3 * group_rows + 127) / 128, 128, 0, st>>>(f);
     RG_CUDA_CHECK(cudaGetLastError());
     return 0;

@@ -69,6 +69,32 @@ def test_mixed_close_pairs_force_error(gpulib):
     assert mx < MAX_REL and rms < RMS_REL
 
 
+def test_mixed_planetesimal_events_from_the_heavy_rows(gpulib):
+    """Planetesimals (NSI) against the star and the giants in the double-float kernels (the
+    giants' rows in the few-sink kernel, the planetesimals' rows in the row kernel, each with
+    its block's event screens): planetesimals placed inside the giants' Hill spheres and two
+    overlapping a giant give the FP64 path's close-encounter and collision records over two
+    fixed steps."""
+    disk = bodies.config_disk("planetesimal_disk")
+    offsets = [(0.05 * k, 0.03, 0.01) for k in range(1, 9)] + [(3e-4, 0.0, 0.0), (0.0, -2e-4, 1e-4)]
+    for k, off in enumerate(offsets):
+        g = 1 + k % 2
+        for f, c in zip("xyz", off):
+            disk.r[f][3 + k] = disk.r[f][g] + c
+    thr = bodies.thresholds(collision_factor=1.0)
+    lists = {}
+    for mode in (T.GRAVITY_FP64, T.GRAVITY_MIXED):
+        s = lib.System(disk, thr)
+        s.set_gravity_mode(mode)
+        s.set_integrator(T.INT_RKF78, 0.01, False)
+        s.set_event_options(hill_factor=3.0)
+        s.advance(0.02)
+        lists[mode] = [(int(e["event_name"]), int(e["id1"]), int(e["id2"])) for e in s.events()]
+    kinds = {k for k, _, _ in lists[T.GRAVITY_FP64]}
+    assert {T.EVENT_CLOSE_ENCOUNTER, T.EVENT_COLLISION} <= kinds, lists[T.GRAVITY_FP64]
+    assert lists[T.GRAVITY_MIXED] == lists[T.GRAVITY_FP64]
+
+
 def test_mixed_fp64_reference_matches_oracle_rows(gpulib):
     """The FP64 accelerations used as the yardstick above are the oracle's."""
     disk = bodies.config_disk("self_gravitating", n=2048)
