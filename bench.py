@@ -449,6 +449,7 @@ def ensemble_section(args):
         e = Ensemble(disks, thr)
         e.set_integrator(0.001, tol)
         e.set_options(gravity_mode=mode, hill_factor=hill)
+        tune = None if args.no_autotune else e.autotune(2)  # tile shapes for these disks
         if proposer is not None:
             proposer.attach(e)
         e.advance(warm_day)
@@ -466,7 +467,7 @@ def ensemble_section(args):
         out = {"sim_years_per_s": sim_years / secs, "seconds": secs, "sim_years": sim_years, "attempts": tried,
                "rejected_frac": failed / max(tried, 1), "max_dE_over_E": dE, "events": int(len(ev)),
                "all_done": all(a["status"] == T.SYS_DONE for a in st),
-               "iterations": int(g1 - g0), "ms_per_iteration": 1e3 * secs / max(g1 - g0, 1)}
+               "iterations": int(g1 - g0), "ms_per_iteration": 1e3 * secs / max(g1 - g0, 1), "autotune": tune}
         if proposer is not None:
             out["proposed"] = sum(a["n_proposed"] for a in st)
             out["proposals_accepted"] = sum(a["n_proposal_accepted"] for a in st)

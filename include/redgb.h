@@ -290,6 +290,16 @@ RG_API int rg_ens_energy(rg_ens* ens, int sys, double* energy, double angmom[3])
 RG_API int rg_ens_get_stream(rg_ens* ens, void** stream);
 RG_API int rg_ens_kernel_count(rg_ens* ens, int64_t* n_kernels, int64_t* n_graph_launches);
 
+/* Tile-shape autotuner of the ensemble (no counterpart in the reference, which has one
+ * launch shape per kernel): times one gravity evaluation of every disk for each candidate
+ * shape of the current gravity mode (`reps` evaluations each, CUDA events on the ensemble's
+ * stream) and keeps the fastest.  FP64 mode: sinks per pair-parallel CTA x the row-kernel
+ * source limit -- every candidate sums in the reference's order, so results stay bit-exact;
+ * mixed mode: sources per few-sink CTA (0 = automatic, 512, 1024, 2048; reported in
+ * `mixed_chunks`) x the row-kernel limit.  The ensemble's state is not changed.  `out` (may be
+ * NULL) receives the choice. */
+RG_API int rg_ens_autotune(rg_ens* ens, int reps, rg_tune_t* out);
+
 /* ------------------------------------------------------------------ learned step proposer */
 
 /*

@@ -527,7 +527,7 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
                 rc = launch_grav_df_rowseq(g, c->d_split, c->st);
                 c->n_kernels++;
             } else {
-                rc = launch_grav_df_few(g, c->d_split, c->d_few_row0 + gr.off, gr.max_src, gr.max_sinks, c->d_terms,
+                rc = launch_grav_df_few(g, c->d_split, c->d_few_row0 + gr.off, gr.max_src, gr.max_sinks, 0, c->d_terms,
                                         c->few_rows,
                                         c->few_pitch, c->d_row_sink, c->d_row_nsrc, nullptr, gr.row_base, gr.rows,
                                         c->st);

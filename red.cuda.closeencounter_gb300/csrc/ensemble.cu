@@ -499,6 +499,9 @@ struct rg_ens {
     int n_sys = 0;
     int cap = 0;
     int device = 0, n_sm = 152;
+    // gravity launch shapes (rg_ens_autotune): row-kernel source limit, sinks per FP64
+    // pair-parallel CTA, sources per few-sink CTA (0: automatic)
+    int rowseq_max_src = 64, pairpar_S = 16, few_chunk = 0;
     std::vector<int> base, ntot;
     std::vector<std::array<int, 7>> cnt;
     std::vector<rg_param_t> p;
@@ -707,14 +710,14 @@ void build_gravity_plan(rg_ens* e)
         };
         for (const auto& k : blks) {
             if (k.s1 <= k.s0) continue;
-            if (k.src1 <= 64) {
+            if (k.src1 <= e->rowseq_max_src) {
                 add(0, GROUP_ROWSEQ, k.s0, k.s1, k.src1, k.block, 128);
                 add(1, GROUP_DF_ROWSEQ, k.s0, k.s1, k.src1, k.block, 128);
             } else if (k.s1 - k.s0 <= ENS_FEW_BLOCK) {
                 add(0, GROUP_FEW_SERIAL, k.s0, k.s1, k.src1, k.block, FEW_SINKS_MAX);
                 add(1, GROUP_DF_FEW, k.s0, k.s1, k.src1, k.block, FEW_SINKS_MAX);
             } else {
-                add(0, GROUP_PAIRPAR, k.s0, k.s1, k.src1, k.block, 16);
+                add(0, GROUP_PAIRPAR, k.s0, k.s1, k.src1, k.block, e->pairpar_S);  // S sinks per CTA and tile
                 const int light0 = k.block == 0 ? std::max(k.s0, std::min(n_heavy, k.s1)) : k.s0;
                 add(1, GROUP_DF_FEW, k.s0, light0, k.src1, k.block, FEW_SINKS_MAX);
                 add(1, GROUP_MIXED, light0, k.s1, k.src1, k.block, MIXED_SINKS_PER_TILE);
@@ -854,7 +857,7 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
         g.tiles = e->d_tiles + gr.off;
         g.n_tiles = gr.n;
         switch (gr.kind) {
-        case GROUP_PAIRPAR: rc = launch_grav_fp64_pairpar(g, 16, e->st); e->n_kernels++; break;
+        case GROUP_PAIRPAR: rc = launch_grav_fp64_pairpar(g, e->pairpar_S, e->st); e->n_kernels++; break;
         case GROUP_ROWSEQ: rc = launch_grav_fp64_rowseq(g, e->st); e->n_kernels++; break;
         case GROUP_FEW_SERIAL:
         case GROUP_FEW_TREE:
@@ -877,7 +880,8 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
                 rc = launch_grav_df_rowseq(g, e->d_split, e->st);
                 e->n_kernels++;
             } else {
-                rc = launch_grav_df_few(g, e->d_split, e->d_few_row0 + gr.off, gr.max_src, gr.max_sinks, e->d_terms,
+                rc = launch_grav_df_few(g, e->d_split, e->d_few_row0 + gr.off, gr.max_src, gr.max_sinks, e->few_chunk,
+                                        e->d_terms,
                                         e->few_rows,
                                         e->few_pitch, e->d_row_sink, e->d_row_nsrc, e->d_row_sys, gr.row_base, gr.rows,
                                         e->st);
@@ -1922,6 +1926,98 @@ int rg_ens_get_stream(rg_ens* e, void** stream)
     if (!e || !stream) return set_error(RG_ERR_ARG, "bad argument");
     *stream = (void*)e->st;
     return RG_OK;
+}
+
+// CUDA-event time of one gravity evaluation of every disk (stage-0 form, no event records)
+// on the step-start state, written to a stage buffer; `reps` evaluations after a warm-up
+static int time_ens_evaluations(rg_ens* e, int reps, double* ms)
+{
+    const size_t cap = (size_t)e->cap;
+    double* acc = e->d_k[0] + 3 * cap;
+    int rc = ens_gravity(e, e->d_y, e->d_y + 3 * cap, acc, 0, nullptr, false);
+    if (rc) return rc;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    RG_CUDA_CHECK(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return set_error(RG_ERR_CUDA, "cudaEventCreate");
+    }
+    cudaEventRecord(e0, e->st);
+    for (int k = 0; k < reps && !rc; k++) rc = ens_gravity(e, e->d_y, e->d_y + 3 * cap, acc, 0, nullptr, false);
+    cudaEventRecord(e1, e->st);
+    cudaError_t err = cudaEventSynchronize(e1);
+    float t = 0.0f;
+    if (!rc && err == cudaSuccess) err = cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (err != cudaSuccess) return set_error(RG_ERR_CUDA, "autotune timing");
+    *ms = t / std::max(1, reps);
+    return RG_OK;
+}
+
+// the ensemble's tile shapes, timed on its own disks: FP64 mode sinks per pair-parallel CTA x
+// the row-kernel source limit (each candidate sums in the reference's order: results stay
+// bit-exact), mixed mode sources per few-sink CTA x the row-kernel limit
+static int ens_autotune_impl(rg_ens* e, int reps, rg_tune_t* out)
+{
+    struct Shape {
+        int S, rowseq, chunk;
+    };
+    std::vector<Shape> cand;
+    const int rows[3] = {32, 64, 128};
+    if (e->gravity_mode == RG_GRAVITY_MIXED) {
+        const int ch[4] = {0, 512, 1024, 2048};
+        for (int r : rows)
+            for (int k : ch) cand.push_back({e->pairpar_S, r, k});
+    } else {
+        const int ss[3] = {8, 16, 32};
+        for (int r : rows)
+            for (int S : ss) cand.push_back({S, r, e->few_chunk});
+    }
+    const int64_t kernels = e->n_kernels;
+    const Shape before{e->pairpar_S, e->rowseq_max_src, e->few_chunk};
+    double ms_before = 0.0;
+    int rc = time_ens_evaluations(e, reps, &ms_before);
+    Shape best = before;
+    double best_ms = ms_before;
+    for (const Shape& sh : cand) {
+        if (rc) break;
+        e->pairpar_S = sh.S;
+        e->rowseq_max_src = sh.rowseq;
+        e->few_chunk = sh.chunk;
+        build_gravity_plan(e);
+        rc = upload_plans(e);
+        double ms = 0.0;
+        if (!rc) rc = time_ens_evaluations(e, reps, &ms);
+        if (!rc && ms < best_ms) {
+            best_ms = ms;
+            best = sh;
+        }
+    }
+    e->pairpar_S = best.S;
+    e->rowseq_max_src = best.rowseq;
+    e->few_chunk = best.chunk;
+    build_gravity_plan(e);
+    const int rc2 = upload_plans(e);
+    if (!rc) rc = rc2;
+    e->n_kernels = kernels;
+    if (rc) return rc;
+    if (out) {
+        out->pairpar_sinks = best.S;
+        out->rowseq_max_src = best.rowseq;
+        out->mixed_chunks = best.chunk;
+        out->candidates = (int32_t)cand.size();
+        out->ms_per_eval = best_ms;
+        out->ms_before = ms_before;
+    }
+    return RG_OK;
+}
+
+int rg_ens_autotune(rg_ens* e, int reps, rg_tune_t* out)
+{
+    if (!e || reps < 1) return set_error(RG_ERR_ARG, "bad argument");
+    RG_GUARD(ens_autotune_impl(e, reps, out));
 }
 
 int rg_ens_kernel_count(rg_ens* e, int64_t* n_kernels, int64_t* n_graph_launches)

@@ -1034,14 +1034,17 @@ int launch_grav_df_rowseq(const GravArgs& g, const void* split, cudaStream_t st)
 }
 
 int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row0, int max_src, int max_sinks,
-                       double* partial, int rows, long long pitch, const int* row_sink, const int* row_nsrc,
-                       const int* row_sys, int group_row0, int group_rows, cudaStream_t st)
+                       int chunk_hint, double* partial, int rows, long long pitch, const int* row_sink,
+                       const int* row_nsrc, const int* row_sys, int group_row0, int group_rows, cudaStream_t st)
 {
     if (g.n_tiles <= 0 || group_rows <= 0) return 0;
     if (max_sinks > FEW_SINKS_MAX) return set_error(RG_ERR_STATE, "few-sink tile wider than FEW_SINKS_MAX");
     int chunk = DF_FEW_CHUNK_MAX;
-    while (chunk > DF_FEW_CHUNK_MIN && (long long)g.n_tiles * ((max_src + chunk - 1) / chunk) < DF_FEW_GRID_MIN)
-        chunk /= 2;
+    if (chunk_hint > 0)  // a tuned chunk: a multiple of the CTA's 256 threads
+        chunk = std::max(DF_FEW_CHUNK_MIN, std::min(DF_FEW_CHUNK_MAX, chunk_hint / 256 * 256));
+    else
+        while (chunk > DF_FEW_CHUNK_MIN && (long long)g.n_tiles * ((max_src + chunk - 1) / chunk) < DF_FEW_GRID_MIN)
+            chunk /= 2;
     const int chunks = std::max(1, (max_src + chunk - 1) / chunk);
     if ((long long)chunks > pitch) return set_error(RG_ERR_STATE, "few-sink partial buffer too narrow");
     DfFewArgs a{g, (const SplitPos*)split, tile_row0, partial, rows, pitch, chunk};

@@ -93,7 +93,9 @@ int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* hea
 // the row kernel for blocks with a few massive sources, the few-sink kernel for the
 // star's and giants' own rows (partial: 3 x rows x pitch doubles, pitch >= source chunks)
 int launch_grav_df_rowseq(const GravArgs& g, const void* split, cudaStream_t st);
+// chunk_hint: sources per CTA (multiple of 256, 256..2048), or 0 for the automatic choice
 int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row0, int max_src, int max_sinks,
+                       int chunk_hint,
                        double* partial, int rows, long long pitch, const int* row_sink, const int* row_nsrc,
                        const int* row_sys, int group_row0, int group_rows, cudaStream_t st);
 int launch_star_distance(const double* x, const double* y, const double* z, const int* base_of, int n, double* rho,

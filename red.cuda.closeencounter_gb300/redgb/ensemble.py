@@ -28,6 +28,7 @@ def _bind(L):
         "rg_ens_energy": [vp, ci, ctypes.POINTER(cd), vp],
         "rg_ens_get_stream": [vp, ctypes.POINTER(vp)],
         "rg_ens_kernel_count": [vp, ctypes.POINTER(i64), ctypes.POINTER(i64)],
+        "rg_ens_autotune": [vp, ci, ctypes.POINTER(T.Tune)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -124,6 +125,14 @@ class Ensemble:
         p = ctypes.c_void_p()
         self._call("rg_ens_get_stream", self.handle, ctypes.byref(p))
         return p.value
+
+    def autotune(self, reps=3):
+        """Time the candidate tile shapes of the current gravity mode on these disks and keep
+        the fastest (rg_ens_autotune); returns the choice (`mixed_chunks`: sources per
+        few-sink CTA, 0 = automatic)."""
+        t = T.Tune()
+        self._call("rg_ens_autotune", self.handle, int(reps), ctypes.byref(t))
+        return {f: getattr(t, f) for f, _ in t._fields_}
 
     def kernel_count(self):
         a, b = ctypes.c_int64(), ctypes.c_int64()

@@ -51,6 +51,31 @@ def test_ensemble_replay_bit_exact(gpulib, use_graph):
         assert ens.stats(s)["status"] == T.SYS_DONE
 
 
+def test_ensemble_autotune(gpulib):
+    """rg_ens_autotune: FP64 shapes keep the bit-exact replay; mixed shapes keep the energy."""
+    disks = [bodies.make_disk(n_pl=150 + 90 * k, seed=60 + k) for k in range(3)]
+    disks.append(bodies.make_disk(n_pl=200, pl_type=T.BODY_PROTOPLANET, seed=63, m_range=(1e-9, 1e-7), giants=()))
+    thr = bodies.thresholds(collision_factor=0.0)
+    ens = Ensemble(disks, thr)
+    ens.set_integrator(0.001, 1e-10)
+    t = ens.autotune(reps=2)
+    assert t["candidates"] == 9 and t["pairpar_sinks"] in (8, 16, 32) and t["rowseq_max_src"] in (32, 64, 128)
+    assert t["ms_per_eval"] <= t["ms_before"] * 1.001
+    ens.set_step_log(1 << 16)
+    ens.advance(20.0, max_attempts=4000)  # bounded: a wrong shape would collapse the steps
+    _replay_check(ens, disks, thr, ens.step_log())
+    mixed = Ensemble(disks, thr)
+    mixed.set_integrator(0.001, 1e-10)
+    mixed.set_options(gravity_mode=T.GRAVITY_MIXED, hill_factor=3.0)
+    t = mixed.autotune(reps=2)
+    assert t["candidates"] == 12 and t["mixed_chunks"] in (0, 512, 1024, 2048)
+    E0 = [mixed.energy(s)[0] for s in range(len(disks))]
+    mixed.advance(60.0, max_attempts=4000)
+    for s in range(len(disks)):
+        assert abs((mixed.energy(s)[0] - E0[s]) / E0[s]) < 1e-10
+        assert mixed.stats(s)["status"] == T.SYS_DONE
+
+
 def test_ensemble_collisions_match_oracle(gpulib):
     """The reference's collision-merge run as a one-disk ensemble next to a second disk:
     merges, their event records and the resulting states match the oracle."""
