@@ -393,15 +393,31 @@ def dense_ring_section(args):
     }
 
 
-def _compare_events(a, b):
-    """Two event lists of (disk, type, id1, id2): identical, or how many records differ.
-    Over a long interval the trajectories of two precisions part chaotically near the
-    giants, so grazing close encounters may be recorded in one run and not the other;
-    every decision on a given state is taken in FP64 by both."""
-    from collections import Counter
-    ca, cb = Counter(a), Counter(b)
-    return {"identical": a == b, "n": len(a), "n_fp64": len(b),
-            "only_here": sum((ca - cb).values()), "only_fp64": sum((cb - ca).values())}
+def _compare_events(a, b, n_disks):
+    """Two event lists of (disk, type, id1, id2, t_day): identical, or how many records
+    differ, how many disks' lists are identical, and the earliest simulated time of a record
+    found in one list only.  Over a long interval the trajectories of two precisions part
+    chaotically near the giants, so grazing close encounters may be recorded in one run and
+    not the other; every decision on a given state is taken in FP64 by both."""
+    from collections import Counter, defaultdict
+    ka, kb = [x[:4] for x in a], [x[:4] for x in b]
+    ca, cb = Counter(ka), Counter(kb)
+    only = (ca - cb) + (cb - ca)
+    ta, tb = defaultdict(list), defaultdict(list)
+    for x in a:
+        ta[x[:4]].append(x[4])
+    for x in b:
+        tb[x[:4]].append(x[4])
+    first = None
+    for k in only:  # the first record of a pair beyond the count both lists share
+        u, w = sorted(ta[k]), sorted(tb[k])
+        t = (u if len(u) > len(w) else w)[min(len(u), len(w))]
+        first = t if first is None else min(first, t)
+    differing = {k[0] for k in only}
+    return {"identical": ka == kb, "n": len(a), "n_fp64": len(b),
+            "only_here": sum((ca - cb).values()), "only_fp64": sum((cb - ca).values()),
+            "disks_identical": n_disks - len(differing), "disks": n_disks,
+            "first_difference_yr": None if first is None else first / T.YEAR}
 
 
 def ensemble_section(args):
@@ -473,7 +489,8 @@ def ensemble_section(args):
             out["proposed"] = sum(a["n_proposed"] for a in st)
             out["proposals_accepted"] = sum(a["n_proposal_accepted"] for a in st)
             out["fallbacks"] = sum(a["n_fallback"] for a in st)
-        keys = sorted((int(k), int(r["event_name"]), int(r["id1"]), int(r["id2"])) for r, k in zip(ev, sysv))
+        keys = sorted((int(k), int(r["event_name"]), int(r["id1"]), int(r["id2"]), float(r["t"]) / T.GAUSS)
+                      for r, k in zip(ev, sysv))
         e.close()
         return out, keys
 
@@ -518,8 +535,8 @@ def ensemble_section(args):
         "speedup_vs_plain_fp64_sequential": learned["sim_years_per_s"] / sequential["sim_years_per_s"],
         "speedup_vs_plain_fp64_batched": learned["sim_years_per_s"] / plain_fp64["sim_years_per_s"],
         "learned_vs_plain_attempts": plain_mixed["attempts"] / max(learned["attempts"], 1),
-        "event_lists": {name: _compare_events(ev, ev_f) for name, ev in (("learned_vs_fp64", ev_l),
-                                                                         ("mixed_vs_fp64", ev_m))},
+        "event_lists": {name: _compare_events(ev, ev_f, len(disks)) for name, ev in (("learned_vs_fp64", ev_l),
+                                                                                     ("mixed_vs_fp64", ev_m))},
         "proposer": {"train_records": int(len(x)), "train_disks": "seeds 1-64, dither 0.15",
                      "train_years": args.train_years, "loss": loss, "drift_std": float(np.std(y)),
                      "residual_std": net.residual_std, "safety": net.safety, "setup_seconds": train_s},

@@ -311,10 +311,9 @@ enum {
     GROUP_PAIRPAR = 0,
     GROUP_ROWSEQ = 1,
     GROUP_FEW_SERIAL = 2,
-    GROUP_FEW_TREE = 3,
-    GROUP_MIXED = 4,
-    GROUP_DF_ROWSEQ = 5,  // mixed mode: the row kernel in double-float arithmetic
-    GROUP_DF_FEW = 6,     // mixed mode: few heavy sinks in double-float arithmetic
+    GROUP_MIXED = 3,
+    GROUP_DF_ROWSEQ = 4,  // mixed mode: the row kernel in double-float arithmetic
+    GROUP_DF_FEW = 5,     // mixed mode: few heavy sinks in double-float arithmetic
 };
 constexpr int FEW_BLOCK_SINKS = 32;  // blocks with at most this many sinks use the few-sink path
 
@@ -346,7 +345,7 @@ void build_tiles(rg_ctx* c)
         for (int s = s0; s < s1; s += step) {
             c->tiles.push_back(Tile{s, std::min(s + step, s1), 0, src1, 0, 0, block, 0});
             c->heavy_mx.push_back(kind == GROUP_MIXED ? std::min(n_heavy, src1) : 0);
-            if (kind == GROUP_FEW_SERIAL || kind == GROUP_FEW_TREE || kind == GROUP_DF_FEW) {
+            if (kind == GROUP_FEW_SERIAL || kind == GROUP_DF_FEW) {
                 c->few_row0.push_back(c->few_rows);
                 c->few_nsrc.push_back(src1);
                 for (int i = s; i < std::min(s + step, s1); i++) {
@@ -507,10 +506,8 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
             c->n_kernels++;
             break;
         case GROUP_FEW_SERIAL:
-        case GROUP_FEW_TREE:
             rc = launch_grav_fp64_few(g, c->d_few_row0 + gr.off, gr.max_src, c->d_terms, c->few_rows, c->few_pitch,
-                                      c->d_row_sink, c->d_row_nsrc, nullptr, gr.row_base, gr.rows,
-                                      gr.kind == GROUP_FEW_SERIAL, c->st);
+                                      c->d_row_sink, c->d_row_nsrc, nullptr, gr.row_base, gr.rows, c->st);
             c->n_kernels += 2;
             break;
         case GROUP_DF_ROWSEQ:

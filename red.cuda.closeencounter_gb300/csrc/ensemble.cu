@@ -616,17 +616,16 @@ constexpr double GAUSS = 1.720209895e-2;
 constexpr double GAUSS2 = 2.959122082855911025e-4;
 constexpr int STAGE_TILE = 2048;
 constexpr int ENS_FEW_BLOCK = 32;
-// the FP64 plan uses the first four kinds; the mixed-precision plan uses DF_ROWSEQ, DF_FEW
-// (double-float heavy pairs) and MIXED
+// the FP64 plan uses the first three kinds; the mixed-precision plan uses MIXED, DF_ROWSEQ
+// and DF_FEW (double-float heavy pairs)
 enum {
     GROUP_PAIRPAR = 0,
     GROUP_ROWSEQ = 1,
     GROUP_FEW_SERIAL = 2,
-    GROUP_FEW_TREE = 3,
-    GROUP_MIXED = 4,
-    GROUP_DF_ROWSEQ = 5,
-    GROUP_DF_FEW = 6,
-    GROUP_KINDS = 7
+    GROUP_MIXED = 3,
+    GROUP_DF_ROWSEQ = 4,
+    GROUP_DF_FEW = 5,
+    GROUP_KINDS = 6
 };
 
 template <class T>
@@ -733,7 +732,7 @@ void build_gravity_plan(rg_ens* e)
             for (size_t k = 0; k < T.size(); k++) {
                 e->tiles.push_back(T[k]);
                 e->heavy.push_back(hv[mode][kind][k]);
-                if (kind == GROUP_FEW_SERIAL || kind == GROUP_FEW_TREE || kind == GROUP_DF_FEW) {
+                if (kind == GROUP_FEW_SERIAL || kind == GROUP_DF_FEW) {
                     e->few_row0.push_back(e->few_rows);
                     const int nsrc = T[k].src_end - T[k].src_begin;
                     for (int i = T[k].sink_begin; i < T[k].sink_end; i++) {
@@ -860,10 +859,8 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
         case GROUP_PAIRPAR: rc = launch_grav_fp64_pairpar(g, e->pairpar_S, e->st); e->n_kernels++; break;
         case GROUP_ROWSEQ: rc = launch_grav_fp64_rowseq(g, e->st); e->n_kernels++; break;
         case GROUP_FEW_SERIAL:
-        case GROUP_FEW_TREE:
             rc = launch_grav_fp64_few(g, e->d_few_row0 + gr.off, gr.max_src, e->d_terms, e->few_rows, e->few_pitch,
-                                      e->d_row_sink, e->d_row_nsrc, e->d_row_sys, gr.row_base, gr.rows,
-                                      gr.kind == GROUP_FEW_SERIAL, e->st);
+                                      e->d_row_sink, e->d_row_nsrc, e->d_row_sys, gr.row_base, gr.rows, e->st);
             e->n_kernels += 2;
             break;
         case GROUP_DF_ROWSEQ:
@@ -897,12 +894,10 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
                 e->n_kernels++;
             }
             if (!rc) {
-                const int src = std::max(1, (int)(e->pairs_per_eval / std::max(1, e->cap)));
-                int chunks = std::max(1, std::min((4 * e->n_sm + gr.n - 1) / gr.n, src / (4 * MIXED_SOURCE_TILE)));
-                chunks = 1;  // per-disk source counts differ; one chunk keeps the partial buffer simple
-                (void)src;
-                rc = launch_grav_mixed_tiles(g, e->d_split, e->d_heavy + gr.off, e->near_ratio, chunks,
-                                             MIXED_SOURCE_TILE, nullptr, e->cap, e->d_kerr, e->st);
+                // one source chunk: the disks' source counts differ, so a chunked split would
+                // need a partial buffer per disk
+                rc = launch_grav_mixed_tiles(g, e->d_split, e->d_heavy + gr.off, e->near_ratio, 1, MIXED_SOURCE_TILE,
+                                             nullptr, e->cap, e->d_kerr, e->st);
                 e->n_kernels++;
             }
             break;

@@ -321,31 +321,6 @@ __global__ void __launch_bounds__(128) few_sum_serial(FewSumArgs a)
     }
 }
 
-// mixed-precision heavy rows: one CTA per (row, component), compensated tree reduction
-__global__ void __launch_bounds__(256) few_sum_tree(FewSumArgs a)
-{
-    const int comp = blockIdx.x / a.nrows, row = a.row0 + blockIdx.x % a.nrows;
-    if (a.sys_active && !a.sys_active[a.row_sys[row]]) return;
-    const double* T = a.terms + ((long long)comp * a.rows + row) * a.pitch;
-    const int n = a.row_nsrc[row];
-    double s = 0.0, c = 0.0;
-    for (int q = threadIdx.x; q < n; q += blockDim.x) {
-        const double x = T[q];
-        const double t = s + x;
-        c += fabs(s) >= fabs(x) ? (s - t) + x : (x - t) + s;
-        s = t;
-    }
-    s += c;
-    __shared__ double red[256];
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) (comp == 0 ? a.ax : (comp == 1 ? a.ay : a.az))[a.row_sink[row]] = red[0];
-}
-
 // ---------------------------------------------------------------------------------------
 // Host launchers
 int launch_grav_fp64_pairpar(const GravArgs& g, int S, cudaStream_t st)
@@ -369,14 +344,13 @@ int launch_grav_fp64_rowseq(const GravArgs& g, cudaStream_t st)
     return 0;
 }
 
-// Few-sink tiles (at most FEW_MAX sinks each) -> terms -> row sums.  `tiles` holds
-// n_tiles tiles, rows are numbered tile by tile; host arrays row_sink/row_nsrc are on the
-// device already (dev_row_sink, dev_row_nsrc).
-// Few-sink tiles -> terms -> row sums, one launch each for all tiles of the group.
-// tile_row0 (device) gives each tile's first row; max_src bounds the tiles' source counts.
+// Few-sink tiles (at most FEW_MAX sinks each) -> terms -> exact serial row sums, one launch
+// each for all tiles of the group.  Rows are numbered tile by tile; tile_row0 (device) gives
+// each tile's first row, max_src bounds the tiles' source counts, and the row arrays
+// (dev_row_sink, dev_row_nsrc, dev_row_sys) are on the device.
 int launch_grav_fp64_few(const GravArgs& g, const int* tile_row0, int max_src, double* terms, int rows,
                          long long pitch, const int* dev_row_sink, const int* dev_row_nsrc, const int* dev_row_sys,
-                         int group_row0, int group_rows, bool serial, cudaStream_t st)
+                         int group_row0, int group_rows, cudaStream_t st)
 {
     if (g.n_tiles <= 0 || rows <= 0 || group_rows <= 0 || max_src <= 0) return 0;
     FewArgs a{g, tile_row0, terms, rows, pitch};
@@ -384,10 +358,7 @@ int launch_grav_fp64_few(const GravArgs& g, const int* tile_row0, int max_src, d
     RG_CUDA_CHECK(cudaGetLastError());
     FewSumArgs b{terms, rows, group_row0, group_rows, pitch, dev_row_sink, dev_row_nsrc, dev_row_sys, g.sys_active,
                  g.ax, g.ay, g.az};
-    if (serial)
-        few_sum_serial<<<(3 * group_rows + 3) / 4, 128, 0, st>>>(b);
-    else
-        few_sum_tree<<<3 * group_rows, 256, 0, st>>>(b);
+    few_sum_serial<<<(3 * group_rows + 3) / 4, 128, 0, st>>>(b);
     RG_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

@@ -76,7 +76,7 @@ int launch_grav_fp64_rowseq(const GravArgs& g, cudaStream_t st);
 constexpr int FEW_SINKS_MAX = 8;  // sinks per few-sink tile
 int launch_grav_fp64_few(const GravArgs& g, const int* tile_row0, int max_src, double* terms, int rows,
                          long long pitch, const int* dev_row_sink, const int* dev_row_nsrc, const int* dev_row_sys,
-                         int group_row0, int group_rows, bool serial, cudaStream_t st);
+                         int group_row0, int group_rows, cudaStream_t st);
 // mixed precision (gravity_mixed.cu): positions split into FP32 (hi, lo) once per evaluation
 struct SplitPos;
 constexpr int MIXED_SINKS_PER_TILE = 128;
