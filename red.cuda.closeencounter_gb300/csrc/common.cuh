@@ -32,6 +32,7 @@ struct DevEvent {
     int32_t i, j;   // sink, source (body indices of the whole batch)
     int32_t sys, pad;
     double d;
+    double t;  // ensembles: the system's time at the attempt's start (the Hill records' time)
     double ri[3], vi[3], rj[3], vj[3], r0[3], v0[3];
 };
 
@@ -77,6 +78,7 @@ struct GravArgs {
     unsigned int* sys_events;
     const unsigned int* sys_attempt;
     const unsigned int* sys_f0;
+    const double* sys_t;  // per system: the time at the attempt's start
 };
 
 // sequence tag of a record: (attempt << 8) | stage, or the step-start number for Hill

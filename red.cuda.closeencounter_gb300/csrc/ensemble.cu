@@ -835,6 +835,7 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
     g.sys_events = e->d_sys_events;
     g.sys_attempt = e->d_attempt;
     g.sys_f0 = e->d_nf0;
+    g.sys_t = e->d_t;
     int rc = RG_OK;
     if (hill) {
         // distance from each disk's body 0 (the per-body base is the tile's base: use a
@@ -1225,6 +1226,7 @@ void handle_hill(rg_ens* e, std::vector<DevEvent>& recs, const std::vector<unsig
             if (!seen) {
                 rg_event_t x = zero_event();
                 x.event_name = RG_EVENT_CLOSE_ENCOUNTER;
+                x.t = d.t;  // the step start, where the pair was found inside the sphere
                 x.d = d.d;
                 x.id1 = e->md[d.i].id;
                 x.id2 = e->md[d.j].id;

@@ -240,6 +240,7 @@ __device__ __forceinline__ void exact_event_tests(const GravArgs& g, const Tile&
             e->sys = tile.sys;
             e->pad = 0;
             e->d = d;
+            e->t = g.sys_t ? g.sys_t[tile.sys] : 0.0;
             const int b0 = tile.base;
             e->ri[0] = xi; e->ri[1] = yi; e->ri[2] = zi;
             e->rj[0] = xj; e->rj[1] = yj; e->rj[2] = zj;

@@ -126,6 +126,28 @@ def test_ensemble_mixed_and_energy(gpulib):
     assert n_g > 0 and n_k > n_g
 
 
+def test_ensemble_close_encounter_times(gpulib):
+    """A close-encounter record carries the step start at which the pair was found inside the
+    Hill sphere (a wide sphere, 10 mutual Hill radii, so that pairs enter it within 60 days)."""
+    disks = [bodies.config_disk("ensemble_member", seed=s, n=600) for s in (4, 5)]
+    ens = Ensemble(disks, bodies.thresholds(collision_factor=0.0))
+    ens.set_integrator(0.001, 1e-10)
+    ens.set_options(gravity_mode=T.GRAVITY_MIXED, hill_factor=10.0)
+    ens.set_step_log(1 << 18)
+    ens.advance(60.0, max_attempts=20000)
+    ev, sysv = ens.events()
+    log = ens.step_log()
+    later = 0
+    for s in range(len(disks)):
+        mine = log[(log["sys"] == s) & (log["accepted"] == 1)]
+        starts = np.concatenate([[0.0], np.cumsum(mine["dt"])])  # internal units
+        for r, k in zip(ev, sysv):
+            if k == s and r["event_name"] == T.EVENT_CLOSE_ENCOUNTER:
+                assert np.min(np.abs(starts - r["t"])) <= 1e-12 * max(1.0, starts[-1]), (s, r["t"])
+                later += r["t"] > 0.0
+    assert later > 0
+
+
 def test_ensemble_mixed_screen_cutoffs_keep_every_event(gpulib):
     """Three crowded disks (3000 protoplanets with radii x 300 and a giant; Hill factor 3:
     about 20 overlapping and 50 Hill pairs each at the start).  The mixed kernels skip the
