@@ -95,6 +95,41 @@ def test_mixed_planetesimal_events_from_the_heavy_rows(gpulib):
     assert lists[T.GRAVITY_MIXED] == lists[T.GRAVITY_FP64]
 
 
+@pytest.mark.parametrize("case", ["star_only", "star_and_one_planet", "test_particles", "inactive_and_massless",
+                                  "large_protoplanet_block"])
+def test_mixed_edge_cases(gpulib, case):
+    """Small and ragged inputs through the mixed plan: one body, one pair, test particles (NI
+    block), inactive and massless bodies, and an SI block large enough for the mixed kernel
+    with test particles behind it.  Inactive bodies feel nothing; everything else within the
+    force-error bound of the FP64 path."""
+    if case == "star_only":
+        disk = bodies.make_disk(n_pl=0, seed=1, giants=())
+    elif case == "star_and_one_planet":
+        disk = bodies.make_disk(n_pl=0, seed=1, giants=((9.55e-4, 5.2, 0.05),))
+    elif case == "test_particles":
+        disk = bodies.make_disk(n_pl=300, seed=2, n_tp=57)
+    elif case == "inactive_and_massless":
+        disk = bodies.make_disk(n_pl=400, pl_type=T.BODY_PROTOPLANET, seed=5, n_tp=9, m_range=(1e-9, 1e-7))
+        disk.md["id"][[5, 17, 40, 300]] *= -1
+        disk.p["mass"][[7, 8, 301]] = 0.0
+    else:
+        disk = bodies.make_disk(n_pl=2500, pl_type=T.BODY_PROTOPLANET, seed=6, n_tp=33, m_range=(1e-9, 1e-7))
+    g = lib.System(disk, bodies.thresholds())
+    ae = g.calc_accel()
+    g.set_gravity_mode(T.GRAVITY_MIXED)
+    am = g.calc_accel()
+    a_m = np.stack([am[f] for f in "xyz"], 1)
+    a_e = np.stack([ae[f] for f in "xyz"], 1)
+    inactive = disk.md["id"] <= 0
+    assert np.all(a_m[inactive] == 0.0) and np.all(a_e[inactive] == 0.0)
+    norm = np.linalg.norm(a_e, axis=1)
+    ok = norm > 0
+    assert np.array_equal(np.linalg.norm(a_m, axis=1) > 0, ok)
+    if ok.any():
+        rel = np.linalg.norm(a_m - a_e, axis=1)[ok] / norm[ok]
+        assert rel.max() < MAX_REL, (case, rel.max())
+
+
 def test_mixed_fp64_reference_matches_oracle_rows(gpulib):
     """The FP64 accelerations used as the yardstick above are the oracle's."""
     disk = bodies.config_disk("self_gravitating", n=2048)
