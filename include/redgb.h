@@ -201,6 +201,13 @@ RG_API int rg_calc_accel(rg_ctx* ctx, rg_vec_t* a);
  */
 RG_API int rg_autotune(rg_ctx* ctx, int reps, rg_tune_t* out);
 
+/* Test hook for the failure path (no counterpart in the reference): with `on`, the mixed
+ * kernel issues none of its tile copies, so each CTA's bounded wait (one second of the GPU's
+ * global timer) runs out; the evaluation then reports RG_ERR_CUDA ("a gravity tile copy did
+ * not arrive within the wait limit") and the context stays usable.  Nothing faults: the
+ * kernel waits on its own barriers, stops waiting and returns. */
+RG_API int rg_test_hold_tile_copies(rg_ctx* ctx, int on);
+
 /* Integrator and event counters (integrator.cu:258-278, pp_disk.h:129-133). */
 RG_API int rg_get_counters(rg_ctx* ctx, rg_counters_t* c);
 

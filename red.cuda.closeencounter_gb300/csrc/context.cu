@@ -95,6 +95,7 @@ struct rg_ctx {
     int rowseq_max_src = 64;
     int mixed_chunks = 0;  // source chunks of the mixed kernel (0: from the SM count)
     float near_ratio = 1.0e-5f;
+    int hold_tile_copies = 0;  // test hook (rg_test_hold_tile_copies)
     // integrator
     int has_int = 0, int_type = 0, adaptive = 0, ectp = 0, r_max = 0, order = 0;
     double dt_try = 0.0, dt_did = 0.0, tol = 0.0;
@@ -557,7 +558,7 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
                 }
                 if (!rc)
                     rc = launch_grav_mixed_tiles(g, c->d_split, c->d_heavy + gr.off, c->near_ratio, chunks, chunk,
-                                                 c->d_partial, c->cap, c->d_kerr, c->st);
+                                                 c->d_partial, c->cap, c->d_kerr, c->hold_tile_copies != 0, c->st);
                 c->n_kernels += chunks > 1;
             }
             c->n_kernels++;
@@ -1699,6 +1700,13 @@ int rg_calc_accel(rg_ctx* c, rg_vec_t* a)
 {
     if (!c || !a) return set_error(RG_ERR_ARG, "bad argument");
     RG_GUARD(calc_accel_impl(c, a));
+}
+
+int rg_test_hold_tile_copies(rg_ctx* c, int on)
+{
+    if (!c) return set_error(RG_ERR_ARG, "null context");
+    c->hold_tile_copies = on ? 1 : 0;
+    return RG_OK;
 }
 
 int rg_autotune(rg_ctx* c, int reps, rg_tune_t* out)

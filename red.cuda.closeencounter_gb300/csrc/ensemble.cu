@@ -898,7 +898,7 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
                 // one source chunk: the disks' source counts differ, so a chunked split would
                 // need a partial buffer per disk
                 rc = launch_grav_mixed_tiles(g, e->d_split, e->d_heavy + gr.off, e->near_ratio, 1, MIXED_SOURCE_TILE,
-                                             nullptr, e->cap, e->d_kerr, e->st);
+                                             nullptr, e->cap, e->d_kerr, false, e->st);
                 e->n_kernels++;
             }
             break;

@@ -198,6 +198,7 @@ struct MixedArgs {
     double* partial;       // n_chunks x 3 x n_part doubles, or nullptr when grid.y == 1
     int n_part;            // row length of `partial`
     unsigned int* err;     // set to 1 when a tile copy did not arrive within the wait limit
+    int hold;              // test hook: issue no tile copies (the waits run out)
 };
 
 constexpr int MX_WARPS = 8;
@@ -536,9 +537,12 @@ __device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile
 // 8 KB copy of MX_T split positions), double-buffered: tile t + 2 is requested while tile t
 // is computed, each buffer's arrival is signalled on its own mbarrier (transaction bytes),
 // and one CTA barrier per tile releases the buffer for reuse.  Every wait on a copy is
-// bounded (MX_WAIT_POLLS polls); a CTA whose copy does not arrive sets a.err, waits (again
-// bounded) for the copies it issued, and returns.
-constexpr unsigned MX_WAIT_POLLS = 1u << 24;
+// bounded, by MX_WAIT_NS of the GPU's global timer (and, should the timer not advance, by
+// MX_WAIT_POLLS polls); a CTA whose copy does not arrive sets a.err, waits (again bounded)
+// for the copies it issued, and returns.  `a.hold` (a test hook) issues no copies, so that
+// the waits run out and the host sees the error status.
+constexpr unsigned long long MX_WAIT_NS = 1000000000ull;  // one second
+constexpr unsigned MX_WAIT_POLLS = 1u << 28;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -560,10 +564,20 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned 
     return ok != 0;
 }
 
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned phase)
 {
-    for (unsigned k = 0; k < MX_WAIT_POLLS; k++)
+    const unsigned long long t0 = global_ns();
+    for (unsigned k = 0; k < MX_WAIT_POLLS; k++) {
         if (mbar_try_wait(bar, phase)) return true;
+        if ((k & 63u) == 63u && global_ns() - t0 > MX_WAIT_NS) return false;
+    }
     return false;
 }
 
@@ -645,7 +659,7 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
     }
     __syncthreads();
     // the first two tiles travel while the heavy sources are summed
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && !a.hold) {
         if (n_tiles > 0) issue(0);
         if (n_tiles > 1) issue(1);
     }
@@ -763,7 +777,7 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
         if (S.fail) break;
         // tile t + 2 into buffer b; its screening data become visible at the next iteration's barrier
         if (t + 2 < n_tiles) {
-            if (threadIdx.x == 0) issue(t + 2);
+            if (threadIdx.x == 0 && !a.hold) issue(t + 2);
             if (SCREEN) stage_screen(t + 2);
         }
     }
@@ -771,7 +785,8 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
         if (threadIdx.x == 0) {
             atomicExch(a.err, 1u);
             // the copies this CTA issued and did not consume: tiles t and t + 1
-            for (int u = t; u < min(t + 2, n_tiles); u++) mbar_wait(&S.bar[u & 1], (unsigned)((u >> 1) & 1));
+            if (!a.hold)
+                for (int u = t; u < min(t + 2, n_tiles); u++) mbar_wait(&S.bar[u & 1], (unsigned)((u >> 1) & 1));
         }
         return;
     }
@@ -1082,7 +1097,8 @@ int launch_split_positions(const double* x, const double* y, const double* z, co
 }
 
 int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* heavy_end, float near_ratio,
-                            int n_chunks, int chunk, double* partial, int n_part, unsigned int* err, cudaStream_t st)
+                            int n_chunks, int chunk, double* partial, int n_part, unsigned int* err, bool hold,
+                            cudaStream_t st)
 {
     if (g.n_tiles <= 0) return 0;
     constexpr int smem = (int)sizeof(MixedSmem);
@@ -1101,6 +1117,7 @@ int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* hea
     a.chunk = n_chunks > 1 ? chunk : (1 << 30);
     a.partial = n_chunks > 1 ? partial : nullptr;
     a.n_part = n_part;
+    a.hold = hold ? 1 : 0;
     const dim3 grid(g.n_tiles, n_chunks > 1 ? n_chunks : 1);
     if (g.record || g.hill)
         grav_mixed_kernel<true><<<grid, 256, smem, st>>>(a);

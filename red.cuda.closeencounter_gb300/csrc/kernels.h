@@ -86,8 +86,9 @@ int launch_split_positions(const double* x, const double* y, const double* z, co
                            const int* base_of, const int* screen_slot, const double* radius, int n,
                            SplitPos* out, float* rf, unsigned int* smax, bool hill, cudaStream_t st);
 constexpr int SCREEN_MAX_WORDS = 4;  // GravArgs::smax per system: radius, mass, star distance, spare
+// hold: test hook -- no tile copies are issued, so the kernel's bounded waits run out
 int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* heavy_end, float near_ratio,
-                            int n_chunks, int chunk, double* partial, int n_part, unsigned int* err,
+                            int n_chunks, int chunk, double* partial, int n_part, unsigned int* err, bool hold,
                             cudaStream_t st);
 // heavy pairs of the mixed-precision mode in double-float arithmetic (gravity_mixed.cu):
 // the row kernel for blocks with a few massive sources, the few-sink kernel for the

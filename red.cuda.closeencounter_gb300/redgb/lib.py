@@ -36,6 +36,7 @@ def load(auto_build=True):
     L.rg_get_profile.argtypes = [vp, ctypes.POINTER(T.Profile)]
     L.rg_measure_pipe_peak.argtypes = [ci, ctypes.POINTER(ctypes.c_double)]
     L.rg_autotune.argtypes = [vp, ci, ctypes.POINTER(T.Tune)]
+    L.rg_test_hold_tile_copies.argtypes = [vp, ci]
     _lib = L
     return L
 
@@ -68,6 +69,11 @@ class System(api.System):
         prof = T.Profile()
         self._call("get_profile", self.handle, ctypes.byref(prof))
         return {f: getattr(prof, f) for f, _ in prof._fields_}
+
+    def test_hold_tile_copies(self, on=True):
+        """Test hook: the mixed kernel issues no tile copies, so its bounded waits run out
+        and the evaluation reports RG_ERR_CUDA (rg_test_hold_tile_copies)."""
+        self._call("test_hold_tile_copies", self.handle, int(bool(on)))
 
     def autotune(self, reps=3):
         """Time the candidate launch shapes of the current gravity mode and keep the fastest

@@ -175,3 +175,25 @@ def test_mixed_screen_cutoffs_keep_every_event(gpulib):
     names = {k for k, _, _ in lists[T.GRAVITY_FP64]}
     assert len(lists[T.GRAVITY_FP64]) > 100 and len(names) >= 2, (len(lists[T.GRAVITY_FP64]), names)
     assert lists[T.GRAVITY_MIXED] == lists[T.GRAVITY_FP64]
+
+
+def test_mixed_wait_limit_reports_an_error(gpulib):
+    """Failure path of the mixed kernel without a fault: with the tile copies held back, every
+    CTA's bounded wait (one second of the GPU's global timer) runs out, the kernel records it
+    and returns, the host reports RG_ERR_CUDA, and the same context then evaluates normally."""
+    import time
+    from redgb.api import RedError
+    disk = bodies.config_disk("self_gravitating", n=4096)
+    s = lib.System(disk, bodies.thresholds())
+    s.set_gravity_mode(T.GRAVITY_MIXED)
+    ref = s.calc_accel()
+    s.test_hold_tile_copies(True)
+    t0 = time.perf_counter()
+    with pytest.raises(RedError) as ei:
+        s.calc_accel()
+    assert ei.value.status == -2 and "wait limit" in str(ei.value)
+    assert time.perf_counter() - t0 < 30.0
+    s.test_hold_tile_copies(False)
+    again = s.calc_accel()
+    for f in "xyz":
+        assert np.array_equal(again[f], ref[f])
