@@ -187,11 +187,16 @@ def run(argv):
 
 
 def main(argv=None):
+    """Exit status 0 on success, 2 for a usage error, 1 for an unreadable or invalid input
+    file (the reference prints the message and exits, main.cu:288-303)."""
     try:
         paths = run(sys.argv[1:] if argv is None else argv)
     except UsageError as x:
         print(x, file=sys.stderr)
         return 2
+    except (OSError, ValueError) as x:
+        print(f"red: {x}", file=sys.stderr)
+        return 1
     if "-v" in (sys.argv if argv is None else argv):
         print("\n".join(paths.values()))
     return 0

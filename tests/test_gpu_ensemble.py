@@ -174,3 +174,28 @@ def test_ensemble_mixed_screen_cutoffs_keep_every_event(gpulib):
         assert all(ens.stats(s)["n_tried_step"] == 1 for s in range(len(disks)))
     assert len(out[T.GRAVITY_FP64]) > 60 and len({k for _, k, _, _ in out[T.GRAVITY_FP64]}) >= 2
     assert out[T.GRAVITY_MIXED] == out[T.GRAVITY_FP64]
+
+
+def test_proposer_fallback_keeps_the_run_correct(gpulib):
+    """A proposer that always asks for the largest step it may (twice the plain controller's):
+    the embedded error estimate rejects its proposals, each disk falls back to the plain
+    controller after two rejections in a row, and the run still ends with |dE/E| < 1e-10."""
+    from redgb.proposer import N_IN, N_PARAM, Proposer
+    disks = [bodies.config_disk("ensemble_member", seed=s, n=600) for s in (7, 8)]
+    ens = Ensemble(disks, bodies.thresholds(collision_factor=0.0))
+    ens.set_integrator(0.001, 1e-10)
+    ens.set_options(gravity_mode=T.GRAVITY_MIXED, hill_factor=0.0)
+    net = Proposer(seed=1)
+    w = np.zeros(N_PARAM, np.float32)
+    w[-1] = 5.0  # the output bias: log(proposed / ideal step) = 5 for every input
+    net.set_params(w)
+    net.set_normalisation(np.zeros(N_IN), np.ones(N_IN))
+    net.attach(ens, safety=1.0, cooldown=16)
+    E0 = [ens.energy(s)[0] for s in range(len(disks))]
+    ens.advance(120.0, max_attempts=20000)
+    st = [ens.stats(s) for s in range(len(disks))]
+    assert all(x["status"] == T.SYS_DONE for x in st)
+    assert sum(x["n_fallback"] for x in st) > 0
+    assert sum(x["n_proposed"] for x in st) > sum(x["n_proposal_accepted"] for x in st)
+    for s in range(len(disks)):
+        assert abs((ens.energy(s)[0] - E0[s]) / E0[s]) < 1e-10

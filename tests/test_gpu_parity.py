@@ -171,6 +171,26 @@ def test_state_records_in_and_out(gpulib):
         s.state(out=(np.zeros(n - 1, T.VEC), np.zeros(n, T.VEC)))
 
 
+def test_nan_in_the_state_is_reported(gpulib):
+    """A NaN position: the first step spreads it exactly as the oracle does (states equal, NaN
+    for NaN); the controller's next step is then infinite, which rg_step (like the
+    reference's integrator) returns and rg_advance's main loop reports as
+    RG_ERR_DT_NONFINITE."""
+    disk = bodies.make_disk(n_pl=40, pl_type=T.BODY_PROTOPLANET, seed=8, n_tp=3)
+    g, o = _pair(disk, bodies.thresholds(), lambda s: s.set_integrator(T.INT_RKF78, 0.01, False))
+    for s in (g, o):
+        r, v = s.state()[:2]
+        r["x"][7] = np.nan
+        s.set_state(r, v)
+    g.step()
+    o.step()
+    _assert_same_state(g, o)
+    g.set_integrator(T.INT_RKF78, 0.01, True, 1e-10)
+    with pytest.raises(RedError) as ei:
+        g.advance(1.0e9, max_steps=3)
+    assert ei.value.status == -4
+
+
 def test_energy_matches_oracle(gpulib):
     disk = bodies.make_disk(n_pl=500, seed=3, n_tp=10, embryos=((1e-6, 1.5, 0.0),))
     g = gpu_system(disk, bodies.thresholds())
