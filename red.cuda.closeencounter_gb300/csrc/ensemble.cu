@@ -508,6 +508,10 @@ struct rg_ens {
     std::vector<rg_body_metadata_t> md;
     std::vector<double> thr;  // 5 per disk
     cudaStream_t st = nullptr;
+    // the row kernels of an evaluation (planetesimals against the star and giants) run on a
+    // side stream beside the other groups: forked after the split, joined before the combine
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     // device, per body
     double* d_y = nullptr;
     double* d_yout = nullptr;
@@ -656,6 +660,9 @@ void free_all(rg_ens* e)
     for (void* q : ptrs) cudaFree(q);
     for (auto& k : e->d_k) cudaFree(k);
     if (e->st) cudaStreamDestroy(e->st);
+    if (e->st2) cudaStreamDestroy(e->st2);
+    if (e->ev_fork) cudaEventDestroy(e->ev_fork);
+    if (e->ev_join) cudaEventDestroy(e->ev_join);
 }
 
 // ------------------------------------------------------------------- plans
@@ -852,13 +859,35 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
                                       e->st));
         g.smax = e->d_smax;
     }
+    const auto& plan = e->plan[e->gravity_mode == RG_GRAVITY_MIXED ? 1 : 0];
     bool split_done = false;
-    for (const auto& gr : e->plan[e->gravity_mode == RG_GRAVITY_MIXED ? 1 : 0]) {
+    if (e->gravity_mode == RG_GRAVITY_MIXED && !plan.empty()) {
+        rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->d_base_of, e->d_screen_slot, e->d_radius,
+                                    e->cap, (SplitPos*)e->d_split, e->d_rf, g.smax ? e->d_smax : nullptr, g.hill != 0,
+                                    e->st);
+        split_done = true;
+        e->n_kernels++;
+        if (rc) return rc;
+    }
+    // fork the row groups onto the side stream when other groups run beside them
+    bool has_row = false, has_other = false;
+    for (const auto& gr : plan) {
+        const bool row = gr.kind == GROUP_ROWSEQ || gr.kind == GROUP_DF_ROWSEQ;
+        has_row = has_row || row;
+        has_other = has_other || !row;
+    }
+    const bool fork = has_row && has_other;
+    if (fork) {
+        RG_CUDA_CHECK(cudaEventRecord(e->ev_fork, e->st));
+        RG_CUDA_CHECK(cudaStreamWaitEvent(e->st2, e->ev_fork, 0));
+    }
+    cudaStream_t row_st = fork ? e->st2 : e->st;
+    for (const auto& gr : plan) {
         g.tiles = e->d_tiles + gr.off;
         g.n_tiles = gr.n;
         switch (gr.kind) {
         case GROUP_PAIRPAR: rc = launch_grav_fp64_pairpar(g, e->pairpar_S, e->st); e->n_kernels++; break;
-        case GROUP_ROWSEQ: rc = launch_grav_fp64_rowseq(g, e->st); e->n_kernels++; break;
+        case GROUP_ROWSEQ: rc = launch_grav_fp64_rowseq(g, row_st); e->n_kernels++; break;
         case GROUP_FEW_SERIAL:
             rc = launch_grav_fp64_few(g, e->d_few_row0 + gr.off, gr.max_src, e->d_terms, e->few_rows, e->few_pitch,
                                       e->d_row_sink, e->d_row_nsrc, e->d_row_sys, gr.row_base, gr.rows, e->st);
@@ -875,7 +904,7 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
             }
             if (rc) break;
             if (gr.kind == GROUP_DF_ROWSEQ) {
-                rc = launch_grav_df_rowseq(g, e->d_split, e->st);
+                rc = launch_grav_df_rowseq(g, e->d_split, row_st);
                 e->n_kernels++;
             } else {
                 rc = launch_grav_df_few(g, e->d_split, e->d_few_row0 + gr.off, gr.max_src, gr.max_sinks, e->few_chunk,
@@ -903,7 +932,11 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
             }
             break;
         }
-        if (rc) return rc;
+        if (rc) break;
+    }
+    if (fork) {  // join (also after an error: a capture must not end with the side stream open)
+        RG_CUDA_CHECK(cudaEventRecord(e->ev_join, e->st2));
+        RG_CUDA_CHECK(cudaStreamWaitEvent(e->st, e->ev_join, 0));
     }
     return rc;
 }
@@ -1332,6 +1365,11 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
         if (!rc) rc = x;
     };
     if (cudaStreamCreateWithFlags(&e->st, cudaStreamNonBlocking) != cudaSuccess) chk(set_error(RG_ERR_CUDA, "stream"));
+    if (!rc && cudaStreamCreateWithFlags(&e->st2, cudaStreamNonBlocking) != cudaSuccess)
+        chk(set_error(RG_ERR_CUDA, "stream"));
+    if (!rc && (cudaEventCreateWithFlags(&e->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&e->ev_join, cudaEventDisableTiming) != cudaSuccess))
+        chk(set_error(RG_ERR_CUDA, "event"));
     chk(dalloc(&e->d_y, 6 * nt));
     chk(dalloc(&e->d_yout, 6 * nt));
     for (auto& k : e->d_k) chk(dalloc(&k, 6 * nt));
