@@ -448,6 +448,28 @@ struct SinkD {
 
 constexpr int MX_GROUP = 16;  // sources summed in plain FP32 before each two-sum
 
+// The detailed FP32 screen of one light pair (sink i, source j) of the mixed kernel, with the
+// same 1e-3 margin as df_screen; candidates are decided in FP64 by exact_event_tests.  sf:
+// the sink's R, m, rho (FP32); Rj, rhoj: the source's.
+__device__ __noinline__ void mixed_screen_pair(const GravArgs& g, const Tile& tile, int i, int j, float r2, float mj,
+                                               float4 sf, float Rj, float rhoj, float inv3M, const SinkD& sd)
+{
+    const int li = i - tile.base, lj = j - tile.base;
+    if (!(li > 0 && li > lj && mj >= 0.0f)) return;
+    const float margin = 1.001f;
+    bool cand = false;
+    if (g.record) {
+        const float lim = g.f_rad_f * (sf.x + Rj) * margin;
+        cand = r2 < lim * lim;
+    }
+    if (g.hill && tile.block != 2 && lj > 0) {
+        const float h = 0.5f * (sf.z + rhoj);
+        const float d3 = r2 * sqrtf(r2);
+        cand = cand || (d3 < g.hill_f3_f * (sf.y + mj) * inv3M * (h * h * h) * (margin * margin * margin));
+    }
+    if (cand && 0 <= g.id[j]) exact_event_tests(g, tile, i, j, sd.x, sd.y, sd.z, sd.R, sd.m, sd.rho);
+}
+
 // One warp-slice of a source tile for MX_R sinks per lane.  DIAG: the slice may hold the
 // sinks themselves (self pairs are skipped); SCREEN: event screens are on.
 template <bool DIAG, bool SCREEN>
@@ -455,8 +477,9 @@ __device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile
                                             const SplitPos* s_sp, const float4* s_sinkf, float inv3M, const float* s_R,
                                             const float* s_rho, const SinkD* s_sink, const int* si,
                                             const float* xh, const float* xl, const float* yh, const float* yl,
-                                            const float* zh, const float* zl, const float* near_lim, Acc2* ax,
-                                            Acc2* ay, Acc2* az, unsigned* near_mask, int lane)
+                                            const float* zh, const float* zl, const float* near_lim,
+                                            const float* cut2, Acc2* ax, Acc2* ay, Acc2* az, unsigned* near_mask,
+                                            int lane)
 {
     const GravArgs& g = a.g;
     float px[MX_R], py[MX_R], pz[MX_R];
@@ -490,28 +513,10 @@ __device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile
             pz[r] = fmaf(w, dz, pz[r]);
             near_mask[r] |= (unsigned)near << (q - q_begin);
             // one compare per pair: beyond its cutoff no pair of this sink can pass the screens
-            if (SCREEN && r2 < s_sinkf[lane + 32 * r].w) {
-                const int li = si[r] - tile.base, lj = j - tile.base;
-                if (li > 0 && li > lj && (!DIAG || j != si[r]) && mj >= 0.0f) {
-                    const float4 sf = s_sinkf[lane + 32 * r];  // R, m, rho of the sink in FP32
-                    const float margin = 1.001f;
-                    bool cand = false;
-                    if (g.record) {
-                        const float lim = g.f_rad_f * (sf.x + s_R[q]) * margin;
-                        cand = r2 < lim * lim;
-                    }
-                    if (g.hill && tile.block != 2 && lj > 0) {
-                        const float h = 0.5f * (sf.z + s_rho[q]);
-                        const float d3 = r2 * sqrtf(r2);
-                        cand = cand || (d3 < g.hill_f3_f * (sf.y + mj) * inv3M * (h * h * h) *
-                                                 (margin * margin * margin));
-                    }
-                    if (cand && 0 <= g.id[j]) {
-                        const SinkD& sd = s_sink[lane + 32 * r];
-                        exact_event_tests(g, tile, si[r], j, sd.x, sd.y, sd.z, sd.R, sd.m, sd.rho);
-                    }
-                }
-            }
+            // (the detailed screen is out of line, so that the pair loop keeps its registers)
+            if (SCREEN && r2 < cut2[r] && (!DIAG || j != si[r]))
+                mixed_screen_pair(g, tile, si[r], j, r2, mj, s_sinkf[lane + 32 * r], s_R[q], s_rho[q], inv3M,
+                                  s_sink[lane + 32 * r]);
         }
         if (((q - q_begin) & (MX_GROUP - 1)) == MX_GROUP - 1) {
 #pragma unroll
@@ -669,13 +674,14 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
     }
 
     int si[MX_R];
-    float xh[MX_R], xl[MX_R], yh[MX_R], yl[MX_R], zh[MX_R], zl[MX_R], near_lim[MX_R];
+    float xh[MX_R], xl[MX_R], yh[MX_R], yl[MX_R], zh[MX_R], zl[MX_R], near_lim[MX_R], cut2[MX_R];
     Acc2 ax[MX_R], ay[MX_R], az[MX_R];
 #pragma unroll
     for (int r = 0; r < MX_R; r++) {
         const int s = lane + 32 * r;
         const int i = tile.sink_begin + s;
         si[r] = i;
+        cut2[r] = SCREEN ? S.sinkf[s].w : -1.0f;
         xh[r] = xl[r] = yh[r] = yl[r] = zh[r] = zl[r] = 0.0f;
         float pull = 0.0f;
         if (i < tile.sink_end) {
@@ -741,10 +747,10 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
             const bool diag = (j0 + q_begin < tile.sink_begin + MX_S) && (j0 + q_end > tile.sink_begin);
             if (diag)
                 mixed_slice<true, SCREEN>(a, tile, j0, q_begin, q_end, S.sp[b], S.sinkf, inv3M, S.R[b], S.rho[b], S.sink, si, xh, xl,
-                                          yh, yl, zh, zl, near_lim, ax, ay, az, near_mask, lane);
+                                          yh, yl, zh, zl, near_lim, cut2, ax, ay, az, near_mask, lane);
             else
                 mixed_slice<false, SCREEN>(a, tile, j0, q_begin, q_end, S.sp[b], S.sinkf, inv3M, S.R[b], S.rho[b], S.sink, si, xh,
-                                           xl, yh, yl, zh, zl, near_lim, ax, ay, az, near_mask, lane);
+                                           xl, yh, yl, zh, zl, near_lim, cut2, ax, ay, az, near_mask, lane);
             // near pairs of this slice: the double-float term (FP64-class accuracy on the FP32
             // pipes), from the FP64 displacement for pairs closer than the split positions resolve
 #pragma unroll
