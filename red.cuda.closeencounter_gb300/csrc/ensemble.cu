@@ -66,6 +66,37 @@ struct EnsStageArgs {
 // y + fma(dt c_q, k_q, ...), half the FP64 operations -- GB300 retires about two FP64
 // operations per SM and clock, so these kernels are bound by FP64 issue, not by HBM.
 template <int FORM, int NTERM, bool FUSED>
+__device__ __forceinline__ double ens_combine_one(const EnsStageArgs& a, const double* w, double dt, long long e)
+{
+    const double y = a.y[e];
+    if (FUSED) {
+        double sum;
+        if (FORM == FORM_SUM) {
+            sum = w[0] * a.k[0][e];
+#pragma unroll
+            for (int q = 1; q < NTERM; q++) sum = fma(w[q], a.k[q][e], sum);
+        } else {
+            sum = w[0] * a.k[0][e];
+            sum = fma(w[1], a.k[1][e], sum);
+            sum = fma(w[2], a.k[2][e] + a.k[3][e], sum);
+            sum = fma(w[3], a.k[4][e] + a.k[5][e], sum);
+            sum = fma(w[4], a.k[6][e], sum);
+        }
+        return y + sum;
+    }
+    if (FORM == FORM_SUM) {
+        double sum = a.c[0] * a.k[0][e];
+#pragma unroll
+        for (int q = 1; q < NTERM; q++) sum = sum + a.c[q] * a.k[q][e];
+        return y + dt * sum;
+    }
+    return y + dt * (a.c[0] * a.k[0][e] + a.c[1] * a.k[1][e] + a.c[2] * (a.k[2][e] + a.k[3][e]) +
+                     a.c[3] * (a.k[4][e] + a.k[5][e]) + a.c[4] * a.k[6][e]);
+}
+
+// Rows one after another, two independent elements per thread and iteration (their loads
+// and FP64 chains interleave: these kernels are bound by FP64 issue and load latency).
+template <int FORM, int NTERM, bool FUSED>
 __global__ void __launch_bounds__(256) ens_combine_kernel(EnsStageArgs a)
 {
     const StageTile t = a.tiles[blockIdx.x];
@@ -77,38 +108,20 @@ __global__ void __launch_bounds__(256) ens_combine_kernel(EnsStageArgs a)
         for (int q = 0; q < MAXT; q++) w[q] = dt * a.c[q];
     }
     const int nb = t.b1 - t.b0;
-    for (int f = threadIdx.x; f < 6 * nb; f += blockDim.x) {
-        const int row = f / nb;
-        const long long e = (long long)row * a.stride + t.b0 + (f - row * nb);
-        const double y = a.y[e];
-        double out;
-        if (FUSED) {
-            double sum;
-            if (FORM == FORM_SUM) {
-                sum = w[0] * a.k[0][e];
-#pragma unroll
-                for (int q = 1; q < NTERM; q++) sum = fma(w[q], a.k[q][e], sum);
+    for (int row = 0; row < 6; row++) {
+        const long long base = (long long)row * a.stride + t.b0;
+        double* out = row < 3 ? a.out_lo + base : a.out_hi + base - 3LL * a.stride;
+        for (int i = threadIdx.x; i < nb; i += 2 * blockDim.x) {
+            const int i2 = i + blockDim.x;
+            const double o1 = ens_combine_one<FORM, NTERM, FUSED>(a, w, dt, base + i);
+            if (i2 < nb) {
+                const double o2 = ens_combine_one<FORM, NTERM, FUSED>(a, w, dt, base + i2);
+                out[i] = o1;
+                out[i2] = o2;
             } else {
-                sum = w[0] * a.k[0][e];
-                sum = fma(w[1], a.k[1][e], sum);
-                sum = fma(w[2], a.k[2][e] + a.k[3][e], sum);
-                sum = fma(w[3], a.k[4][e] + a.k[5][e], sum);
-                sum = fma(w[4], a.k[6][e], sum);
+                out[i] = o1;
             }
-            out = y + sum;
-        } else if (FORM == FORM_SUM) {
-            double sum = a.c[0] * a.k[0][e];
-#pragma unroll
-            for (int q = 1; q < NTERM; q++) sum = sum + a.c[q] * a.k[q][e];
-            out = y + dt * sum;
-        } else {
-            out = y + dt * (a.c[0] * a.k[0][e] + a.c[1] * a.k[1][e] + a.c[2] * (a.k[2][e] + a.k[3][e]) +
-                            a.c[3] * (a.k[4][e] + a.k[5][e]) + a.c[4] * a.k[6][e]);
         }
-        if (row < 3)
-            a.out_lo[e] = out;
-        else
-            a.out_hi[e - 3LL * a.stride] = out;
     }
 }
 
