@@ -459,8 +459,21 @@ def ensemble_section(args):
     net, loss = fit(x, y, seed=0, epochs=30)
     train_s = time.perf_counter() - t0
 
+    t_cpu = time.perf_counter()
     disks = [bodies.config_disk("ensemble_member", seed=s) for s in range(65, 65 + args.ensemble_disks)]
+    t_cpu = time.perf_counter() - t_cpu
     n_bodies = sum(d.n_total for d in disks)
+    # the same ensemble's shapes from the GPU generator (its own random streams)
+    from redgb.icgen import generate_disks, spec_like
+    specs = [spec_like("ensemble_member", seed=s) for s in range(65, 65 + args.ensemble_disks)]
+    generate_disks(specs[:1])  # first use: module load
+    t_gpu = time.perf_counter()
+    gen = generate_disks(specs)
+    t_gpu = time.perf_counter() - t_gpu
+    ic_generator = {"disks": len(gen), "bodies": int(sum(d.n_total for d in gen)), "gpu_seconds": t_gpu,
+                    "cpu_python_seconds": t_cpu, "note": "GPU: rg_generate_disks incl. copies to the host; CPU: "
+                    "bodies.config_disk (numpy draws, scalar Kepler solver per body)"}
+    del gen
 
     def batched(mode, proposer):
         e = Ensemble(disks, thr)
@@ -532,6 +545,7 @@ def ensemble_section(args):
         "plain_mixed_batched": plain_mixed,
         "plain_fp64_batched": plain_fp64,
         "plain_fp64_sequential": sequential,
+        "ic_generator": ic_generator,
         "speedup_vs_plain_fp64_sequential": learned["sim_years_per_s"] / sequential["sim_years_per_s"],
         "speedup_vs_plain_fp64_batched": learned["sim_years_per_s"] / plain_fp64["sim_years_per_s"],
         "learned_vs_plain_attempts": plain_mixed["attempts"] / max(learned["attempts"], 1),

@@ -201,6 +201,17 @@ RG_API int rg_calc_accel(rg_ctx* ctx, rg_vec_t* a);
  */
 RG_API int rg_autotune(rg_ctx* ctx, int reps, rg_tune_t* out);
 
+/* Synthetic disks generated on the GPU (the seeded initial-condition generator of this
+ * project; the reference's own generator is the separate red.cuda.initial program): disk s
+ * gets the records [off_s, off_s + n_total_s) of r, v (AU, AU/day, heliocentric), p and md,
+ * off_s the sum of the previous disks' totals, and its body counts in counts[s].  One thread
+ * per body; each body's random numbers come from Philox4x32-10 with the disk's seed as the
+ * key and (body slot, draw block) as the counter, so the result does not depend on the
+ * launch shape; orbital elements go to Cartesian by the reference's calculate_phase
+ * (tools.cpp:292-359).  Invalid specifications return RG_ERR_ARG. */
+RG_API int rg_generate_disks(int n_sys, const rg_disk_spec_t* specs, rg_counts_t* counts, rg_vec_t* r,
+                             rg_vec_t* v, rg_param_t* p, rg_body_metadata_t* md);
+
 /* Test hook for the failure path (no counterpart in the reference): with `on`, the mixed
  * kernel issues none of its tile copies, so each CTA's bounded wait (one second of the GPU's
  * global timer) runs out; the evaluation then reports RG_ERR_CUDA ("a gravity tile copy did

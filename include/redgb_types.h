@@ -72,6 +72,22 @@ typedef struct rg_profile {
     double  stage_ms;
 } rg_profile_t;
 
+/* one synthetic disk for rg_generate_disks: a 1 Msun star at rest in the origin, giants on
+ * the given orbits (random mean anomaly and argument of pericentre, i = 0), n_pl bodies of
+ * type pl_type (RG_BODY_PROTOPLANET: self-gravitating, or RG_BODY_PLANETESIMAL) and n_tp test
+ * particles */
+typedef struct rg_disk_spec {
+    uint64_t seed;           /* key of the disk's Philox4x32-10 streams                       */
+    int32_t  n_pl, pl_type, n_tp, n_giants;  /* n_giants <= 4                                  */
+    double   giant_m[4], giant_a[4], giant_e[4];  /* [Msun], [AU]; radii from 1.33 g/cm^3      */
+    double   m_lo, m_hi;     /* planetesimal masses, log-uniform [Msun]                      */
+    double   a_lo, a_hi;     /* semi-major axes [AU]                                          */
+    int32_t  a_mode;         /* 0: Sigma ~ r^-1.5 (dN/da ~ a^-0.5); 1: uniform (also the TPs' rule) */
+    int32_t  pad;
+    double   sigma_e, sigma_i;  /* Rayleigh scales of e (capped at 0.9) and i [rad]           */
+    double   rho_pl;         /* planetesimal density [g/cm^3]                                 */
+} rg_disk_spec_t;
+
 /* launch shape of a context's force evaluation (rg_autotune) */
 typedef struct rg_tune {
     int32_t pairpar_sinks;   /* FP64 mode: sinks per pair-parallel CTA (8, 16 or 32)             */
