@@ -15,7 +15,7 @@
 //    (x_j^hi - x_i^hi) + (x_j^lo - x_i^lo): the hi difference is exact for neighbours
 //    (Sterbenz), so the displacement carries the FP64 positions' information down to
 //    FP32 resolution of the displacement itself.  1/r comes from the FP32 rsqrt refined
-//    by one Newton step, and the terms are summed in groups of 16 folded into compensated
+//    by one Newton step, and each warp-slice's 32 terms are summed in FP32 and folded into compensated
 //    (two-sum) FP32 accumulators per component.
 //  * Event tests (collision radius, Hill sphere) are re-evaluated in FP64 for every pair
 //    whose FP32 distance is within a 1e-3 relative margin of a threshold, so the event
@@ -446,7 +446,6 @@ struct SinkD {
     double x, y, z, R, m, rho;
 };
 
-constexpr int MX_GROUP = 16;  // sources summed in plain FP32 before each two-sum
 
 // The detailed FP32 screen of one light pair (sink i, source j) of the mixed kernel, with the
 // same 1e-3 margin as df_screen; candidates are decided in FP64 by exact_event_tests.  sf:
@@ -470,29 +469,41 @@ __device__ __noinline__ void mixed_screen_pair(const GravArgs& g, const Tile& ti
     if (cand && 0 <= g.id[j]) exact_event_tests(g, tile, i, j, sd.x, sd.y, sd.z, sd.R, sd.m, sd.rho);
 }
 
-// One warp-slice of a source tile for MX_R sinks per lane.  DIAG: the slice may hold the
-// sinks themselves (self pairs are skipped); SCREEN: event screens are on.
-template <bool DIAG, bool SCREEN>
-__device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile, int j0, int q_begin, int q_end,
-                                            const SplitPos* s_sp, const float4* s_sinkf, float inv3M, const float* s_R,
-                                            const float* s_rho, const SinkD* s_sink, const int* si,
-                                            const float* xh, const float* xl, const float* yh, const float* yl,
-                                            const float* zh, const float* zl, const float* near_lim,
-                                            const float* cut2, Acc2* ax, Acc2* ay, Acc2* az, unsigned* near_mask,
-                                            int lane)
+// The r^2 below which a pair of one sink and one warp-slice is flagged for the exact pass:
+// every near pair (m_j > near_lim r^2, m_j <= mslice, the slice's largest mass), every
+// self pair (r^2 = 0) and every screen candidate (r^2 < cut2) lies below it.  Proof of the
+// near part: FP32 multiplication is monotone, so r^2 >= c gives fl(near_lim r^2) >=
+// fl(near_lim c), which the check makes >= mslice.  A quotient that fails the check (no
+// heavy source, an overflow) flags every pair of the slice.
+__device__ __forceinline__ float flag_cut2(float mslice, float near_lim, float inv_near_lim, float cut2)
 {
-    const GravArgs& g = a.g;
+    float c = mslice > 0.0f ? mslice * inv_near_lim * 1.0001f : 0.0f;
+    c = fmaxf(fmaxf(c, cut2), 1.17549435e-38f);  // FLT_MIN: self pairs (r^2 = 0) are flagged
+    return near_lim * c >= mslice ? c : 3.0e38f;
+}
+
+// One warp-slice of a source tile (at most 32 sources) for MX_R sinks per lane: the FP32
+// terms of the pairs whose r^2 is at or above the sink's flag cutoff (flag_cut2), one
+// compare per pair, summed in FP32 over the slice and folded into the compensated
+// accumulators once.  The flagged pairs add nothing here; their bits (source q - q_begin)
+// go to `flags` for the warp's flagged-pair rounds.
+__device__ __forceinline__ void mixed_slice(const SplitPos* s_sp, int q_begin, int q_end, const float* xh,
+                                            const float* xl, const float* yh, const float* yl, const float* zh,
+                                            const float* zl, const float* flag2, Acc2* ax, Acc2* ay, Acc2* az,
+                                            unsigned* flags)
+{
     float px[MX_R], py[MX_R], pz[MX_R];
 #pragma unroll
     for (int r = 0; r < MX_R; r++) {
         px[r] = py[r] = pz[r] = 0.0f;
-        near_mask[r] = 0u;
+        flags[r] = 0u;
     }
-    for (int q = q_begin; q < q_end; q++) {
+    unsigned bit = 1u;
+#pragma unroll 4
+    for (int q = q_begin; q < q_end; q++, bit <<= 1) {
         const float4 pxy = s_sp[q].xy;
         const float4 pzm = s_sp[q].zm;
         const float mj = pzm.z;
-        const int j = j0 + q;
 #pragma unroll
         for (int r = 0; r < MX_R; r++) {
             const float dx = (pxy.x - xh[r]) + (pxy.y - xl[r]);
@@ -500,42 +511,66 @@ __device__ __forceinline__ void mixed_slice(const MixedArgs& a, const Tile& tile
             const float dz = (pzm.x - zh[r]) + (pzm.y - zl[r]);
             // finite: split_positions clamps coordinates to 1e15 AU
             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-            bool near = mj > near_lim[r] * r2;
-            if (DIAG) near = near && j != si[r];
+            const bool flag = r2 < flag2[r];
             const float y0 = rsqrt_approx(r2);
             const float hr2 = 0.5f * r2;
             const float y = y0 * fmaf(-hr2, y0 * y0, 1.5f);
-            float w = mj * (y * y * y);
-            if (DIAG) w = (j == si[r]) ? 0.0f : w;
-            w = near ? 0.0f : w;
+            const float w = flag ? 0.0f : mj * (y * y * y);
             px[r] = fmaf(w, dx, px[r]);
             py[r] = fmaf(w, dy, py[r]);
             pz[r] = fmaf(w, dz, pz[r]);
-            near_mask[r] |= (unsigned)near << (q - q_begin);
-            // one compare per pair: beyond its cutoff no pair of this sink can pass the screens
-            // (the detailed screen is out of line, so that the pair loop keeps its registers)
-            if (SCREEN && r2 < cut2[r] && (!DIAG || j != si[r]))
-                mixed_screen_pair(g, tile, si[r], j, r2, mj, s_sinkf[lane + 32 * r], s_R[q], s_rho[q], inv3M,
-                                  s_sink[lane + 32 * r]);
-        }
-        if (((q - q_begin) & (MX_GROUP - 1)) == MX_GROUP - 1) {
-#pragma unroll
-            for (int r = 0; r < MX_R; r++) {
-                two_sum_add(ax[r], px[r]);
-                two_sum_add(ay[r], py[r]);
-                two_sum_add(az[r], pz[r]);
-                px[r] = py[r] = pz[r] = 0.0f;
-            }
+            flags[r] |= flag ? bit : 0u;
         }
     }
-    if (((q_end - q_begin) & (MX_GROUP - 1)) != 0) {  // a partial last group (uniform over the warp)
 #pragma unroll
-        for (int r = 0; r < MX_R; r++) {
-            two_sum_add(ax[r], px[r]);
-            two_sum_add(ay[r], py[r]);
-            two_sum_add(az[r], pz[r]);
-        }
+    for (int r = 0; r < MX_R; r++) {
+        two_sum_add(ax[r], px[r]);
+        two_sum_add(ay[r], py[r]);
+        two_sum_add(az[r], pz[r]);
     }
+}
+
+// One flagged pair (sink i, source j = j0 + q), classified exactly: a self pair adds
+// nothing; a screen candidate (r^2 < cut2, the pair loop's FP32 r^2 recomputed by the same
+// operations) goes to the detailed screen; a near pair (m_j > near_lim r^2) gives its
+// double-float term, from the FP64 displacement where the split positions would not resolve
+// the pair (close_r2); any other pair gives its FP32 term (lo parts 0).
+struct FlagTerm {
+    float hx, lx, hy, ly, hz, lz;
+};
+
+template <bool SCREEN>
+__device__ __forceinline__ FlagTerm mixed_flag_term(const MixedArgs& a, const Tile& tile, int i, int j, int q,
+                                                    const SplitPos* s_sp, const float* s_R, const float* s_rho,
+                                                    const float4 sf, const SinkD& sd, const SplitPos sp,
+                                                    float near_lim, float inv3M)
+{
+    const GravArgs& g = a.g;
+    FlagTerm f{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    if (j == i) return f;
+    const SplitPos pj = s_sp[q];
+    const float mj = pj.zm.z;
+    const float dx = (pj.xy.x - sp.xy.x) + (pj.xy.y - sp.xy.y);
+    const float dy = (pj.xy.z - sp.xy.z) + (pj.xy.w - sp.xy.w);
+    const float dz = (pj.zm.x - sp.zm.x) + (pj.zm.y - sp.zm.y);
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    if (SCREEN && r2 < sf.w) mixed_screen_pair(g, tile, i, j, r2, mj, sf, s_R[q], s_rho[q], inv3M, sd);
+    if (mj > near_lim * r2) {
+        DF tx, ty, tz;
+        float r2f;
+        df_term(sp, pj, tx, ty, tz, r2f);
+        if (r2f < close_r2(sp))
+            df_term_fp64(sd.x, sd.y, sd.z, g.px[j], g.py[j], g.pz[j], mj, pj.zm.w, tx, ty, tz, r2f);
+        f = FlagTerm{tx.hi, tx.lo, ty.hi, ty.lo, tz.hi, tz.lo};
+    } else {
+        const float y0 = rsqrt_approx(r2);
+        const float y = y0 * fmaf(-0.5f * r2, y0 * y0, 1.5f);
+        const float w = mj * (y * y * y);
+        f.hx = w * dx;
+        f.hy = w * dy;
+        f.hz = w * dz;
+    }
+    return f;
 }
 
 // Source tiles reach shared memory by TMA bulk copies (cp.async.bulk, one thread issues an
@@ -602,6 +637,10 @@ struct MixedSmem {
     SplitPos sp[2][MX_T];              // double-buffered source tiles (TMA destination)
     SinkD sink[MX_S];
     float4 sinkf[MX_S];                // R, m, rho, r^2 cutoff of the sinks in FP32 (screens)
+    float2 near_lim[MX_S];             // the sinks' near-pair limits and their reciprocals
+    SplitPos sinksp[MX_S];             // the sinks' split positions
+    FlagTerm fterm[MX_WARPS][32];      // one round of a warp's flagged-pair terms
+    unsigned short fitem[MX_WARPS][32];  // the round's items: owner lane << 7 | row << 5 | source bit
     Acc2 part[MX_WARPS][3][MX_S];      // per-warp compensated partial sums
     float R[2][MX_T], rho[2][MX_T];    // screening data of the tiles (SCREEN only)
     unsigned long long bar[2];
@@ -654,6 +693,21 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
         }
         S.sink[s] = sd;
         S.sinkf[s] = make_float4((float)sd.R, (float)sd.m, (float)sd.rho, 0.0f);
+        SplitPos sp;
+        sp.xy = sp.zm = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float pull = 0.0f;
+        if (i < tile.sink_end) {
+            sp = a.sp[i];
+            if (tile.src_begin < heavy_end) {  // m / r^2 of the first heavy source: the near-pair scale
+                const int j = tile.src_begin;
+                const double dx = g.px[j] - sd.x, dy = g.py[j] - sd.y, dz = g.pz[j] - sd.z;
+                pull = (float)(g.mass[j] / (dx * dx + dy * dy + dz * dz));
+            }
+        }
+        S.sinksp[s] = sp;
+        // a pair is near when m_j > near_lim * r^2; without a heavy source there is no scale
+        const float nl = pull > 0.0f ? a.near_ratio * pull : 3.0e38f;
+        S.near_lim[s] = make_float2(nl, 1.0f / nl);
     }
     const float inv3M = (SCREEN && g.hill) ? (float)(1.0 / (3.0 * g.mass[tile.base])) : 0.0f;
     // .w: the sink's cutoff on r^2 (screen_cut2); padding sinks get none
@@ -674,29 +728,15 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
     }
 
     int si[MX_R];
-    float xh[MX_R], xl[MX_R], yh[MX_R], yl[MX_R], zh[MX_R], zl[MX_R], near_lim[MX_R], cut2[MX_R];
+    float xh[MX_R], xl[MX_R], yh[MX_R], yl[MX_R], zh[MX_R], zl[MX_R];
     Acc2 ax[MX_R], ay[MX_R], az[MX_R];
 #pragma unroll
     for (int r = 0; r < MX_R; r++) {
         const int s = lane + 32 * r;
-        const int i = tile.sink_begin + s;
-        si[r] = i;
-        cut2[r] = SCREEN ? S.sinkf[s].w : -1.0f;
-        xh[r] = xl[r] = yh[r] = yl[r] = zh[r] = zl[r] = 0.0f;
-        float pull = 0.0f;
-        if (i < tile.sink_end) {
-            const SplitPos sp = a.sp[i];
-            xh[r] = sp.xy.x; xl[r] = sp.xy.y; yh[r] = sp.xy.z; yl[r] = sp.xy.w;
-            zh[r] = sp.zm.x; zl[r] = sp.zm.y;
-            if (tile.src_begin < heavy_end) {  // m / r^2 of the first heavy source: the near-pair scale
-                const SinkD sd = S.sink[s];
-                const int j = tile.src_begin;
-                const double dx = g.px[j] - sd.x, dy = g.py[j] - sd.y, dz = g.pz[j] - sd.z;
-                pull = (float)(g.mass[j] / (dx * dx + dy * dy + dz * dz));
-            }
-        }
-        // a pair is near when m_j > near_lim * r^2; without a heavy source there is no scale
-        near_lim[r] = pull > 0.0f ? a.near_ratio * pull : 3.0e38f;
+        si[r] = tile.sink_begin + s;
+        const SplitPos sp = S.sinksp[s];
+        xh[r] = sp.xy.x; xl[r] = sp.xy.y; yh[r] = sp.xy.z; yl[r] = sp.xy.w;
+        zh[r] = sp.zm.x; zl[r] = sp.zm.y;
         ax[r] = ay[r] = az[r] = Acc2{0.0f, 0.0f};
     }
 
@@ -731,52 +771,82 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
     }
     if (SCREEN) __syncthreads();  // the screening data of tiles 0 and 1 are visible
 
-    constexpr int SLICE = MX_T / MX_WARPS;  // 32 sources per warp and tile: one near-mask bit each
+    constexpr int SLICE = MX_T / MX_WARPS;  // 32 sources per warp and tile: one flag bit each
     int t = 0;
     for (; t < n_tiles; t++) {
         const int b = t & 1;
         const int j0 = first + t * MX_T;
         const int nj = min(MX_T, src_hi - j0);
-        const bool arrived = mbar_wait(&S.bar[b], (unsigned)((t >> 1) & 1));
+        // one answer per warp, so that the warp's shuffles below see all of its lanes
+        const bool arrived = __all_sync(0xffffffffu, mbar_wait(&S.bar[b], (unsigned)((t >> 1) & 1)));
         if (!arrived) S.fail = 1;
         const int q_begin = warp * SLICE;
         const int q_end = min(nj, q_begin + SLICE);
         if (arrived && q_begin < q_end) {
-            unsigned near_mask[MX_R];
-            // does this slice hold any of the CTA's sinks?
-            const bool diag = (j0 + q_begin < tile.sink_begin + MX_S) && (j0 + q_end > tile.sink_begin);
-            if (diag)
-                mixed_slice<true, SCREEN>(a, tile, j0, q_begin, q_end, S.sp[b], S.sinkf, inv3M, S.R[b], S.rho[b], S.sink, si, xh, xl,
-                                          yh, yl, zh, zl, near_lim, cut2, ax, ay, az, near_mask, lane);
-            else
-                mixed_slice<false, SCREEN>(a, tile, j0, q_begin, q_end, S.sp[b], S.sinkf, inv3M, S.R[b], S.rho[b], S.sink, si, xh,
-                                           xl, yh, yl, zh, zl, near_lim, cut2, ax, ay, az, near_mask, lane);
-            // near pairs of this slice: the double-float term (FP64-class accuracy on the FP32
-            // pipes), from the FP64 displacement for pairs closer than the split positions resolve
+            // the slice's largest mass, for the flag cutoffs
+            float mslice = q_begin + lane < q_end ? S.sp[b][q_begin + lane].zm.z : 0.0f;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1) mslice = fmaxf(mslice, __shfl_xor_sync(0xffffffffu, mslice, off));
+            float flag2[MX_R];
+            unsigned flags[MX_R];
 #pragma unroll
             for (int r = 0; r < MX_R; r++) {
-                unsigned m = near_mask[r];
-                if (!m) continue;
-                SplitPos sp;
-                sp.xy = make_float4(xh[r], xl[r], yh[r], yl[r]);
-                sp.zm = make_float4(zh[r], zl[r], 0.0f, 0.0f);
-                const float close2 = close_r2(sp);
-                while (m) {
-                    const int bit = __ffs(m) - 1;
-                    m &= m - 1;
-                    const SplitPos pj = S.sp[b][q_begin + bit];
-                    DF tx, ty, tz;
-                    float r2f;
-                    df_term(sp, pj, tx, ty, tz, r2f);
-                    if (r2f < close2) {
-                        const int j = j0 + q_begin + bit;
-                        const SinkD& sd = S.sink[lane + 32 * r];
-                        df_term_fp64(sd.x, sd.y, sd.z, g.px[j], g.py[j], g.pz[j], pj.zm.z, pj.zm.w, tx, ty, tz, r2f);
-                    }
-                    acc_df(ax[r], tx);
-                    acc_df(ay[r], ty);
-                    acc_df(az[r], tz);
+                const float2 nl = S.near_lim[lane + 32 * r];
+                flag2[r] = flag_cut2(mslice, nl.x, nl.y, S.sinkf[lane + 32 * r].w);
+            }
+            mixed_slice(S.sp[b], q_begin, q_end, xh, xl, yh, yl, zh, zl, flag2, ax, ay, az, flags);
+            // The flagged pairs, shared out over the warp: each round, the lanes list up to 32
+            // of their items (in row, source order) at an exclusive prefix of their counts,
+            // each lane computes one listed item, and the owners add the round's terms in
+            // their listing order -- the same order as a lane walking its own items.
+            int cnt = 0;
+#pragma unroll
+            for (int r = 0; r < MX_R; r++) cnt += __popc(flags[r]);
+            while (__any_sync(0xffffffffu, cnt > 0)) {
+                int incl = cnt;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const int v = __shfl_up_sync(0xffffffffu, incl, d);
+                    if (lane >= d) incl += v;
                 }
+                const int off = incl - cnt;
+                const int n_items = min(32, __shfl_sync(0xffffffffu, incl, 31));
+                int take = max(0, min(cnt, 32 - off));
+                cnt -= take;
+                int taken[MX_R];
+                int k = off;
+#pragma unroll
+                for (int r = 0; r < MX_R; r++) {
+                    taken[r] = 0;
+                    while (take > 0 && flags[r]) {
+                        const int bit = __ffs(flags[r]) - 1;
+                        flags[r] &= flags[r] - 1;
+                        S.fitem[warp][k++] = (unsigned short)((lane << 7) | (r << 5) | bit);
+                        taken[r]++;
+                        take--;
+                    }
+                }
+                __syncwarp();
+                if (lane < n_items) {
+                    const unsigned it = S.fitem[warp][lane];
+                    const int s = (int)(it >> 7) + 32 * (int)((it >> 5) & 3u);
+                    const int q = q_begin + (int)(it & 31u);
+                    S.fterm[warp][lane] = mixed_flag_term<SCREEN>(a, tile, tile.sink_begin + s, j0 + q, q, S.sp[b], S.R[b],
+                                                                  S.rho[b], S.sinkf[s], S.sink[s], S.sinksp[s],
+                                                                  S.near_lim[s].x, inv3M);
+                }
+                __syncwarp();
+                k = off;
+#pragma unroll
+                for (int r = 0; r < MX_R; r++) {
+                    for (int u = 0; u < taken[r]; u++, k++) {
+                        const FlagTerm f = S.fterm[warp][k];
+                        acc_df(ax[r], DF{f.hx, f.lx});
+                        acc_df(ay[r], DF{f.hy, f.ly});
+                        acc_df(az[r], DF{f.hz, f.lz});
+                    }
+                }
+                __syncwarp();  // the round's lists are read before the next round writes them
             }
         }
         __syncthreads();  // buffer b is free; the fail flag is visible
