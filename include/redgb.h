@@ -196,8 +196,11 @@ RG_API int rg_calc_accel(rg_ctx* ctx, rg_vec_t* a);
  * evaluation in the current gravity mode on the current state (`reps` evaluations each,
  * CUDA events on the context's stream) and keeps the fastest.  FP64 mode: sinks per
  * pair-parallel CTA x the row-kernel source limit -- every candidate sums in the same
- * order, so results stay bit-exact; mixed mode: source chunks x the row-kernel limit.
- * Counters are left as they were.  `out` (may be NULL) receives the choice.
+ * order, so results stay bit-exact; mixed mode: first the row-kernel limit, then the mixed
+ * kernel's sources per grid.y chunk (whole tiles of 256 sources: for each chunk count up to
+ * 24 the smallest chunk that gives it and one tile less, so that the grid's last wave of
+ * CTAs can be filled; reported in `mixed_chunks`, 0 = from the SM count).  Counters are left
+ * as they were.  `out` (may be NULL) receives the choice.
  */
 RG_API int rg_autotune(rg_ctx* ctx, int reps, rg_tune_t* out);
 

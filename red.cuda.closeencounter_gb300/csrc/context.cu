@@ -53,6 +53,9 @@ struct rg_ctx {
     int device = 0;
     // device
     cudaStream_t st = nullptr;
+    // the double-float rows (star, giants) run on st2 beside the mixed kernel on st
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     double* d_y = nullptr;     // 6 rows: r, v
     double* d_yout = nullptr;  // 6 rows
     double* d_k[13] = {};      // 6 rows each: dr/dt (stage velocities), dv/dt
@@ -93,7 +96,8 @@ struct rg_ctx {
     int gravity_mode = RG_GRAVITY_FP64;
     int pairpar_S = 16;
     int rowseq_max_src = 64;
-    int mixed_chunks = 0;  // source chunks of the mixed kernel (0: from the SM count)
+    int mixed_chunk_src = 0;  // sources per grid.y chunk of the mixed kernel, a multiple of
+                              // MIXED_SOURCE_TILE (0: from the SM count)
     float near_ratio = 1.0e-5f;
     int hold_tile_copies = 0;  // test hook (rg_test_hold_tile_copies)
     // integrator
@@ -207,6 +211,9 @@ void free_all(rg_ctx* c)
     cudaFree(c->d_records);
     if (c->h_pin) cudaFreeHost(c->h_pin);
     for (auto e : c->ev_pool) cudaEventDestroy(e);
+    if (c->st2) cudaStreamDestroy(c->st2);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->st) cudaStreamDestroy(c->st);
 }
 
@@ -494,6 +501,22 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
     c->n_pairs += c->pairs_per_eval;
     const long prof = prof_begin(c, 0);
     bool split_done = false;
+    // with a mixed group, the double-float row groups (a few sinks: star, giants) run on a
+    // side stream beside it: they write other rows and append events atomically
+    bool fork = false;
+    if (c->gravity_mode == RG_GRAVITY_MIXED && mixed_tiles)
+        for (const auto& gr : c->plan[1]) fork = fork || gr.kind == GROUP_DF_ROWSEQ || gr.kind == GROUP_DF_FEW;
+    if (fork) {
+        rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, nullptr, c->d_screen_slot, c->d_radius,
+                                    c->n_total(), (SplitPos*)c->d_split, c->d_rf, g.smax ? c->d_smax : nullptr,
+                                    g.hill != 0, c->st);
+        if (rc) return rc;
+        split_done = true;
+        c->n_kernels++;
+        RG_CUDA_CHECK(cudaEventRecord(c->ev_fork, c->st));
+        RG_CUDA_CHECK(cudaStreamWaitEvent(c->st2, c->ev_fork, 0));
+    }
+    const cudaStream_t row_st = fork ? c->st2 : c->st;
     for (const auto& gr : c->plan[c->gravity_mode == RG_GRAVITY_MIXED ? 1 : 0]) {
         g.tiles = c->d_tiles + gr.off;
         g.n_tiles = gr.n;
@@ -522,13 +545,13 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
             }
             if (rc) break;
             if (gr.kind == GROUP_DF_ROWSEQ) {
-                rc = launch_grav_df_rowseq(g, c->d_split, c->st);
+                rc = launch_grav_df_rowseq(g, c->d_split, row_st);
                 c->n_kernels++;
             } else {
                 rc = launch_grav_df_few(g, c->d_split, c->d_few_row0 + gr.off, gr.max_src, gr.max_sinks, 0, c->d_terms,
                                         c->few_rows,
                                         c->few_pitch, c->d_row_sink, c->d_row_nsrc, nullptr, gr.row_base, gr.rows,
-                                        c->st);
+                                        row_st);
                 c->n_kernels += 2;
             }
             break;
@@ -543,12 +566,15 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
             if (!rc) {
                 // split the sources over grid.y so that about 4 CTAs per SM are in flight
                 const int src = c->tiles[gr.off].src_end - c->tiles[gr.off].src_begin;
-                int chunks = c->mixed_chunks > 0
-                                 ? std::min(c->mixed_chunks, std::max(1, src / MIXED_SOURCE_TILE))
-                                 : std::max(1, std::min((4 * c->n_sm + gr.n - 1) / gr.n, src / (4 * MIXED_SOURCE_TILE)));
-                const int chunk = ((src + chunks - 1) / chunks + MIXED_SOURCE_TILE - 1) / MIXED_SOURCE_TILE *
-                                  MIXED_SOURCE_TILE;
-                chunks = (src + chunk - 1) / chunk;
+                const int src_tiles = (src + MIXED_SOURCE_TILE - 1) / MIXED_SOURCE_TILE;
+                int chunk;
+                if (c->mixed_chunk_src > 0) {
+                    chunk = std::min(c->mixed_chunk_src, src_tiles * MIXED_SOURCE_TILE);
+                } else {
+                    const int n = std::max(1, std::min((4 * c->n_sm + gr.n - 1) / gr.n, src / (4 * MIXED_SOURCE_TILE)));
+                    chunk = (src_tiles + n - 1) / n * MIXED_SOURCE_TILE;
+                }
+                const int chunks = (src + chunk - 1) / chunk;
                 if (chunks > 1 && (size_t)chunks * 3 * c->cap > c->partial_cap) {
                     cudaFree(c->d_partial);
                     c->d_partial = nullptr;
@@ -564,8 +590,13 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
             c->n_kernels++;
             break;
         }
-        if (rc) return rc;
+        if (rc) break;
     }
+    if (fork) {  // joined on every path, so that no row kernel outlives the call's stream order
+        RG_CUDA_CHECK(cudaEventRecord(c->ev_join, c->st2));
+        RG_CUDA_CHECK(cudaStreamWaitEvent(c->st, c->ev_join, 0));
+    }
+    if (rc) return rc;
     prof_end(c, prof);
     return rc;
 }
@@ -1278,6 +1309,10 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
         if (!rc) rc = x;
     };
     if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess) chk(set_error(RG_ERR_CUDA, "stream"));
+    if (!rc && (cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking) != cudaSuccess ||
+                cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+                cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess))
+        chk(set_error(RG_ERR_CUDA, "stream"));
     chk(dalloc(&c->d_y, (size_t)6 * nt));
     chk(dalloc(&c->d_yout, (size_t)6 * nt));
     for (auto& k : c->d_k) chk(dalloc(&k, (size_t)6 * nt));
@@ -1623,46 +1658,69 @@ static int time_evaluations(rg_ctx* c, int reps, double* ms)
     return RG_OK;
 }
 
+// Mixed mode tunes in two stages: the row-kernel limit with the current chunking, then the
+// mixed kernel's chunk size.  Chunk candidates: for every chunk count n up to 24, the
+// smallest whole number of source tiles that gives n chunks and one tile less, so that the
+// tuner can pick the grid whose last wave of CTAs is best filled.
 static int autotune_impl(rg_ctx* c, int reps, rg_tune_t* out)
 {
     struct Shape {
-        int S, rowseq, chunks;
+        int S, rowseq, chunk_src;
     };
-    std::vector<Shape> cand;
     const int rows[3] = {32, 64, 128};
-    if (c->gravity_mode == RG_GRAVITY_MIXED) {
-        const int ch[5] = {0, 1, 2, 4, 8};
-        for (int r : rows)
-            for (int k : ch) cand.push_back({c->pairpar_S, r, k});
-    } else {
-        const int ss[3] = {8, 16, 32};
-        for (int r : rows)
-            for (int S : ss) cand.push_back({S, r, c->mixed_chunks});
-    }
     // tuning evaluations leave the counters as they were
     const int64_t evals = c->n_gravity_evals, pairs = c->n_pairs, kernels = c->n_kernels;
-    const Shape before{c->pairpar_S, c->rowseq_max_src, c->mixed_chunks};
+    const Shape before{c->pairpar_S, c->rowseq_max_src, c->mixed_chunk_src};
     double ms_before = 0.0, best_ms = 0.0;
     int rc = time_evaluations(c, reps, &ms_before);
     Shape best = before;
     best_ms = ms_before;
-    for (const Shape& sh : cand) {
-        if (rc) break;
-        c->pairpar_S = sh.S;
-        c->rowseq_max_src = sh.rowseq;
-        c->mixed_chunks = sh.chunks;
-        build_tiles(c);
-        double ms = 0.0;
-        rc = time_evaluations(c, reps, &ms);
-        if (!rc && ms < best_ms) {
-            best_ms = ms;
-            best = sh;
+    int n_cand = 0;
+    auto run = [&](const std::vector<Shape>& cand) {
+        for (const Shape& sh : cand) {
+            if (rc) break;
+            c->pairpar_S = sh.S;
+            c->rowseq_max_src = sh.rowseq;
+            c->mixed_chunk_src = sh.chunk_src;
+            build_tiles(c);
+            double ms = 0.0;
+            rc = time_evaluations(c, reps, &ms);
+            n_cand++;
+            if (!rc && ms < best_ms) {
+                best_ms = ms;
+                best = sh;
+            }
         }
+        c->pairpar_S = best.S;
+        c->rowseq_max_src = best.rowseq;
+        c->mixed_chunk_src = best.chunk_src;
+        build_tiles(c);
+    };
+    std::vector<Shape> cand;
+    if (c->gravity_mode == RG_GRAVITY_MIXED) {
+        for (int r : rows) cand.push_back({c->pairpar_S, r, c->mixed_chunk_src});
+        run(cand);
+        int src_tiles = 0;  // the largest mixed group's sources, in tiles
+        for (const auto& gr : c->plan[1])
+            if (gr.kind == GROUP_MIXED)
+                src_tiles = std::max(src_tiles, (c->tiles[gr.off].src_end - c->tiles[gr.off].src_begin +
+                                                 MIXED_SOURCE_TILE - 1) / MIXED_SOURCE_TILE);
+        std::vector<int> ks;
+        for (int n = 1; n <= 24 && src_tiles > 0; n++) {
+            const int k = (src_tiles + n - 1) / n;
+            for (int kk : {k, k - 1})
+                if (kk >= 1 && std::find(ks.begin(), ks.end(), kk) == ks.end()) ks.push_back(kk);
+        }
+        cand.clear();
+        cand.push_back({best.S, best.rowseq, 0});
+        for (int k : ks) cand.push_back({best.S, best.rowseq, k * MIXED_SOURCE_TILE});
+        run(cand);
+    } else {
+        const int ss[3] = {8, 16, 32};
+        for (int r : rows)
+            for (int S : ss) cand.push_back({S, r, c->mixed_chunk_src});
+        run(cand);
     }
-    c->pairpar_S = best.S;
-    c->rowseq_max_src = best.rowseq;
-    c->mixed_chunks = best.chunks;
-    build_tiles(c);
     c->n_gravity_evals = evals;
     c->n_pairs = pairs;
     c->n_kernels = kernels;
@@ -1670,8 +1728,8 @@ static int autotune_impl(rg_ctx* c, int reps, rg_tune_t* out)
     if (out) {
         out->pairpar_sinks = best.S;
         out->rowseq_max_src = best.rowseq;
-        out->mixed_chunks = best.chunks;
-        out->candidates = (int32_t)cand.size();
+        out->mixed_chunks = best.chunk_src;
+        out->candidates = (int32_t)n_cand;
         out->ms_per_eval = best_ms;
         out->ms_before = ms_before;
     }

@@ -29,7 +29,13 @@ def test_mixed_autotune_keeps_force_error(gpulib):
     ref = s.calc_accel()
     s.set_gravity_mode(T.GRAVITY_MIXED)
     t = s.autotune(reps=2)
-    assert t["candidates"] == 15 and t["mixed_chunks"] in (0, 1, 2, 4, 8)
+    # 3 row limits, then 0 (automatic) and the chunk sizes in tiles of 256 sources: for each
+    # chunk count up to 24, the smallest size giving it and one tile less
+    tiles = -(-disk.n_total // 256)
+    sizes = {k for n in range(1, 25) for k in (-(-tiles // n), -(-tiles // n) - 1) if k >= 1}
+    assert t["candidates"] == 3 + 1 + len(sizes)
+    assert t["mixed_chunks"] == 0 or t["mixed_chunks"] // 256 in sizes
+    assert t["ms_per_eval"] <= t["ms_before"] * 1.001
     am = s.calc_accel()
     a_m = np.stack([am[f] for f in "xyz"], 1)
     a_e = np.stack([ref[f] for f in "xyz"], 1)
