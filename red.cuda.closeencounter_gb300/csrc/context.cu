@@ -73,10 +73,13 @@ struct rg_ctx {
     unsigned int* d_smax = nullptr;  // the screens' maxima (split_positions)
     int* d_screen_slot = nullptr;    // per body: 0 for a light body, -1 for a heavy one
     DevEvent* d_ev = nullptr;
-    unsigned int* d_ev_count = nullptr;
     DevEvent* d_hill = nullptr;
-    unsigned int* d_hill_count = nullptr;
-    unsigned int* d_kerr = nullptr;  // set by a gravity kernel whose tile copy timed out
+    // one allocation, read back by one copy per step: [0] events, [1] Hill events, [2] set by
+    // a gravity kernel whose tile copy timed out
+    unsigned int* d_counters = nullptr;
+    unsigned int* d_ev_count = nullptr;    // d_counters + 0
+    unsigned int* d_hill_count = nullptr;  // d_counters + 1
+    unsigned int* d_kerr = nullptr;        // d_counters + 2
     unsigned int ev_cap = 0;
     EjectRec* d_ej = nullptr;
     unsigned int* d_ej_count = nullptr;
@@ -84,7 +87,7 @@ struct rg_ctx {
     double* d_dt = nullptr;
     double* d_part = nullptr;
     double* d_records = nullptr;  // r and v as vec_t records (state in / out): 8 doubles per body
-    double* h_pin = nullptr;  // pinned: [0] dt, [1] max bits, [2..3] counts
+    double* h_pin = nullptr;  // pinned: [0] dt, [1] max bits, [2..3] counts, [4..5] d_counters
     // host mirrors of the body parameters (authoritative; the state lives on the device)
     std::vector<rg_param_t> p;
     std::vector<rg_body_metadata_t> md;
@@ -199,10 +202,8 @@ void free_all(rg_ctx* c)
     cudaFree(c->d_row_nsrc);
     cudaFree(c->d_few_row0);
     cudaFree(c->d_ev);
-    cudaFree(c->d_ev_count);
     cudaFree(c->d_hill);
-    cudaFree(c->d_hill_count);
-    cudaFree(c->d_kerr);
+    cudaFree(c->d_counters);
     cudaFree(c->d_ej);
     cudaFree(c->d_ej_count);
     cudaFree(c->d_maxbits);
@@ -650,11 +651,11 @@ int kernel_flag_error(rg_ctx* c, unsigned int flag)
 // order its CPU loop creates them: stage by stage, sink i, source j ascending.
 int collect_events(rg_ctx* c)
 {
-    unsigned int counts[3] = {0, 0, 0};
-    RG_CUDA_CHECK(cudaMemcpyAsync(&counts[0], c->d_ev_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->st));
-    RG_CUDA_CHECK(cudaMemcpyAsync(&counts[1], c->d_hill_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->st));
-    RG_CUDA_CHECK(cudaMemcpyAsync(&counts[2], c->d_kerr, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->st));
+    // the three counters in one copy to pinned memory: one round trip per step
+    unsigned int* const h_counts = reinterpret_cast<unsigned int*>(&c->h_pin[4]);
+    RG_CUDA_CHECK(cudaMemcpyAsync(h_counts, c->d_counters, 3 * sizeof(unsigned int), cudaMemcpyDeviceToHost, c->st));
     RG_CUDA_CHECK(cudaStreamSynchronize(c->st));
+    const unsigned int counts[3] = {h_counts[0], h_counts[1], h_counts[2]};
     if (int krc = kernel_flag_error(c, counts[2])) return krc;
     const int nsi = c->n_si();
     for (int kind = 0; kind < 2; kind++) {
@@ -823,8 +824,7 @@ int ytemp_stage(rg_ctx* c, int form, int r, const int* stages, const double* coe
 int stage_zero(rg_ctx* c)
 {
     const size_t cap = (size_t)c->cap;
-    RG_CUDA_CHECK(cudaMemsetAsync(c->d_ev_count, 0, sizeof(unsigned int), c->st));
-    RG_CUDA_CHECK(cudaMemsetAsync(c->d_hill_count, 0, sizeof(unsigned int), c->st));
+    RG_CUDA_CHECK(cudaMemsetAsync(c->d_ev_count, 0, 2 * sizeof(unsigned int), c->st));  // and d_hill_count
     if (c->n_total() > 0)
         RG_CUDA_CHECK(cudaMemcpyAsync(c->d_k[0], c->d_y + 3 * cap, 3 * cap * sizeof(double),
                                       cudaMemcpyDeviceToDevice, c->st));
@@ -1323,11 +1323,14 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
     chk(dalloc(&c->d_type, nt));
     chk(dalloc(&c->d_rho, nt));
     chk(dalloc(&c->d_ev, c->ev_cap));
-    chk(dalloc(&c->d_ev_count, 1));
     chk(dalloc(&c->d_hill, c->ev_cap));
-    chk(dalloc(&c->d_hill_count, 1));
-    chk(dalloc(&c->d_kerr, 1));
-    if (!rc && cudaMemset(c->d_kerr, 0, sizeof(unsigned int)) != cudaSuccess)
+    chk(dalloc(&c->d_counters, 4));
+    if (!rc) {
+        c->d_ev_count = c->d_counters;
+        c->d_hill_count = c->d_counters + 1;
+        c->d_kerr = c->d_counters + 2;
+    }
+    if (!rc && cudaMemset(c->d_counters, 0, 4 * sizeof(unsigned int)) != cudaSuccess)
         chk(set_error(RG_ERR_CUDA, "cudaMemset"));
     chk(dalloc(&c->d_ej, nt));
     chk(dalloc(&c->d_ej_count, 1));
