@@ -1330,8 +1330,8 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
         c->d_hill_count = c->d_counters + 1;
         c->d_kerr = c->d_counters + 2;
     }
-    if (!rc && cudaMemset(c->d_counters, 0, 4 * sizeof(unsigned int)) != cudaSuccess)
-        chk(set_error(RG_ERR_CUDA, "cudaMemset"));
+    if (!rc && cudaMemsetAsync(c->d_counters, 0, 4 * sizeof(unsigned int), c->st) != cudaSuccess)
+        chk(set_error(RG_ERR_CUDA, "cudaMemsetAsync"));
     chk(dalloc(&c->d_ej, nt));
     chk(dalloc(&c->d_ej_count, 1));
     chk(dalloc(&c->d_maxbits, 1));

@@ -14,9 +14,9 @@
 //    force evaluation (split_positions, O(N) integer work).  The displacement is
 //    (x_j^hi - x_i^hi) + (x_j^lo - x_i^lo): the hi difference is exact for neighbours
 //    (Sterbenz), so the displacement carries the FP64 positions' information down to
-//    FP32 resolution of the displacement itself.  1/r comes from the FP32 rsqrt refined
-//    by one Newton step, and each warp-slice's 32 terms are summed in FP32 and folded into compensated
-//    (two-sum) FP32 accumulators per component.
+//    FP32 resolution of the displacement itself.  1/r^3 comes from the FP32 rsqrt with a
+//    first-order correction taken on r^-3 (light_w), and each warp-slice's 32 terms are
+//    summed in FP32 and folded into compensated (two-sum) FP32 accumulators per component.
 //  * Event tests (collision radius, Hill sphere) are re-evaluated in FP64 for every pair
 //    whose FP32 distance is within a 1e-3 relative margin of a threshold, so the event
 //    list is decided in FP64 exactly as in the FP64 kernel.
@@ -165,6 +165,18 @@ __device__ __forceinline__ float rsqrt_approx(float x)
     float y;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
+}
+
+// m r^-3 of a light pair from the FP32 rsqrt seed y0 = r^-1 (1 + d): with s = y0^2,
+// y0^3 (2.5 - 1.5 r^2 s) = r^-3 (1 - 7.5 d^2 + O(d^3)) -- the first-order correction taken on
+// y^3 itself, one multiplication fewer than a Newton step on y followed by y^3; |d| < 2^-22,
+// so the truncation (~2e-13) is far below the FP32 rounding of the term.
+__device__ __forceinline__ float light_w(float mj, float r2)
+{
+    const float y0 = rsqrt_approx(r2);
+    const float s = y0 * y0;
+    const float t = fmaf(-1.5f * r2, s, 2.5f);
+    return (mj * (y0 * s)) * t;
 }
 
 // compensated accumulation: s + c tracks the exact sum of the added terms to ~2^-46
@@ -512,10 +524,7 @@ __device__ __forceinline__ void mixed_slice(const SplitPos* s_sp, int q_begin, i
             // finite: split_positions clamps coordinates to 1e15 AU
             const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
             const bool flag = r2 < flag2[r];
-            const float y0 = rsqrt_approx(r2);
-            const float hr2 = 0.5f * r2;
-            const float y = y0 * fmaf(-hr2, y0 * y0, 1.5f);
-            const float w = flag ? 0.0f : mj * (y * y * y);
+            const float w = flag ? 0.0f : light_w(mj, r2);
             px[r] = fmaf(w, dx, px[r]);
             py[r] = fmaf(w, dy, py[r]);
             pz[r] = fmaf(w, dz, pz[r]);
@@ -563,9 +572,7 @@ __device__ __forceinline__ FlagTerm mixed_flag_term(const MixedArgs& a, const Ti
             df_term_fp64(sd.x, sd.y, sd.z, g.px[j], g.py[j], g.pz[j], mj, pj.zm.w, tx, ty, tz, r2f);
         f = FlagTerm{tx.hi, tx.lo, ty.hi, ty.lo, tz.hi, tz.lo};
     } else {
-        const float y0 = rsqrt_approx(r2);
-        const float y = y0 * fmaf(-0.5f * r2, y0 * y0, 1.5f);
-        const float w = mj * (y * y * y);
+        const float w = light_w(mj, r2);
         f.hx = w * dx;
         f.hy = w * dy;
         f.hz = w * dz;
