@@ -26,6 +26,7 @@
 // Sources are staged in shared memory as FP32 (hi, lo) quads; the per-warp compensated
 // partial sums are added in FP64 at the end.
 #include <algorithm>
+#include <atomic>
 #include <string>
 
 #include "../../include/redgb.h"
@@ -1185,11 +1186,15 @@ int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* hea
 {
     if (g.n_tiles <= 0) return 0;
     constexpr int smem = (int)sizeof(MixedSmem);
-    static bool attr_set = false;
-    if (!attr_set) {
+    // the shared-memory opt-in is a per-device attribute of each kernel: set once per device
+    // (setting it again from another thread is harmless)
+    static std::atomic<bool> attr_set[64];
+    int dev = 0;
+    RG_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64 || !attr_set[dev].load(std::memory_order_acquire)) {
         RG_CUDA_CHECK(cudaFuncSetAttribute(grav_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         RG_CUDA_CHECK(cudaFuncSetAttribute(grav_mixed_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        attr_set = true;
+        if (dev >= 0 && dev < 64) attr_set[dev].store(true, std::memory_order_release);
     }
     MixedArgs a;
     a.err = err;

@@ -69,6 +69,23 @@ def test_mixed_close_pairs_force_error(gpulib):
     assert mx < MAX_REL and rms < RMS_REL
 
 
+def test_mixed_crowded_clump_force_error(gpulib):
+    """256 self-gravitating bodies within 5e-4 AU of one point: every pair of the clump is a
+    near pair, so a warp-slice over the clump flags up to 32 x 128 pairs (self pairs included)
+    and the kernel's exact pass runs many rounds of 32 shared items; the clump's own pairs
+    take the double-float term from FP64 displacements."""
+    disk = bodies.config_disk("self_gravitating", n=4096)
+    rng = np.random.default_rng(7)
+    centre = [float(disk.r[f][1000]) for f in "xyz"]
+    for k in range(100, 356):
+        off = rng.uniform(-5e-4, 5e-4, 3)
+        for f, o, c in zip("xyz", off, centre):
+            disk.r[f][k] = c + o
+    mx, rms, _, _ = force_error(disk)
+    print(f"crowded clump: max rel {mx:.3e} rms rel {rms:.3e}")
+    assert mx < MAX_REL and rms < RMS_REL
+
+
 def test_mixed_planetesimal_events_from_the_heavy_rows(gpulib):
     """Planetesimals (NSI) against the star and the giants in the double-float kernels (the
     giants' rows in the few-sink kernel, the planetesimals' rows in the row kernel, each with
