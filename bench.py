@@ -47,7 +47,7 @@ FLOP_PER_PAIR = 36  # the reference's own count (pp_disk.cu:170-184,293)
 # one ncu capture of `python bench.py --no-ensemble --no-dense-ring --no-cpu-baseline --no-autotune
 # --steps 3 --warmup 3`
 # (profiles/grav_mixed_kernel_self_gravitating_16384.md, .../grav_fp64_pairpar_...md)
-NCU_TRAFFIC = {("self_gravitating_16384_rk4", "mixed"): 1333248, ("self_gravitating_16384_rk4", "fp64"): 819712}
+NCU_TRAFFIC = {("self_gravitating_16384_rk4", "mixed"): 1332224, ("self_gravitating_16384_rk4", "fp64"): 819712}
 
 
 def dist_init():
