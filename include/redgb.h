@@ -215,6 +215,38 @@ RG_API int rg_autotune(rg_ctx* ctx, int reps, rg_tune_t* out);
 RG_API int rg_generate_disks(int n_sys, const rg_disk_spec_t* specs, rg_counts_t* counts, rg_vec_t* r,
                              rg_vec_t* v, rg_param_t* p, rg_body_metadata_t* md);
 
+/*
+ * Disks from per-body-type distributions, on the GPU: the reference's initial-condition
+ * program (red.cuda.initial populate_disk, main.cu:29-86, and its driver, main.cu:470-538)
+ * for many disks at once.  Per body: the physical properties (mass, radius, density, drag
+ * coefficient) from their distributions, the one of mass, radius and density that is not
+ * given derived from the other two (tools.cpp:238-261; superplanetesimals keep what they
+ * drew); the orbital elements (the star: all 0).  Per disk, when pp_total_mass > 0: the
+ * protoplanets' masses scaled to that sum (summed from the last body down, as
+ * tools::get_total_mass does) and their radius or density derived again.  Then positions
+ * and velocities by calculate_phase with mu = k^2 (m_0 + m_i), m_0 the disk's first body,
+ * which sits at rest in the origin; with to_bc the disk is moved to its barycentre
+ * (tools::transform_to_bc).  Draws: Philox4x32-10 keyed by the disk's seed, counter (body
+ * slot, item, attempt), so a disk does not depend on its batch.  The power law repeats the
+ * reference's rejection steps (at most 10 000 attempts); the lognormal, whose rejection in
+ * the reference samples the true truncated density, is drawn by its inverse distribution
+ * function.  The reference's element ranges are not part of the spec, since its redraw
+ * condition (util_init.cpp:61-69) can never hold.  Disk s gets the records
+ * [off_s, off_s + n_s) of r, v (AU, AU/day), p and md (ids 1..n_s) and counts[s].
+ * RG_ERR_ARG: an invalid distribution, a body type with other than exactly one of mass,
+ * radius and density missing ("Missing physical parameters!" in the reference), a phase the
+ * Kepler solver does not converge for, a mass scaling that misses its target by more than
+ * 1e-15 (the reference's own checks), or a power-law draw that reached its attempt limit.
+ */
+RG_API int rg_populate_disks(int n_sys, const rg_body_disk_t* disks, rg_counts_t* counts, rg_vec_t* r,
+                             rg_vec_t* v, rg_param_t* p, rg_body_metadata_t* md);
+
+/* Masses of a minimum-mass solar nebula's gas and solids (Hayashi 1981; red.cuda.initial
+ * nebula.cpp:23-95): the integral of 2 pi r Sigma(r), Sigma = f_neb Sigma_1 r^p times the gas
+ * ratio (gas) or, beyond the snow line, the ice factor (solids), over [r_1, r_2]. */
+RG_API int rg_mmsn_gas_mass(const rg_mmsn_component_t* c, double* m);
+RG_API int rg_mmsn_solid_mass(const rg_mmsn_component_t* c, double* m);
+
 /* Test hook for the failure path (no counterpart in the reference): with `on`, the mixed
  * kernel issues none of its tile copies, so each CTA's bounded wait (one second of the GPU's
  * global timer) runs out; the evaluation then reports RG_ERR_CUDA ("a gravity tile copy did

@@ -88,6 +88,55 @@ typedef struct rg_disk_spec {
     double   rho_pl;         /* planetesimal density [g/cm^3]                                 */
 } rg_disk_spec_t;
 
+/* The distributions of the reference's initial-condition program (red.cuda.initial
+ * distribution.h:34-119), one per orbital element and physical property of a body type.
+ * Parameters by kind (u uniform on (0, 1]):                                                */
+enum {
+    RG_DIST_NONE = 0,        /* not given: the element is 0; of mass, radius and density the
+                                one not given is derived from the other two               */
+    RG_DIST_UNIFORM = 1,     /* p[0] x_min, p[1] x_max: x_min + (x_max - x_min) u           */
+    RG_DIST_EXPONENTIAL = 2, /* p[0] lambda: -log(u) / lambda                               */
+    RG_DIST_RAYLEIGH = 3,    /* p[0] sigma: sigma sqrt(-2 log u)                            */
+    RG_DIST_NORMAL = 4,      /* p[0] mean, p[1] scale (the reference calls it variance):
+                                mean + scale sqrt(-2 log u) cos(2 pi u')                   */
+    RG_DIST_POWER_LAW = 5,   /* p[0] x_min > 0, p[1] x_max, p[2] power: the reference's
+                                rejection steps, density ~ x^power - min(x_min^power,
+                                x_max^power)                                               */
+    RG_DIST_LOGNORMAL = 6,   /* p[0] x_min, p[1] x_max, p[2] mu, p[3] sigma: lognormal
+                                density truncated to [x_min, x_max]                        */
+    RG_DIST_LOG_UNIFORM = 7  /* p[0] x_min > 0, p[1] x_max (not in the reference)          */
+};
+typedef struct rg_dist {
+    int32_t kind;
+    int32_t pad;
+    double  p[4];
+} rg_dist_t;
+
+enum { RG_OE_SMA = 0, RG_OE_ECC = 1, RG_OE_INC = 2, RG_OE_PERI = 3, RG_OE_NODE = 4, RG_OE_MEAN = 5, RG_OE_N = 6 };
+enum { RG_PP_MASS = 0, RG_PP_RADIUS = 1, RG_PP_DENSITY = 2, RG_PP_DRAG_COEFF = 3, RG_PP_N = 4 };
+
+/* one disk for rg_populate_disks (red.cuda.initial's body_disk_t, main.cu:29-86 and the
+ * driver steps of main.cu:470-538) */
+typedef struct rg_body_disk {
+    uint64_t  seed;                 /* key of the disk's Philox4x32-10 streams                */
+    int32_t   n_body[7];            /* per body type, the reference's order (star first)      */
+    int32_t   to_bc;                /* 1: move the disk to its barycentre (transform_to_bc)   */
+    double    pp_total_mass;        /* > 0: scale the protoplanets' masses to this sum [Msun]
+                                       and re-derive their radius or density                 */
+    rg_dist_t oe[7][RG_OE_N];       /* sma [AU], ecc, inc, peri, node, mean [rad]; star: none */
+    rg_dist_t pp[7][RG_PP_N];       /* mass [Msun], radius [AU], density [Msun/AU^3], cd      */
+} rg_body_disk_t;
+
+/* one component of a minimum-mass solar nebula (red.cuda.initial nebula.h:5-48) */
+typedef struct rg_mmsn_component {
+    double r_1, r_2;   /* inner and outer radius [AU]                                          */
+    double r_SL;       /* the snow line [AU]                                                   */
+    double f_neb;      /* nebular mass factor (1: the MMSN)                                    */
+    double Sigma_1;    /* surface density of solids at 1 AU [mass / AU^2]                     */
+    double f;          /* gas: the gas-to-dust ratio; solids: the ice condensation factor      */
+    double p;          /* profile index of the surface density                                 */
+} rg_mmsn_component_t;
+
 /* launch shape of a context's force evaluation (rg_autotune) */
 typedef struct rg_tune {
     int32_t pairpar_sinks;   /* FP64 mode: sinks per pair-parallel CTA (8, 16 or 32)             */

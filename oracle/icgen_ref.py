@@ -133,3 +133,179 @@ def generate(spec):
                                      2.0 * math.pi * uM)
         typ[k] = 6
     return r, v, m, R, rho, typ
+
+
+# ------------------------------------------------------------------ rg_populate_disks
+# Restatement of the GPU populate steps (csrc/icgen.cu), which follow the reference's
+# red.cuda.initial: populate_disk (main.cu:29-86), the mass scaling and re-derivation
+# (main.cu:472-509), the phases (main.cu:511-536) and tools::transform_to_bc
+# (tools.cpp:122-176).  Distributions: distribution.cpp:117-249, the lognormal density
+# sampled by its inverse distribution function and the power law by the reference's own
+# rejection steps.
+POP_ITEM0 = 16
+(DIST_NONE, DIST_UNIFORM, DIST_EXPONENTIAL, DIST_RAYLEIGH, DIST_NORMAL, DIST_POWER_LAW, DIST_LOGNORMAL,
+ DIST_LOG_UNIFORM) = range(8)
+BODY_STAR, BODY_PROTOPLANET, BODY_SUPERPLANETESIMAL = 0, 3, 4
+
+
+def draw2a(seed, k, blk, att):
+    """draw2 with the attempt counter (attempt 0 is draw2)."""
+    k = np.asarray(k, np.uint64)
+    c = philox4x32_10(k, np.full_like(k, blk), np.full_like(k, att), np.zeros_like(k), seed & 0xFFFFFFFF, seed >> 32)
+    return uniform53(c[0], c[1]), uniform53(c[2], c[3])
+
+
+def sample_dist(kind, p, seed, k, blk):
+    """One value per body slot k from draw block blk (see csrc/icgen.cu sample_dist)."""
+    from scipy.special import ndtr, ndtri
+    u0, u1 = draw2(seed, k, blk)
+    u = 1.0 - u0
+    if kind == DIST_UNIFORM:
+        return p[0] + (p[1] - p[0]) * u
+    if kind == DIST_EXPONENTIAL:
+        return -1.0 / p[0] * np.log(u)
+    if kind == DIST_RAYLEIGH:
+        return p[0] * np.sqrt(-2.0 * np.log(u))
+    if kind == DIST_NORMAL:
+        return p[0] + p[1] * np.sqrt(-2.0 * np.log(u)) * np.cos(2.0 * math.pi * (1.0 - u1))
+    if kind == DIST_POWER_LAW:  # the reference's rejection steps (distribution.cpp:187-207)
+        x0, x1, pw = p[0], p[1], p[2]
+        y_min = 0.0 if pw == 0.0 else math.pow(x0, pw)
+        y_max = 1.0 if pw == 0.0 else math.pow(x1, pw)
+        y_min, y_max = min(y_min, y_max), max(y_min, y_max)
+        d_y, d_x = y_max - y_min, x1 - x0
+        area_max = d_x * d_y
+        k = np.asarray(k)
+        if not d_y > 0.0:
+            return np.full(k.shape, x0)
+        out = np.full(k.shape, np.nan)
+        todo = np.ones(k.shape, bool)
+        for att in range(10000):
+            if att > 0:
+                u0, u1 = draw2a(seed, k, blk, att)
+            x = area_max * (1.0 - u0) / d_y + x0
+            y = y_min + (y_max - y_min) * (1.0 - u1)
+            ok = todo & ~(y > np.power(x, pw))
+            out[ok] = x[ok]
+            todo &= ~ok
+            if not todo.any():
+                return out
+        raise ValueError("a power-law draw reached its attempt limit")
+    if kind == DIST_LOGNORMAL:
+        x0, x1, mu, sg = p
+        c0 = ndtr((math.log(x0) - mu) / sg) if x0 > 0 else 0.0
+        c1 = ndtr((math.log(x1) - mu) / sg)
+        x = np.exp(mu + sg * ndtri(c0 + u0 * (c1 - c0)))
+        return np.minimum(np.maximum(x, x0), x1)
+    if kind == DIST_LOG_UNIFORM:
+        return np.exp(math.log(p[0]) + u0 * (math.log(p[1]) - math.log(p[0])))
+    return np.zeros_like(u0)
+
+
+def density_of(m, R):
+    """tools.cpp:245-254."""
+    R = np.asarray(R, np.float64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return np.where(R == 0.0, 0.0, m / (FOUR_PI_OVER_THREE * (R * R * R)))
+
+
+def mass_of(R, rho):
+    """tools.cpp:256-261."""
+    return FOUR_PI_OVER_THREE * (R * R * R) * rho
+
+
+def _protoplanet_mass(m, typ):
+    tot = 0.0
+    for j in range(len(m) - 1, -1, -1):  # tools::get_total_mass: from the last body down
+        if typ[j] == BODY_PROTOPLANET:
+            tot += float(m[j])
+    return tot
+
+
+def populate(disk):
+    """(r [n, 3], v [n, 3], mass, radius, density, cd, body type) of one BodyDisk (redgb.icgen);
+    raises ValueError where rg_populate_disks returns RG_ERR_ARG after drawing."""
+    n_body = list(disk.n_body)
+    n = int(sum(n_body))
+    typ = np.repeat(np.arange(7, dtype=np.int32), n_body)
+    k = np.arange(n)
+    pp = np.zeros((n, 4))
+    oe = np.zeros((n, 6))
+    for t in range(7):
+        idx = k[typ == t]
+        if idx.size == 0:
+            continue
+        items = disk.pp.get(t, {})
+        for e in range(4):
+            d = items.get(e)
+            if d is not None and d.kind != DIST_NONE:
+                pp[idx, e] = sample_dist(d.kind, d.p, disk.seed, idx, POP_ITEM0 + e)
+        if t != BODY_SUPERPLANETESIMAL:
+            hm, hr, hd = (items.get(e) is not None and items[e].kind != DIST_NONE for e in range(3))
+            if not hm and hr and hd:
+                pp[idx, 0] = mass_of(pp[idx, 1], pp[idx, 2])
+            elif not hr and hm and hd:
+                pp[idx, 1] = radius_of(pp[idx, 0], pp[idx, 2])
+            elif not hd and hm and hr:
+                pp[idx, 2] = density_of(pp[idx, 0], pp[idx, 1])
+        if t != BODY_STAR:
+            for e in range(6):
+                d = disk.oe.get(t, {}).get(e)
+                if d is not None and d.kind != DIST_NONE:
+                    oe[idx, e] = sample_dist(d.kind, d.p, disk.seed, idx, POP_ITEM0 + 4 + e)
+    m = pp[:, 0]
+    if disk.pp_total_mass > 0.0:
+        f = disk.pp_total_mass / _protoplanet_mass(m, typ)
+        m[typ == BODY_PROTOPLANET] *= f
+        if abs(_protoplanet_mass(m, typ) - disk.pp_total_mass) > 1.0e-15:
+            raise ValueError("the required mass was not reached")
+        for t in range(7):
+            sel = (typ == t) & (m > 0.0)
+            items = disk.pp.get(t, {})
+            hr = items.get(1) is not None and items[1].kind != DIST_NONE
+            hd = items.get(2) is not None and items[2].kind != DIST_NONE
+            if not hd and hr:
+                pp[sel, 2] = density_of(m[sel], pp[sel, 1])
+            if not hr and hd:
+                pp[sel, 1] = radius_of(m[sel], pp[sel, 2])
+    r, v = np.zeros((n, 3)), np.zeros((n, 3))
+    if n > 1:
+        mu = GAUSS2 * (m[0] + m[1:])
+        r[1:], v[1:] = calculate_phase(mu, *(oe[1:, e] for e in range(6)))
+    if disk.to_bc:
+        R0, V0, M0 = [0.0, 0.0, 0.0], [0.0, 0.0, 0.0], 0.0
+        for j in range(n - 1, -1, -1):  # compute_bc: from the last body down
+            mj = float(m[j])
+            for c in range(3):
+                R0[c] += mj * float(r[j, c])
+                V0[c] += mj * float(v[j, c])
+        for j in range(n - 1, -1, -1):
+            M0 += float(m[j])
+        r -= np.array([x / M0 for x in R0])
+        v -= np.array([x / M0 for x in V0])
+    return r, v, m, pp[:, 1], pp[:, 2], pp[:, 3], typ
+
+
+def mmsn_gas(r_1, r_2, r_SL, f_neb, Sigma_1, f_gas, p):
+    """nebula.cpp:23-46."""
+    p2 = p + 2.0
+    if p2 != 0.0:
+        return 2.0 * math.pi * f_neb * f_gas * Sigma_1 / p2 * (math.pow(r_2, p2) - math.pow(r_1, p2))
+    return 2.0 * math.pi * f_neb * f_gas * Sigma_1 * (math.log(r_2) - math.log(r_1))
+
+
+def mmsn_solid(r_1, r_2, r_SL, f_neb, Sigma_1, f_ice, p):
+    """nebula.cpp:63-95."""
+    p2 = p + 2.0
+    C = 2.0 * math.pi * f_neb * Sigma_1 / p2 if p2 != 0.0 else 2.0 * math.pi * f_neb * Sigma_1
+
+    def integral(a, b):
+        return math.pow(b, p2) - math.pow(a, p2) if p2 != 0.0 else math.log(b) - math.log(a)
+
+    if r_SL <= r_1:
+        I = f_ice * integral(r_1, r_2)
+    elif r_SL <= r_2:
+        I = integral(r_1, r_SL) + f_ice * integral(r_SL, r_2)
+    else:
+        I = integral(r_1, r_2)
+    return C * I

@@ -111,3 +111,194 @@ def generate_disks(specs):
         out.append(disk)
         o += n
     return out
+
+
+# ------------------------------------------------------------------ rg_populate_disks
+# The reference's initial-condition program (red.cuda.initial): per body type, one
+# distribution per orbital element and physical property (distribution.h, main.cu:29-86).
+(DIST_NONE, DIST_UNIFORM, DIST_EXPONENTIAL, DIST_RAYLEIGH, DIST_NORMAL, DIST_POWER_LAW, DIST_LOGNORMAL,
+ DIST_LOG_UNIFORM) = range(8)
+OE_SMA, OE_ECC, OE_INC, OE_PERI, OE_NODE, OE_MEAN = range(6)
+PP_MASS, PP_RADIUS, PP_DENSITY, PP_DRAG_COEFF = range(4)
+TYPE_NAMES = ("star", "giant", "rocky", "proto", "superpl", "pl", "testp")  # util_init.cpp:16-29
+
+# unit conversions of the reference's constants (red_constants.h): 1 Msun = 1.98911e33 g,
+# 1 AU = 1.495978707e11 m = 215.094 solar radii
+SOLAR_RADIUS_AU = 1.0 / 215.094
+_GRAM_TO_SOLAR = 1.0 / (1.0e3 * 1.98911e30)
+_CM_TO_AU = 1.0e-2 * (1.0 / 1.495978707e11)
+GRAM_PER_CM2 = _GRAM_TO_SOLAR / (_CM_TO_AU * _CM_TO_AU)              # g/cm^2 -> Msun/AU^2
+GRAM_PER_CM3 = _GRAM_TO_SOLAR / (_CM_TO_AU * _CM_TO_AU * _CM_TO_AU)  # g/cm^3 -> Msun/AU^3
+
+
+class DistC(ctypes.Structure):
+    """rg_dist_t."""
+    _fields_ = [("kind", ctypes.c_int32), ("pad", ctypes.c_int32), ("p", ctypes.c_double * 4)]
+
+
+class BodyDiskC(ctypes.Structure):
+    """rg_body_disk_t."""
+    _fields_ = [("seed", ctypes.c_uint64), ("n_body", ctypes.c_int32 * 7), ("to_bc", ctypes.c_int32),
+                ("pp_total_mass", ctypes.c_double), ("oe", (DistC * 6) * 7), ("pp", (DistC * 4) * 7)]
+
+
+class MmsnC(ctypes.Structure):
+    """rg_mmsn_component_t."""
+    _fields_ = [(f, ctypes.c_double) for f in ("r_1", "r_2", "r_SL", "f_neb", "Sigma_1", "f", "p")]
+
+
+@dataclasses.dataclass(frozen=True)
+class Dist:
+    """One distribution: `kind` (DIST_*) and its parameters (see rg_dist_t)."""
+    kind: int = DIST_NONE
+    p: tuple = ()
+
+
+def uniform(x_min, x_max):
+    return Dist(DIST_UNIFORM, (x_min, x_max))
+
+
+def exponential(lam):
+    return Dist(DIST_EXPONENTIAL, (lam,))
+
+
+def rayleigh(sigma):
+    return Dist(DIST_RAYLEIGH, (sigma,))
+
+
+def normal(mean, scale):
+    return Dist(DIST_NORMAL, (mean, scale))
+
+
+def power_law(x_min, x_max, power):
+    return Dist(DIST_POWER_LAW, (x_min, x_max, power))
+
+
+def lognormal(x_min, x_max, mu, sigma):
+    return Dist(DIST_LOGNORMAL, (x_min, x_max, mu, sigma))
+
+
+def log_uniform(x_min, x_max):
+    return Dist(DIST_LOG_UNIFORM, (x_min, x_max))
+
+
+@dataclasses.dataclass
+class BodyDisk:
+    """One disk for rg_populate_disks: body counts per type (the reference's order), and per
+    type {OE_*: Dist} and {PP_*: Dist}; what is not given is DIST_NONE."""
+    seed: int
+    n_body: tuple
+    oe: dict = dataclasses.field(default_factory=dict)
+    pp: dict = dataclasses.field(default_factory=dict)
+    pp_total_mass: float = 0.0
+    to_bc: bool = False
+
+    def to_c(self):
+        c = BodyDiskC()
+        c.seed = self.seed
+        for t in range(7):
+            c.n_body[t] = self.n_body[t]
+        c.to_bc = 1 if self.to_bc else 0
+        c.pp_total_mass = self.pp_total_mass
+        for table, field in ((self.oe, c.oe), (self.pp, c.pp)):
+            for t, items in table.items():
+                for e, d in items.items():
+                    field[t][e].kind = d.kind
+                    for q, x in enumerate(d.p):
+                        field[t][e].p[q] = x
+        return c
+
+    @property
+    def n_total(self):
+        return int(sum(self.n_body))
+
+    def names(self):
+        out = []
+        for t, n in enumerate(self.n_body):
+            out += ["star"] if (t == 0 and n == 1) else [f"{TYPE_NAMES[t]}{i + 1}" for i in range(n)]
+        return out
+
+
+def _bind_populate(L):
+    if getattr(L, "_populate_bound", False):
+        return L
+    vp = ctypes.c_void_p
+    L.rg_populate_disks.argtypes = [ctypes.c_int, vp, vp, vp, vp, vp, vp]
+    L.rg_populate_disks.restype = ctypes.c_int
+    for f in ("rg_mmsn_gas_mass", "rg_mmsn_solid_mass"):
+        getattr(L, f).argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+        getattr(L, f).restype = ctypes.c_int
+    L._populate_bound = True
+    return L
+
+
+def populate_disks(disks):
+    """One bodies.Disk per BodyDisk, drawn on the GPU (rg_populate_disks)."""
+    L = _bind_populate(lib.load())
+    disks = list(disks)
+    arr = (BodyDiskC * max(len(disks), 1))(*[d.to_c() for d in disks])
+    total = sum(d.n_total for d in disks)
+    counts = (T.Counts * max(len(disks), 1))()
+    r, v = np.zeros(max(total, 1), T.VEC), np.zeros(max(total, 1), T.VEC)
+    p, md = np.zeros(max(total, 1), T.PARAM), np.zeros(max(total, 1), T.BODY_MD)
+    vp = ctypes.c_void_p
+    rc = L.rg_populate_disks(len(disks), ctypes.cast(arr, vp), ctypes.cast(counts, vp), T.ptr(r), T.ptr(v), T.ptr(p),
+                             T.ptr(md))
+    if rc:
+        raise RedError("rg_populate_disks", rc, L.rg_last_error().decode())
+    out, o = [], 0
+    for d in disks:
+        n = d.n_total
+        disk = bodies.empty_disk(list(d.n_body))
+        disk.r[:], disk.v[:], disk.p[:], disk.md[:] = r[o:o + n], v[o:o + n], p[o:o + n], md[o:o + n]
+        disk.names = d.names()
+        out.append(disk)
+        o += n
+    return out
+
+
+def _mmsn(fn, r_1, r_2, r_SL, f_neb, Sigma_1, f, p):
+    L = _bind_populate(lib.load())
+    c = MmsnC(r_1, r_2, r_SL, f_neb, Sigma_1, f, p)
+    m = ctypes.c_double()
+    rc = getattr(L, fn)(ctypes.cast(ctypes.byref(c), ctypes.c_void_p), ctypes.byref(m))
+    if rc:
+        raise RedError(fn, rc, L.rg_last_error().decode())
+    return m.value
+
+
+def mmsn_gas_mass(r_1, r_2, r_SL, f_neb, Sigma_1, f_gas, p):
+    """Gas mass of a minimum-mass solar nebula (rg_mmsn_gas_mass; host arithmetic only)."""
+    return _mmsn("rg_mmsn_gas_mass", r_1, r_2, r_SL, f_neb, Sigma_1, f_gas, p)
+
+
+def mmsn_solid_mass(r_1, r_2, r_SL, f_neb, Sigma_1, f_ice, p):
+    """Solid mass of a minimum-mass solar nebula (rg_mmsn_solid_mass; host arithmetic only)."""
+    return _mmsn("rg_mmsn_solid_mass", r_1, r_2, r_SL, f_neb, Sigma_1, f_ice, p)
+
+
+# the reference's "Dvorak disk" (main.cu:88-137, 440-470): a 1 Msun star and protoplanets in
+# the solid component of an MMSN with f_neb = 3, Sigma_1 = 7 g/cm^2, the snow line at 2.7 AU
+DVORAK_SOLIDS = dict(r_1=0.9, r_2=2.7, r_SL=2.7, f_neb=3.0, Sigma_1=7.0 * GRAM_PER_CM2, f_ice=4.2, p=-1.5)
+DVORAK_GAS = dict(r_1=0.025, r_2=33.0, r_SL=2.7, f_neb=3.0, Sigma_1=7.0 * GRAM_PER_CM2, f_gas=240.0, p=-1.5)
+
+
+def dvorak_disk(seed, n_pp=2000, m_solid=None):
+    """The reference's Dvorak disk as a BodyDisk: protoplanets with a ~ a^-1.5 on [0.9, 2.7] AU,
+    Rayleigh e (0.01), i = 0, lognormal masses scaled to the nebula's solid mass, basalt
+    density (2.7 g/cm^3); moved to the barycentre."""
+    if m_solid is None:
+        m_solid = mmsn_solid_mass(**DVORAK_SOLIDS)
+    s = DVORAK_SOLIDS
+    star, proto = T.BODY_STAR, T.BODY_PROTOPLANET
+    n_body = [0] * 7
+    n_body[star], n_body[proto] = 1, n_pp
+    return BodyDisk(
+        seed=seed, n_body=tuple(n_body), to_bc=True, pp_total_mass=m_solid,
+        pp={star: {PP_MASS: uniform(1.0, 1.0), PP_RADIUS: uniform(SOLAR_RADIUS_AU, SOLAR_RADIUS_AU),
+                   PP_DRAG_COEFF: uniform(0.0, 0.0)},
+            proto: {PP_MASS: lognormal(0.1, 3.0, 0.0, 0.25), PP_DENSITY: uniform(2.7 * GRAM_PER_CM3, 2.7 * GRAM_PER_CM3),
+                    PP_DRAG_COEFF: uniform(0.0, 0.0)}},
+        oe={proto: {OE_SMA: power_law(s["r_1"], s["r_2"], s["p"]), OE_ECC: rayleigh(0.01), OE_INC: uniform(0.0, 0.0),
+                    OE_PERI: uniform(0.0, 2.0 * np.pi), OE_NODE: uniform(0.0, 0.0),
+                    OE_MEAN: uniform(0.0, 2.0 * np.pi)}})
