@@ -474,6 +474,26 @@ def ensemble_section(args):
                     "cpu_python_seconds": t_cpu, "note": "GPU: rg_generate_disks incl. copies to the host; CPU: "
                     "bodies.config_disk (numpy draws, scalar Kepler solver per body)"}
     del gen
+    # the reference's initial-condition program on the GPU: 256 of its Dvorak disks (2000
+    # protoplanets each, scaled to the MMSN solids, moved to the barycentre)
+    from redgb.icgen import dvorak_disk, populate_disks
+    dv = [dvorak_disk(seed=s, n_pp=2000) for s in range(1, 257)]
+    populate_disks(dv[:1])
+    t_pop = time.perf_counter()
+    pop = populate_disks(dv)
+    t_pop = time.perf_counter() - t_pop
+    ic_generator["populate"] = {"disks": len(pop), "bodies": int(sum(d.n_total for d in pop)), "gpu_seconds": t_pop,
+                                "note": "rg_populate_disks incl. copies to the host"}
+    del pop
+    if not args.no_cpu_baseline:
+        import icgen_ref  # the restatement, timed as the CPU figure on a sample of 4 disks
+        t_ref = time.perf_counter()
+        for d in dv[:4]:
+            icgen_ref.populate(d)
+        t_ref = (time.perf_counter() - t_ref) / 4
+        ic_generator["populate"]["cpu_restatement_seconds_per_disk"] = t_ref
+        ic_generator["populate"]["cpu_sample"] = "4 disks through oracle/icgen_ref.populate (numpy, one thread)"
+    del dv
 
     def batched(mode, proposer):
         e = Ensemble(disks, thr)
