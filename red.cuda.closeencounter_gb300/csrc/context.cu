@@ -1179,12 +1179,13 @@ int check_close_encounter(rg_ctx* c, int* n_handled)  // pp_disk.cu:742-770
 
 // number_of_bodies::update_numbers + pp_disk::remove_inactive_bodies
 // (number_of_bodies.cpp:27-104, pp_disk.cu:1324-1409)
+// pp_disk::remove_inactive_bodies (pp_disk.cu:1324-1409): the host records (p, md, epoch)
+// are filtered on the host, where they live; the positions and velocities are gathered on the
+// device by the list of kept bodies, so the state does not travel to the host and back.
 int remove_inactive_bodies(rg_ctx* c)
 {
     const int old_n = c->n_total();
-    std::vector<double> h;
-    int rc = download_state(c, h);
-    if (rc) return rc;
+    int rc = RG_OK;
     int inactive[7] = {0};
     for (int i = 0; i < old_n; i++) {
         if (!(0 < c->md[i].id && RG_BODY_PADDINGPARTICLE > c->md[i].body_type)) {
@@ -1198,11 +1199,12 @@ int remove_inactive_bodies(rg_ctx* c)
         c->cnt[k] -= inactive[k];
     }
     const int n = c->n_total();
-    std::vector<double> hn((size_t)6 * n);
+    std::vector<int> keep;
+    keep.reserve(n);
     int k = 0;
     for (int i = 0; i < old_n; i++) {
         if (0 < c->md[i].id && RG_BODY_PADDINGPARTICLE > c->md[i].body_type) {
-            for (int r = 0; r < 6; r++) hn[(size_t)r * n + k] = h[(size_t)r * old_n + i];
+            keep.push_back(i);
             c->p[k] = c->p[i];
             c->md[k] = c->md[i];
             c->epoch[k] = c->epoch[i];
@@ -1213,8 +1215,23 @@ int remove_inactive_bodies(rg_ctx* c)
     c->p.resize(n);
     c->md.resize(n);
     c->epoch.resize(n);
-    rc = upload_state(c, hn);
-    if (!rc) rc = upload_params(c);
+    if (n > 0) {
+        // the list goes to a temporary device array; the gather writes d_yout (scratch between
+        // steps), which is then copied back into d_y
+        int* d_keep = nullptr;
+        rc = dalloc(&d_keep, (size_t)n);
+        if (rc) return rc;
+        cudaError_t e = cudaMemcpyAsync(d_keep, keep.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->st);
+        if (e == cudaSuccess) rc = launch_gather_rows(c->d_y, c->d_yout, c->cap, d_keep, n, c->st);
+        if (e == cudaSuccess && !rc)
+            e = cudaMemcpy2DAsync(c->d_y, c->cap * sizeof(double), c->d_yout, c->cap * sizeof(double),
+                                  n * sizeof(double), 6, cudaMemcpyDeviceToDevice, c->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);  // keep (host) and d_keep outlive the copies
+        cudaFree(d_keep);
+        if (e != cudaSuccess) return cuda_fail(e, "compaction", __FILE__, __LINE__);
+        if (rc) return rc;
+    }
+    rc = upload_params(c);
     build_tiles(c);
     return rc;
 }

@@ -58,6 +58,8 @@ int launch_ejection(const double* x, const double* y, const double* z, const int
 // vec_t records (r, v: 4 doubles per body) <-> the 6 state rows of `stride`; v / k on the way
 // in, v * k on the way out when `scale`
 int launch_records_to_rows(const double* r, const double* v, int n, int stride, double k, double* y, cudaStream_t st);
+// dst[c][k] = src[c][keep[k]] for the 6 state rows (stride doubles apart), k < n
+int launch_gather_rows(const double* src, double* dst, int stride, const int* keep, int n, cudaStream_t st);
 int launch_rows_to_records(const double* y, int n, int stride, double k, bool scale, double* r, double* v,
                            cudaStream_t st);
 

@@ -261,6 +261,28 @@ int launch_rows_to_records(const double* y, int n, int stride, double k, bool sc
     return 0;
 }
 
+// Compaction of the state rows (the device side of pp_disk::remove_inactive_bodies,
+// pp_disk.cu:1324-1409): dst row c, column k = src row c, column keep[k], for the 6 rows of
+// positions and velocities.  Pure data movement, so the compacted state is bit-identical to
+// the one a host copy makes.
+__global__ void gather_rows_kernel(const double* __restrict__ src, double* __restrict__ dst, int stride,
+                                   const int* __restrict__ keep, int n)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const size_t s = (size_t)stride;
+    const int i = keep[k];
+    for (int c = 0; c < 6; c++) dst[c * s + k] = src[c * s + i];
+}
+
+int launch_gather_rows(const double* src, double* dst, int stride, const int* keep, int n, cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    gather_rows_kernel<<<(n + 255) / 256, 256, 0, st>>>(src, dst, stride, keep, n);
+    RG_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
 // ---------------------------------------------------------------------------------------
 // Energy and angular momentum partials (not in the reference).  Per body i: kinetic
 // energy, the potential of the pairs (i, j < i) the force model couples (all j < i for a

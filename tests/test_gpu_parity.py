@@ -122,6 +122,23 @@ def test_inactive_and_zero_mass_bodies(gpulib):
     _assert_same_state(g, o)
 
 
+def test_compaction_matches_oracle(gpulib):
+    """pp_disk::remove_inactive_bodies on the device (the state rows gathered by the list of
+    kept bodies): the same state, ids and counts as the oracle's host compaction, bit for bit,
+    and the same next step.  With n = 0 the rebuild check always compacts."""
+    disk = bodies.make_disk(n_pl=200, pl_type=T.BODY_PROTOPLANET, seed=9, n_tp=6)
+    disk.md["id"][[3, 50, 51, 150, disk.n_total - 1]] *= -1
+    g, o = _pair(disk, bodies.thresholds(), lambda s: s.set_integrator(T.INT_RKF78, 3.0, True, 1e-10))
+    assert g.check_for_rebuild_vectors(0) and o.check_for_rebuild_vectors(0)
+    (cg, ng), (co, no) = g.n_total(), o.n_total()
+    assert ng == no == disk.n_total - 5
+    assert [getattr(cg, f) for f, _ in cg._fields_] == [getattr(co, f) for f, _ in co._fields_]
+    _assert_same_state(g, o)
+    g.step()
+    o.step()
+    _assert_same_state(g, o)
+
+
 def test_hill_close_encounters_match_oracle(gpulib):
     disk = bodies.make_disk(n_pl=120, pl_type=T.BODY_PROTOPLANET, seed=5, m_range=(1e-7, 1e-5),
                             giants=((9.55e-4, 5.2, 0.05),), a_range=(1.0, 1.3), sigma_e=0.05, sigma_i=0.02)
