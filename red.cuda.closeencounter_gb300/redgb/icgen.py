@@ -302,3 +302,51 @@ def dvorak_disk(seed, n_pp=2000, m_solid=None):
         oe={proto: {OE_SMA: power_law(s["r_1"], s["r_2"], s["p"]), OE_ECC: rayleigh(0.01), OE_INC: uniform(0.0, 0.0),
                     OE_PERI: uniform(0.0, 2.0 * np.pi), OE_NODE: uniform(0.0, 0.0),
                     OE_MEAN: uniform(0.0, 2.0 * np.pi)}})
+
+
+# the other disks of the reference's initial-condition program (main.cu:187-385): a star and
+# n bodies of one type on uniform elements; each moved to the barycentre, no mass scaling
+_DEG = 1.745329251994329509e-2                 # DegreeToRadian
+_JUPITER = 1.0 / 1.0473486e3                   # JupiterToSolar
+_CERES = 1.0 / 2.109342e9                      # CeresToSolar
+_KM = 1.0 / (1.495978707e11 / 1.0e3)           # KilometerToAu
+PRESETS = ("dvorak", "n_gp", "n_pp", "n_spl", "n_pl")
+_PRESET_N = {"dvorak": 2000, "n_gp": 10, "n_pp": 1000, "n_spl": 10, "n_pl": 10}
+
+
+def reference_preset(name, seed, n=None):
+    """The BodyDisk of one of the reference's disk set-ups (PRESETS), with n bodies besides the
+    star (the reference's own count when None).  Its `n_tp` set-up (mass, radius and density
+    all given: the reference refuses it) and its two-body set-up (a radius from 0/0) are not
+    offered."""
+    n = _PRESET_N[name] if n is None else n
+    if name == "dvorak":
+        return dvorak_disk(seed, n_pp=n)
+    two_pi = 2.0 * np.pi
+    star = {PP_MASS: uniform(1.0, 1.0), PP_RADIUS: uniform(SOLAR_RADIUS_AU, SOLAR_RADIUS_AU),
+            PP_DRAG_COEFF: uniform(0.0, 0.0)}
+    wide = {OE_SMA: uniform(1.0, 10.0), OE_ECC: uniform(0.0, 0.1), OE_INC: uniform(0.0, 10.0 * _DEG),
+            OE_PERI: uniform(0.0, two_pi), OE_NODE: uniform(0.0, two_pi), OE_MEAN: uniform(0.0, two_pi)}
+    if name == "n_gp":
+        t, oe = T.BODY_GIANTPLANET, wide
+        pp = {PP_MASS: uniform(0.1 * _JUPITER, 1.0 * _JUPITER), PP_DENSITY: uniform(1.0 * GRAM_PER_CM3, 2.0 * GRAM_PER_CM3),
+              PP_DRAG_COEFF: uniform(0.0, 0.0)}
+    elif name == "n_pp":
+        t = T.BODY_PROTOPLANET
+        oe = {OE_SMA: uniform(100.0, 100.0001), OE_ECC: uniform(0.0, 0.01), OE_INC: uniform(0.0, 0.0),
+              OE_PERI: uniform(0.0, two_pi), OE_NODE: uniform(0.0, 0.0), OE_MEAN: uniform(0.0, two_pi)}
+        pp = {PP_RADIUS: uniform(1.0e3 * _KM, 1.0e3 * _KM), PP_DENSITY: uniform(2.7 * GRAM_PER_CM3, 2.7 * GRAM_PER_CM3),
+              PP_DRAG_COEFF: uniform(0.0, 0.0)}
+    elif name == "n_spl":
+        t, oe = T.BODY_SUPERPLANETESIMAL, wide
+        pp = {PP_MASS: uniform(1.0e-10, 1.0e-9), PP_RADIUS: uniform(10.0 * _KM, 30.0 * _KM),
+              PP_DENSITY: uniform(1.0 * GRAM_PER_CM3, 3.0 * GRAM_PER_CM3), PP_DRAG_COEFF: uniform(1.0, 2.7)}
+    elif name == "n_pl":
+        t, oe = T.BODY_PLANETESIMAL, wide
+        pp = {PP_MASS: uniform(1.0e-3 * _CERES, 1.0e-2 * _CERES),
+              PP_DENSITY: uniform(1.0 * GRAM_PER_CM3, 3.0 * GRAM_PER_CM3), PP_DRAG_COEFF: uniform(0.0, 0.0)}
+    else:
+        raise ValueError(f"unknown disk set-up {name!r}; one of {PRESETS}")
+    n_body = [0] * 7
+    n_body[T.BODY_STAR], n_body[t] = 1, n
+    return BodyDisk(seed=seed, n_body=tuple(n_body), to_bc=True, pp={T.BODY_STAR: star, t: pp}, oe={t: oe})

@@ -154,3 +154,20 @@ def test_populate_refusals(gpulib):
     bad.oe[T.BODY_PROTOPLANET][I.OE_SMA] = I.power_law(0.0, 2.7, -1.5)  # x_min must be positive
     with pytest.raises(RedError):
         I.populate_disks([bad])
+
+
+def test_initial_command_line_writes_body_files(gpulib, tmp_path):
+    """python -m redgb.initial: two of the reference's n_pl disks drawn on the GPU, written as
+    body files that read back as the restatement's disks and load into a context."""
+    from redgb import initial, lib
+    assert initial.main(["n_pl", "--n", "50", "--seed", "7", "--count", "2", "-o", str(tmp_path / "disk")]) == 0
+    for k, seed in ((1, 7), (2, 8)):
+        disk = bodies.read_body_file(tmp_path / f"disk_{k}.txt")
+        r, v, m, R, rho, cd, typ = ref.populate(I.reference_preset("n_pl", seed, 50))
+        assert disk.counts == (1, 0, 0, 0, 0, 50, 0) and np.array_equal(disk.md["body_type"], typ)
+        np.testing.assert_allclose(disk.p["mass"], m, rtol=1e-12)
+        rg = np.stack([disk.r[f] for f in "xyz"], 1)
+        assert np.abs(rg - r).max() <= 1e-11 * np.abs(r).max()
+    s = lib.System(bodies.read_body_file(tmp_path / "disk_1.txt"), bodies.thresholds())
+    s.set_integrator(T.INT_RKF78, tolerance=1e-10)
+    s.advance(10.0)

@@ -141,3 +141,31 @@ def test_dvorak_disk_spec():
     assert abs(m[1:].sum() - d.pp_total_mass) < 1e-15
     np.testing.assert_allclose(rho[1:], 2.7 * icgen.GRAM_PER_CM3, rtol=0)
     assert abs((m[:, None] * r).sum(0)).max() < 1e-15 and abs((m[:, None] * v).sum(0)).max() < 1e-17
+
+
+@pytest.mark.parametrize("name", ["dvorak", "n_gp", "n_pp", "n_spl", "n_pl"])
+def test_reference_presets_restated(name, tmp_path):
+    """The reference's disk set-ups as specs: counts, derived properties, barycentre, and a
+    body file written from the restatement reads back the same."""
+    from redgb import bodies, icgen
+    spec = icgen.reference_preset(name, seed=4, n=40)
+    r, v, m, R, rho, cd, typ = ref.populate(spec)
+    assert spec.n_total == 41 and typ[0] == T.BODY_STAR and np.all(typ[1:] == typ[1])
+    assert np.all(np.isfinite(r)) and np.all(np.isfinite(v)) and np.all(np.isfinite(R))
+    assert abs((m[:, None] * r).sum(0)).max() < 1e-12 * abs(m[:, None] * r).max()
+    if name == "n_pp":  # radius and density given: mass = 4 pi / 3 R^3 rho
+        np.testing.assert_allclose(m[1:], 4.0 / 3.0 * np.pi * R[1:] ** 3 * rho[1:], rtol=1e-14)
+    if name == "n_spl":  # superplanetesimals keep all three as drawn
+        assert np.all((m[1:] >= 1e-10) & (m[1:] <= 1e-9))
+    disk = bodies.empty_disk(list(spec.n_body))
+    for f, col in zip("xyz", range(3)):
+        disk.r[f], disk.v[f] = r[:, col], v[:, col]
+    disk.p["mass"], disk.p["radius"], disk.p["density"], disk.p["cd"] = m, R, rho, cd
+    disk.md["id"], disk.md["body_type"] = np.arange(1, 42), typ
+    disk.names = spec.names()
+    path = tmp_path / f"{name}.txt"
+    bodies.write_body_file(path, disk)
+    back = bodies.read_body_file(path)
+    assert back.counts == disk.counts and back.names == disk.names
+    np.testing.assert_allclose(back.p["mass"], m, rtol=1e-15)
+    np.testing.assert_allclose(back.r["x"], r[:, 0], rtol=1e-15, atol=0)
