@@ -169,3 +169,13 @@ def test_reference_presets_restated(name, tmp_path):
     assert back.counts == disk.counts and back.names == disk.names
     np.testing.assert_allclose(back.p["mass"], m, rtol=1e-15)
     np.testing.assert_allclose(back.r["x"], r[:, 0], rtol=1e-15, atol=0)
+
+
+def test_initial_command_line_arguments():
+    """redgb.initial refuses a non-positive disk count and the set-ups it does not offer
+    before it draws anything."""
+    from redgb import initial
+    for argv in (["n_pl", "--count", "0", "-o", "x"], ["n_tp", "-o", "x"], ["two_body", "-o", "x"],
+                 ["n_pl", "--n", "-1", "-o", "x"]):
+        with pytest.raises(SystemExit):
+            initial.main(argv)
