@@ -37,3 +37,44 @@ def test_library_exports_every_declared_symbol():
 def test_record_sizes_match_reference_layout():
     from redgb import types as T
     assert (T.VEC.itemsize, T.PARAM.itemsize, T.BODY_MD.itemsize, T.EVENT.itemsize) == (32, 32, 24, 472)
+
+
+def test_generator_structs_match_the_header(tmp_path):
+    """The ctypes mirrors of the initial-condition structs have the header's sizes and field
+    offsets (a small C++ program compiled against include/redgb_types.h prints them)."""
+    import shutil
+    import subprocess
+    import pytest
+    from redgb import icgen
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    src = tmp_path / "layout.cpp"
+    src.write_text("""
+#include <cstddef>
+#include <cstdio>
+#include "redgb_types.h"
+#define P(T, f) std::printf("%s.%s %zu\\\\n", #T, #f, offsetof(T, f));
+int main() {
+    std::printf("rg_dist_t %zu\\\\nrg_body_disk_t %zu\\\\nrg_mmsn_component_t %zu\\\\nrg_disk_spec_t %zu\\\\n",
+                sizeof(rg_dist_t), sizeof(rg_body_disk_t), sizeof(rg_mmsn_component_t), sizeof(rg_disk_spec_t));
+    P(rg_dist_t, p) P(rg_body_disk_t, n_body) P(rg_body_disk_t, to_bc) P(rg_body_disk_t, pp_total_mass)
+    P(rg_body_disk_t, oe) P(rg_body_disk_t, pp) P(rg_mmsn_component_t, p)
+    P(rg_disk_spec_t, giant_m) P(rg_disk_spec_t, m_lo) P(rg_disk_spec_t, a_mode) P(rg_disk_spec_t, sigma_e)
+    P(rg_disk_spec_t, rho_pl)
+    return 0;
+}
+""".replace("\\\\n", "\\n"))
+    exe = tmp_path / "layout"
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(H.ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.rsplit(" ", 1) for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                               check=True).stdout.split("\n") if line)
+    got = {k: int(v) for k, v in got.items()}
+    assert got["rg_dist_t"] == ctypes.sizeof(icgen.DistC)
+    assert got["rg_body_disk_t"] == ctypes.sizeof(icgen.BodyDiskC)
+    assert got["rg_mmsn_component_t"] == ctypes.sizeof(icgen.MmsnC)
+    assert got["rg_disk_spec_t"] == ctypes.sizeof(icgen.DiskSpecC)
+    for cname, cls in (("rg_dist_t", icgen.DistC), ("rg_body_disk_t", icgen.BodyDiskC),
+                       ("rg_mmsn_component_t", icgen.MmsnC), ("rg_disk_spec_t", icgen.DiskSpecC)):
+        for key, off in got.items():
+            if key.startswith(cname + "."):
+                assert getattr(cls, key.split(".", 1)[1]).offset == off, key
