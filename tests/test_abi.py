@@ -78,3 +78,28 @@ int main() {
         for key, off in got.items():
             if key.startswith(cname + "."):
                 assert getattr(cls, key.split(".", 1)[1]).offset == off, key
+
+
+def test_every_mirrored_struct_matches_the_header(tmp_path):
+    """Sizes of all C structs the Python view mirrors (ctypes classes and numpy records)."""
+    import shutil
+    import subprocess
+    import pytest
+    from redgb import types as T
+    if shutil.which("g++") is None:
+        pytest.skip("no g++")
+    names = ["rg_vec_t", "rg_param_t", "rg_body_metadata_t", "rg_orbelem_t", "rg_event_t", "rg_counts_t",
+             "rg_counters_t", "rg_profile_t", "rg_tune_t", "rg_ens_stats_t", "rg_step_rec_t"]
+    src = tmp_path / "sizes.cpp"
+    body = "".join(f'    std::printf("{n} %zu\\n", sizeof({n}));\n' for n in names)
+    src.write_text('#include <cstdio>\n#include "redgb_types.h"\nint main() {\n' + body + "    return 0;\n}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run(["g++", "-std=c++17", "-I", os.path.join(H.ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {k: int(v) for k, v in (line.split() for line in
+                                  subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines())}
+    mirrors = {"rg_vec_t": T.VEC.itemsize, "rg_param_t": T.PARAM.itemsize, "rg_body_metadata_t": T.BODY_MD.itemsize,
+               "rg_orbelem_t": T.ORBELEM.itemsize, "rg_event_t": T.EVENT.itemsize,
+               "rg_counts_t": ctypes.sizeof(T.Counts), "rg_counters_t": ctypes.sizeof(T.Counters),
+               "rg_profile_t": ctypes.sizeof(T.Profile), "rg_tune_t": ctypes.sizeof(T.Tune),
+               "rg_ens_stats_t": ctypes.sizeof(T.EnsStats), "rg_step_rec_t": T.STEP_REC.itemsize}
+    assert got == mirrors
