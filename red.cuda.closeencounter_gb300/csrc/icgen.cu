@@ -555,6 +555,7 @@ static int populate_impl(int n_sys, const rg_body_disk_t* disks, rg_counts_t* co
         total += n;
     }
     if (total == 0) return RG_OK;
+    std::vector<int> err(n_sys, 0);  // host allocations first: nothing after the device ones throws
     rg_body_disk_t* d_disks = nullptr;
     long long* d_off = nullptr;
     int *d_n = nullptr, *d_dob = nullptr, *d_b0 = nullptr, *d_err = nullptr;
@@ -576,7 +577,6 @@ static int populate_impl(int n_sys, const rg_body_disk_t* disks, rg_counts_t* co
     auto check = [&](cudaError_t e, const char* what) {
         if (!rc && e != cudaSuccess) rc = cuda_fail(e, what, __FILE__, __LINE__);
     };
-    std::vector<int> err(n_sys, 0);
     if (!rc) {
         check(cudaMemcpy(d_disks, disks, n_sys * sizeof(rg_body_disk_t), cudaMemcpyHostToDevice), "disks");
         check(cudaMemcpy(d_off, offset.data(), n_sys * sizeof(long long), cudaMemcpyHostToDevice), "offsets");
