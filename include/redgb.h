@@ -274,12 +274,16 @@ RG_API int rg_energy(rg_ctx* ctx, double* energy, double angmom[3]);
  * The call allocates nothing: its scratch is a fixed device array of
  * RG_ENERGY_NOALLOC_MAX_BODIES bodies (2.5 MiB per device, part of the library image), and
  * a larger n_total is rejected with RG_ERR_ARG before any device work.  The first call on
- * each device looks the scratch's address up with that device current; a caller that
- * captures streams makes that first call before its capture begins.  Nothing in the
- * scratch needs to start at zero.  There is one scratch per device, so calls on the same
- * device must not overlap (from two threads, or on two streams with both in flight): they
- * would race on it.  The work runs on `stream` (NULL: the default stream), which the call
- * synchronises before it returns the results.
+ * each device looks the scratch's address up with that device current and keeps it for
+ * later calls.  That address belongs to the CUDA runtime's primary context of the device:
+ * callers that make their own driver-API context current are not supported, and a
+ * cudaDeviceReset invalidates the kept address.  Nothing in the scratch needs to start at
+ * zero.  There is one scratch per device, so calls on the same device must not overlap
+ * (from two threads, or on two streams with both in flight): they would race on it.
+ * The work runs on `stream` (NULL: the legacy default stream), and the call copies the
+ * four results to the host and synchronises that stream before it returns.  It therefore
+ * cannot be made on a stream that is being captured into a CUDA graph, nor on the legacy
+ * NULL stream while any global-mode capture is in progress.
  */
 #define RG_ENERGY_NOALLOC_MAX_BODIES 65536
 RG_API int rg_energy_noalloc(const rg_counts_t* counts, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/redgb.h"
+#include "abi_guard.h"
 #include "common.cuh"
 #include "host_tools.h"
 #include "kernels.h"
@@ -1275,14 +1276,6 @@ int do_step(rg_ctx* c)
 }  // namespace
 
 // ============================================================================ C ABI
-#define RG_GUARD(expr)                                                                    \
-    try {                                                                                 \
-        return (expr);                                                                    \
-    } catch (const std::bad_alloc&) {                                                     \
-        return set_error(RG_ERR_NOMEM, "host allocation failed");                         \
-    } catch (...) {                                                                       \
-        return set_error(RG_ERR_STATE, "unexpected exception");                           \
-    }
 
 extern "C" {
 

@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "../../include/redgb.h"
+#include "abi_guard.h"
 #include "common.cuh"
 #include "host_tools.h"
 #include "kernels.h"
@@ -1303,14 +1304,6 @@ void handle_hill(rg_ens* e, std::vector<DevEvent>& recs, const std::vector<unsig
 }  // namespace
 
 // ============================================================================ C ABI
-#define RG_GUARD(expr)                                                    \
-    try {                                                                 \
-        return (expr);                                                    \
-    } catch (const std::bad_alloc&) {                                     \
-        return set_error(RG_ERR_NOMEM, "host allocation failed");         \
-    } catch (...) {                                                       \
-        return set_error(RG_ERR_STATE, "unexpected exception");           \
-    }
 
 namespace {
 

@@ -16,6 +16,12 @@
 // read within one call, and so are the four results.  There is one scratch per device, so
 // calls on the same device must not overlap (two host threads, or two streams with the
 // work of both calls in flight) -- they would overwrite each other's partials.
+//
+// The cached address belongs to the CUDA runtime's primary context of that device, the
+// context every runtime-API caller uses.  A caller that makes its own driver-API context
+// current, or that calls cudaDeviceReset (which destroys the primary context and with it
+// the address), is not supported: the kernels would write through an address that is not
+// valid in the current context.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -24,6 +30,7 @@
 #include <string>
 
 #include "../../include/redgb.h"
+#include "abi_guard.h"
 
 namespace redgb {
 int set_error(int code, const std::string& msg);
@@ -134,12 +141,8 @@ __global__ void energy_sum_kernel(const double* part, int n, double* res)
     }
 }
 
-}  // namespace
-
-extern "C" {
-
-int rg_energy_noalloc(const rg_counts_t* counts, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,
-                      const rg_body_metadata_t* md, void* stream, double* energy, double angmom[3])
+int energy_noalloc_impl(const rg_counts_t* counts, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,
+                       const rg_body_metadata_t* md, void* stream, double* energy, double* angmom)
 {
     if (!counts) return redgb::set_error(RG_ERR_ARG, "rg_energy_noalloc: null counts");
     const int c[7] = {counts->n_s, counts->n_gp, counts->n_rp, counts->n_pp, counts->n_spl, counts->n_pl, counts->n_tp};
@@ -183,6 +186,16 @@ int rg_energy_noalloc(const rg_counts_t* counts, const rg_vec_t* r, const rg_vec
         angmom[2] = h[3];
     }
     return RG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int rg_energy_noalloc(const rg_counts_t* counts, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,
+                      const rg_body_metadata_t* md, void* stream, double* energy, double angmom[3])
+{
+    RG_GUARD(energy_noalloc_impl(counts, r, v, p, md, stream, energy, angmom));
 }
 
 }  // extern "C"

@@ -195,6 +195,13 @@ class System:
                    T.ptr(md), ctypes.byref(t))
         return r, v, p, md, t.value
 
+    def time(self, internal=True):
+        """The clock alone (internal units, or days with internal=False); copies no state."""
+        t = ctypes.c_double()
+        self._call("get_state_internal" if internal else "get_state", self.handle, None, None, None, None,
+                   ctypes.byref(t))
+        return t.value
+
     def set_state(self, r, v):
         self._call("set_state", self.handle, T.ptr(np.ascontiguousarray(r)), T.ptr(np.ascontiguousarray(v)))
 

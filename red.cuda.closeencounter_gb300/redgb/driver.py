@@ -33,7 +33,7 @@ def run_main_loop(system, stop_day, output_interval_day, *, radii_enhance_factor
     snap()
     n = 0
     while True:
-        t = system.state(internal=True)[4]
+        t = system.time(internal=True)
         if not t <= stop or (max_steps and n >= max_steps):
             break
         if oi <= abs(ps):

@@ -3,8 +3,10 @@
 Run in a checkout that has the reference sources (this is the only script that reads
 them; nothing in the test suite does):
 
-    make -f oracle/ref.mk REF=/root/reference -j8      # builds oracle/_ref/red (CPU path)
-    python tests/golden/make_golden.py --ref /root/reference
+    make -f oracle/ref.mk REF=<reference checkout> -j8   # builds oracle/_ref/red (CPU path)
+    python tests/golden/make_golden.py --ref <reference checkout>
+
+The checkout can also be named by the RED_REFERENCE environment variable.
 
 Each case writes a body list and a parameter file, runs ``red -cpu -ef`` (the
 reference's FP64 CPU path, single thread) and stores inputs, result snapshots and event
@@ -139,14 +141,23 @@ def cases():
     d = bodies.make_disk(n_pl=16, seed=11, a_range=(1.0, 3.0), sigma_e=0.3, sigma_i=0.05, n_tp=4)
     out.append(("disk_eject_hit", d, dict(integrator="rkf8", tolerance=1e-10, length_yr=3.0, output_interval_yr=0.5,
                                           ejection=3.2, hit_centrum=0.3, collision_factor=1.0)))
+    # the plain FP64 planetesimal-disk workload: star, two giants, 1024 planetesimals (seed 0),
+    # RKF7(8) at 1e-10 for 1000 years with collisions, ejection (100 AU) and hit-star (0.05 AU)
+    # on; snapshots every 250 years
+    out.append(("planetesimal_disk_1000yr", bodies.config_disk("planetesimal_disk"),
+                dict(integrator="rkf8", tolerance=1e-10, length_yr=1000.0, output_interval_yr=250.0, ejection=100.0,
+                     hit_centrum=0.05, collision_factor=1.0)))
     return out
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", default=os.environ.get("RED_REFERENCE"),
+                    help="the reference checkout (default: $RED_REFERENCE)")
     ap.add_argument("--only", default=None)
     args = ap.parse_args()
+    if not args.ref:
+        sys.exit("name the reference checkout: --ref <dir> or RED_REFERENCE=<dir>")
     if not os.path.exists(RED):
         sys.exit("oracle/_ref/red missing: make -f oracle/ref.mk REF=<reference> first")
     tin = os.path.join(args.ref, "red.cuda", "TestRun", "InputTest")

@@ -116,4 +116,4 @@ def compare_events(events, ref):
 
 
 FIXTURES = ["twobody_euler", "n1_massive_n3", "disk_nsi_rkf78", "disk_si_rkf78_collide", "disk_si_rkf78_ce",
-            "disk_si_rk4_fixed", "disk_si_rk4_adaptive", "disk_eject_hit"]
+            "disk_si_rk4_fixed", "disk_si_rk4_adaptive", "disk_eject_hit", "planetesimal_disk_1000yr"]

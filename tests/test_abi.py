@@ -103,3 +103,39 @@ def test_every_mirrored_struct_matches_the_header(tmp_path):
                "rg_profile_t": ctypes.sizeof(T.Profile), "rg_tune_t": ctypes.sizeof(T.Tune),
                "rg_ens_stats_t": ctypes.sizeof(T.EnsStats), "rg_step_rec_t": T.STEP_REC.itemsize}
     assert got == mirrors
+
+
+def test_energy_noalloc_host_checks_without_a_device():
+    """rg_energy_noalloc's argument checks run on the host before any device work, so they
+    are exercised here without a GPU: no bodies gives zeros; a negative count, a missing
+    body array with bodies to read, or more bodies than its fixed scratch holds give
+    RG_ERR_ARG."""
+    from redgb import lib, types as T
+    L = lib.load()
+    f = L.rg_energy_noalloc
+    vp, dp = ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)
+    f.argtypes = [ctypes.POINTER(T.Counts), vp, vp, vp, vp, vp, dp, dp]
+    f.restype = ctypes.c_int
+    RG_ERR_ARG = -1
+
+    def call(counts, arrays=(None, None, None, None)):
+        e = ctypes.c_double(123.0)
+        Lm = (ctypes.c_double * 3)(1.0, 2.0, 3.0)
+        rc = f(ctypes.byref(counts) if counts is not None else None, *arrays, None, ctypes.byref(e), Lm)
+        return rc, e.value, list(Lm)
+
+    assert call(T.Counts()) == (0, 0.0, [0.0, 0.0, 0.0])
+    assert call(None)[0] == RG_ERR_ARG
+    neg = T.Counts()
+    neg.n_s, neg.n_pl = 1, -2
+    assert call(neg)[0] == RG_ERR_ARG and "negative" in L.rg_last_error().decode()
+    some = T.Counts()
+    some.n_s, some.n_pl = 1, 10
+    fake = ctypes.c_void_p(16)  # never dereferenced: a missing array is refused first
+    for k in range(4):
+        arrays = [fake] * 4
+        arrays[k] = None
+        assert call(some, arrays)[0] == RG_ERR_ARG and "null body array" in L.rg_last_error().decode()
+    big = T.Counts()
+    big.n_s, big.n_pl = 1, 65536
+    assert call(big)[0] == RG_ERR_ARG and "65536" in L.rg_last_error().decode()
