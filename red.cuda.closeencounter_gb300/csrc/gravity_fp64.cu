@@ -7,8 +7,12 @@
 // other in ascending j.  This file is compiled with -fmad=false and keeps that operation
 // order, so the accelerations equal the CPU path's bit for bit.
 //
-// GB300 design.  The serial sum is only 3 FP64 adds per pair; the sqrt, the division and
-// the multiplies (~35 FP64 operations) do not depend on the order.  The pair-parallel
+// GB300 design.  GB300 retires about two FP64 lanes per SM and clock, so the FP64 pipe
+// bounds this file.  The square root and the division of each pair term, about half of its
+// FP64 instructions in hardware form, are computed exactly (correctly rounded, the same
+// bits) with integer arithmetic on the other pipes (exact_fp64.h); the FP64 pipe keeps the
+// 15 subtractions, multiplications and additions.  The serial sum is only 3 FP64 adds per
+// pair; the pair terms do not depend on the order.  The pair-parallel
 // kernel therefore lets all 256 threads of a CTA compute the S x J pair terms of a tile
 // (S sinks x J sources) into shared memory, and 3 S threads then add them in source
 // order.  That keeps every SM's FP64 pipe busy however few sinks a block has (3 sinks x
@@ -16,6 +20,7 @@
 // The row-serial kernel (thread per sink) serves blocks with few sources per sink
 // (planetesimals x 3 massive bodies).  Sources are staged through shared memory in both.
 #include "common.cuh"
+#include "exact_fp64.h"
 
 namespace redgb {
 
@@ -33,13 +38,13 @@ __device__ __forceinline__ void pair_term(const GravArgs& g, const Tile& tile, i
     const double dy = yj - yi;
     const double dz = zj - zi;
     const double r2 = dx * dx + dy * dy + dz * dz;
-    const double d = sqrt(r2);
-    const double w = mj / (d * r2);
+    const double d = rn_sqrt(r2);         // sqrt.rn, computed on the integer pipes
+    const double w = rn_div(mj, d * r2);  // div.rn, likewise (exact_fp64.h)
     o.tx = w * dx;
     o.ty = w * dy;
     o.tz = w * dz;
     const int li = i - tile.base, lj = j - tile.base;
-    bool rad = g.record && li > 0 && li > lj && d < g.f_rad * (Ri + Rj);
+    bool rad = g.record && li > 0 && li > lj && d < tile_f_rad(g, tile) * (Ri + Rj);
     bool hill = false;
     if (g.hill && tile.block != 2 && li > 0 && li > lj && lj > 0) {
         const double h = 0.5 * (rhoi + rhoj);
@@ -76,16 +81,21 @@ __device__ __forceinline__ void pair_term(const GravArgs& g, const Tile& tile, i
 }
 
 // ---------------------------------------------------------------------------------------
-// Pair-parallel kernel: CTA = S sinks, source tiles of J = 1024 / S.
-template <int S>
+// Pair-parallel kernel: CTA = S sinks, source tiles of J = 1024 / S.  ASTRO: the
+// astrocentric frame of the reference's CPU path -- each sink starts from the star's pull
+// and, for every source it interacts with, adds the direct term and then subtracts the
+// source's indirect term (pp_disk.cu:413-454), in source order.
+template <int S, bool ASTRO>
 __global__ void __launch_bounds__(256) grav_fp64_pairpar(GravArgs g)
 {
     constexpr int NT = 256;
     constexpr int J = 1024 / S;
     constexpr int STRIDE = NT / S;  // source offset between a thread's terms
     constexpr int JPT = J / STRIDE;  // terms per thread per tile
+    constexpr int JA = ASTRO ? J : 1;
     __shared__ double tx[J * S], ty[J * S], tz[J * S];
     __shared__ double sx[J], sy[J], sz[J], sm[J], sR[J], srho[J];
+    __shared__ double sind[3][JA];  // ASTRO: the sources' indirect terms
     __shared__ int sid[J];
 
     const Tile tile = g.tiles[blockIdx.x];
@@ -106,6 +116,7 @@ __global__ void __launch_bounds__(256) grav_fp64_pairpar(GravArgs g)
     const int bc = t / S;  // phase-B component (0, 1, 2) for t < 3 S
     const double* Tb = bc == 0 ? tx : (bc == 1 ? ty : tz);
     double acc = 0.0;
+    if (ASTRO && t < 3 * S && sink_ok) acc = g.astro[bc * g.astro_stride + i];
 
     for (int j0 = tile.src_begin; j0 < tile.src_end; j0 += J) {
         const int nj = min(J, tile.src_end - j0);
@@ -114,6 +125,11 @@ __global__ void __launch_bounds__(256) grav_fp64_pairpar(GravArgs g)
             sx[q] = g.px[j]; sy[q] = g.py[j]; sz[q] = g.pz[j];
             sm[q] = g.mass[j]; sR[q] = g.radius[j]; sid[q] = g.id[j];
             srho[q] = g.hill ? g.rho[j] : 0.0;
+            if (ASTRO) {
+                sind[0][q] = g.astro[3 * g.astro_stride + j];
+                sind[1][q] = g.astro[4 * g.astro_stride + j];
+                sind[2][q] = g.astro[5 * g.astro_stride + j];
+            }
         }
         __syncthreads();
 #pragma unroll
@@ -129,7 +145,18 @@ __global__ void __launch_bounds__(256) grav_fp64_pairpar(GravArgs g)
         }
         __syncthreads();
         if (t < 3 * S) {
-            for (int q = 0; q < nj; q++) acc = acc + Tb[q * S + s];
+            if (ASTRO) {
+                if (active) {
+                    const double* Ib = sind[bc < 3 ? bc : 0];
+                    for (int q = 0; q < nj; q++)
+                        if (j0 + q != i && 0 <= sid[q]) {
+                            acc = acc + Tb[q * S + s];
+                            acc = acc - Ib[q];
+                        }
+                }
+            } else {
+                for (int q = 0; q < nj; q++) acc = acc + Tb[q * S + s];
+            }
         }
         __syncthreads();
     }
@@ -322,17 +349,64 @@ __global__ void __launch_bounds__(128) few_sum_serial(FewSumArgs a)
     }
 }
 
+// The astrocentric frame's per-body terms (pp_disk.cu:413-420 and 447-454) for bodies
+// [1, n): the star's pull on body i, -mu / (r2 sqrt(r2)) r_i with mu = m_star + m_i, and the
+// indirect term m_i / (r2 sqrt(r2)) r_i, r2 = |r_i|^2, each component evaluated as the
+// reference writes it (division first, then the product).  Body 0 (the star) gets zeros.
+__global__ void astro_terms_kernel(const double* __restrict__ x, const double* __restrict__ y,
+                                   const double* __restrict__ z, const double* __restrict__ mass, int n,
+                                   double m_star, double* __restrict__ out, long long stride)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double sx = 0.0, sy = 0.0, sz = 0.0, ix = 0.0, iy = 0.0, iz = 0.0;
+    if (i > 0) {
+        const double xi = x[i], yi = y[i], zi = z[i], m = mass[i];
+        const double r2 = xi * xi + yi * yi + zi * zi;
+        const double den = r2 * rn_sqrt(r2);
+        const double mu = m_star + m;
+        const double ws = -mu / den;
+        const double wi = rn_div(m, den);
+        sx = ws * xi; sy = ws * yi; sz = ws * zi;
+        ix = wi * xi; iy = wi * yi; iz = wi * zi;
+    }
+    out[i] = sx;
+    out[stride + i] = sy;
+    out[2 * stride + i] = sz;
+    out[3 * stride + i] = ix;
+    out[4 * stride + i] = iy;
+    out[5 * stride + i] = iz;
+}
+
 // ---------------------------------------------------------------------------------------
 // Host launchers
 int launch_grav_fp64_pairpar(const GravArgs& g, int S, cudaStream_t st)
 {
     if (g.n_tiles <= 0) return 0;
-    if (S == 16)
-        grav_fp64_pairpar<16><<<g.n_tiles, 256, 0, st>>>(g);
-    else if (S == 32)
-        grav_fp64_pairpar<32><<<g.n_tiles, 256, 0, st>>>(g);
-    else
-        grav_fp64_pairpar<8><<<g.n_tiles, 256, 0, st>>>(g);
+    if (g.astro) {
+        if (S == 16)
+            grav_fp64_pairpar<16, true><<<g.n_tiles, 256, 0, st>>>(g);
+        else if (S == 32)
+            grav_fp64_pairpar<32, true><<<g.n_tiles, 256, 0, st>>>(g);
+        else
+            grav_fp64_pairpar<8, true><<<g.n_tiles, 256, 0, st>>>(g);
+    } else {
+        if (S == 16)
+            grav_fp64_pairpar<16, false><<<g.n_tiles, 256, 0, st>>>(g);
+        else if (S == 32)
+            grav_fp64_pairpar<32, false><<<g.n_tiles, 256, 0, st>>>(g);
+        else
+            grav_fp64_pairpar<8, false><<<g.n_tiles, 256, 0, st>>>(g);
+    }
+    RG_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int launch_astro_terms(const double* x, const double* y, const double* z, const double* mass, int n, double m_star,
+                       double* out, long long stride, cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    astro_terms_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, mass, n, m_star, out, stride);
     RG_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
