@@ -66,10 +66,13 @@ typedef struct rg_counters {
 
 /* kernel timing of a context (rg_set_profiling): CUDA events around every launch */
 typedef struct rg_profile {
-    int64_t gravity_launches;  /* force evaluations timed            */
-    double  gravity_ms;        /* their summed device time           */
-    int64_t stage_launches;    /* stage-combine / error kernels timed */
+    int64_t gravity_launches;  /* force evaluations timed                                */
+    double  gravity_ms;        /* their summed device time                               */
+    int64_t stage_launches;    /* stage-combine / error kernels timed                    */
     double  stage_ms;
+    int64_t other_launches;    /* the rest of a step: state copy, ejection / hit-star
+                                  screen, step-size controller, features (ensembles)     */
+    double  other_ms;
 } rg_profile_t;
 
 /* one synthetic disk for rg_generate_disks: a 1 Msun star at rest in the origin, giants on
@@ -213,6 +216,9 @@ enum {
     RG_BODY_TESTPARTICLE = 6,
     RG_BODY_PADDINGPARTICLE = 7
 };
+
+/* red_type.h:38-43 frame_center_t: the origin of the coordinates (parameter.cpp:257-266) */
+enum { RG_FRAME_ASTRO = 0, RG_FRAME_BARY = 1 };
 
 /* red_type.h:76-82 event_counter_name_t */
 enum { RG_COUNTER_TOTAL = 0, RG_COUNTER_LAST_CLEAR = 1, RG_COUNTER_LAST_STEP = 2 };

@@ -65,8 +65,8 @@ class OracleSystem(System):
 
     prefix = "ro_"
 
-    def __init__(self, disk, thr):
-        super().__init__(lib(), disk, thr, _create_extra=False)
+    def __init__(self, disk, thr, frame=T.FRAME_BARY):
+        super().__init__(lib(), disk, thr, _create_extra=False, frame=frame)
 
     def set_dt_replay(self, dts_internal):
         a = np.ascontiguousarray(dts_internal, np.float64)

@@ -54,6 +54,7 @@ typedef struct ro_sys {
     int close_encounter, inner_steps;
     double hill_factor;
     int event_time_mode;
+    int frame; /* RG_FRAME_BARY or RG_FRAME_ASTRO (pp_disk.h frame_center) */
     /* pp_disk::events / event_counter (pp_disk.h:187-192) */
     rg_event_t* events;
     int event_counter, event_cap;
@@ -350,16 +351,46 @@ static double mass_of_star(const ro_sys* s)
     return 0.0;
 }
 
+/* tools.cpp:180-236 get_star_bc_phase + transform_to_ac: every body minus body 0's phase
+ * (the reference tests body 0's type for every j, so body 0 must be the star), the loop
+ * running j = n-1 .. 0 so that body 0 ends exactly at rest in the origin. */
+static int transform_to_ac(int n, const rg_body_metadata_t* md, rg_vec_t* r, rg_vec_t* v)
+{
+    if (md[0].body_type != RG_BODY_STAR) return RO_ERR_ARG; /* "No star is included!" */
+    const rg_vec_t R0 = r[0], V0 = v[0];
+    for (int j = n - 1; j >= 0; j--) {
+        r[j].x -= R0.x; r[j].y -= R0.y; r[j].z -= R0.z;
+        v[j].x -= V0.x; v[j].y -= V0.y; v[j].z -= V0.z;
+    }
+    return RO_OK;
+}
+
 /* pp_disk::pp_disk + load + options::create_pp_disk (pp_disk.cu:1204-1235,1614-1683;
- * options.cpp:197-235) for the barycentric frame. */
+ * options.cpp:197-235) in the barycentric frame. */
 int ro_create(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,
               const rg_body_metadata_t* md, const double* epoch, const double thr[RG_THRESHOLD_N],
               ro_sys** out)
+{
+    return ro_create_in_frame(n, r, v, p, md, epoch, thr, RG_FRAME_BARY, out);
+}
+
+/* The same in either frame (options.cpp:206-220): a system whose body 0 sits at rest in the
+ * origin is moved to its barycentre in the barycentric frame; any other system is moved to
+ * body 0 (the star) in the astrocentric frame.  The astrocentric frame is refused for
+ * systems with non-self-interacting bodies (super-planetesimals, planetesimals, test
+ * particles): their blocks take the star, at the origin, as source 0, whose indirect term
+ * m_0 / (0 * sqrt(0)) * 0 (pp_disk.cu:447-454) makes the reference's accelerations NaN. */
+int ro_create_in_frame(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,
+                       const rg_body_metadata_t* md, const double* epoch, const double thr[RG_THRESHOLD_N],
+                       int frame_center, ro_sys** out)
 {
     if (!n || !r || !v || !p || !md || !thr || !out) return RO_ERR_ARG;
     if (n->n_s < 0 || n->n_gp < 0 || n->n_rp < 0 || n->n_pp < 0 || n->n_spl < 0 || n->n_pl < 0 ||
         n->n_tp < 0)
         return RO_ERR_ARG;
+    if (frame_center != RG_FRAME_BARY && frame_center != RG_FRAME_ASTRO) return RO_ERR_ARG;
+    if (frame_center == RG_FRAME_ASTRO && (n->n_spl > 0 || n->n_pl > 0 || n->n_tp > 0))
+        return RO_ERR_NOT_IMPLEMENTED;
     ro_sys* s = (ro_sys*)calloc(1, sizeof(ro_sys));
     if (!s) return RO_ERR_NOMEM;
     s->n_s = n->n_s; s->n_gp = n->n_gp; s->n_rp = n->n_rp; s->n_pp = n->n_pp;
@@ -393,12 +424,20 @@ int ro_create(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v, const 
     }
     s->close_encounter = 0;
     s->inner_steps = 1;
+    s->frame = frame_center;
     for (int i = 0; i < RG_THRESHOLD_N; i++) s->thr[i] = thr[i];
 
-    /* options.cpp:206-212: barycentric transform if the first body sits at rest in 0 */
+    /* options.cpp:206-220: barycentric transform if the first body sits at rest in 0,
+     * astrocentric transform otherwise */
     if (0 == fabs(s->y[0][0].x) && 0 == fabs(s->y[0][0].y) && 0 == fabs(s->y[0][0].z) &&
-        0 == fabs(s->y[1][0].x) && 0 == fabs(s->y[1][0].y) && 0 == fabs(s->y[1][0].z))
-        ro_transform_to_bc(nt, s->p, s->y[0], s->y[1]);
+        0 == fabs(s->y[1][0].x) && 0 == fabs(s->y[1][0].y) && 0 == fabs(s->y[1][0].z)) {
+        if (frame_center == RG_FRAME_BARY) ro_transform_to_bc(nt, s->p, s->y[0], s->y[1]);
+    } else if (frame_center == RG_FRAME_ASTRO) {
+        if (transform_to_ac(nt, s->md, s->y[0], s->y[1]) != RO_OK) {
+            ro_destroy(s);
+            return RO_ERR_ARG;
+        }
+    }
     /* pp_disk::transform_time / transform_velocity (pp_disk.cu:1512-1551) */
     for (int j = 0; j < nt; j++) s->epoch[j] *= GAUSS;
     for (int j = 0; j < nt; j++) {
@@ -496,8 +535,12 @@ static void event_elements(const ro_sys* s, const rg_vec_t* r, const rg_vec_t* v
         ra.x = ra.y = ra.z = 0.0;
         va.x = va.y = va.z = 0.0;
     }
+    if (s->frame == RG_FRAME_ASTRO) { /* pp_disk.cu:554-560: the coordinates as they are */
+        ra = r[idx];
+        ra.w = 0.0;
+        va = v[idx];
+    }
     rg_vec_t vt = {va.x * GAUSS, va.y * GAUSS, va.z * GAUSS, 0.0};
-    (void)s;
     ro_calculate_orbital_element(mu, oe, &ra, &vt);
 }
 
@@ -515,8 +558,18 @@ static void grav_block(ro_sys* s, double t_event, int sink_x, int sink_y, int sr
     const double f_rad = s->thr[RG_THRESHOLD_RADII_ENHANCE_FACTOR];
     const double M_star = p[0].mass;
     const double f3 = s->hill_factor * s->hill_factor * s->hill_factor;
+    const int astro = s->frame == RG_FRAME_ASTRO;
     for (int i = sink_x; i < sink_y; i++) {
-        a[i].x = a[i].y = a[i].z = a[i].w = 0.0;
+        if (!astro) {
+            a[i].x = a[i].y = a[i].z = a[i].w = 0.0;
+        } else {
+            /* pp_disk.cu:413-420: the star's pull as the starting value */
+            const double mu = mass_of_star(s) + p[i].mass;
+            const double r2 = SQR(r[i].x) + SQR(r[i].y) + SQR(r[i].z);
+            a[i].x = -mu / (r2 * sqrt(r2)) * r[i].x;
+            a[i].y = -mu / (r2 * sqrt(r2)) * r[i].y;
+            a[i].z = -mu / (r2 * sqrt(r2)) * r[i].z;
+        }
         if (0 < md[i].id) {
             rg_vec_t dVec = {0.0, 0.0, 0.0, 0.0};
             for (int j = src_x; j < src_y; j++) {
@@ -530,6 +583,13 @@ static void grav_block(ro_sys* s, double t_event, int sink_x, int sink_y, int sr
                 a[i].x += dVec.w * dVec.x;
                 a[i].y += dVec.w * dVec.y;
                 a[i].z += dVec.w * dVec.z;
+                if (astro) {
+                    /* pp_disk.cu:447-454: the indirect term of source j */
+                    const double r2 = SQR(r[j].x) + SQR(r[j].y) + SQR(r[j].z);
+                    a[i].x -= p[j].mass / (r2 * sqrt(r2)) * r[j].x;
+                    a[i].y -= p[j].mass / (r2 * sqrt(r2)) * r[j].y;
+                    a[i].z -= p[j].mass / (r2 * sqrt(r2)) * r[j].z;
+                }
                 s->n_pairs++;
 
                 if (record && i > 0 && i > j && d < f_rad * (p[i].radius + p[j].radius)) {
@@ -610,15 +670,18 @@ static void grav_block(ro_sys* s, double t_event, int sink_x, int sink_y, int sr
 }
 
 /* pp_disk::cpu_calc_grav_accel (pp_disk.cu:585-607) with the bounds of
- * number_of_bodies::get_bound_SI/NSI/NI (number_of_bodies.cpp:196-258), barycentric. */
+ * number_of_bodies::get_bound_SI/NSI/NI (number_of_bodies.cpp:196-258): the astrocentric
+ * frame starts the SI block's sinks and sources at 1, so the star's row is never written
+ * (its derivative buffers stay at their initial zero, pp_disk's calloc-like allocation). */
 static void cpu_calc_grav_accel(ro_sys* s, double curr_t, const rg_vec_t* r, const rg_vec_t* v,
                                 rg_vec_t* a, int record, int hill)
 {
     const int nsi = n_SI(s), nnsi = n_NSI(s), nni = n_NI(s), nm = n_massive(s);
     const double t_nsi = s->event_time_mode ? curr_t : s->t;
+    const int b = s->frame == RG_FRAME_ASTRO ? 1 : 0;
     record = record && s->inner_steps;
     s->n_gravity_evals++;
-    if (0 < nsi) grav_block(s, curr_t, 0, nsi, 0, nm, r, v, a, record, hill);
+    if (b < nsi) grav_block(s, curr_t, b, nsi, b, nm, r, v, a, record, hill);
     if (0 < nnsi) grav_block(s, t_nsi, nsi, nsi + nnsi, 0, nsi, r, v, a, record, hill);
     if (0 < nni) grav_block(s, t_nsi, nm, nm + nni, 0, nm, r, v, a, record, 0);
 }

@@ -27,6 +27,9 @@ typedef struct ro_sys ro_sys;
 int  ro_create(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v,
                const rg_param_t* p, const rg_body_metadata_t* md, const double* epoch,
                const double thr[RG_THRESHOLD_N], ro_sys** out);
+int  ro_create_in_frame(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v,
+                        const rg_param_t* p, const rg_body_metadata_t* md, const double* epoch,
+                        const double thr[RG_THRESHOLD_N], int frame_center, ro_sys** out);
 void ro_destroy(ro_sys* s);
 int  ro_set_integrator(ro_sys* s, int type, double dt_day, int adaptive, double tolerance,
                        int error_check_for_tp);

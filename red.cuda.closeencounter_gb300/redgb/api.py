@@ -33,6 +33,7 @@ def bind(lib, prefix, has_last_error=True):
     vp, ci, cd = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
     sigs = {
         "create": None,
+        "create_in_frame": None,
         "destroy": [vp],
         "set_integrator": [vp, ci, cd, ci, cd, ci],
         "set_event_options": [vp, ci, ci, cd, ci],
@@ -70,7 +71,7 @@ class System:
 
     prefix = "rg_"
 
-    def __init__(self, lib, disk, thr, event_capacity=0, _create_extra=True):
+    def __init__(self, lib, disk, thr, event_capacity=0, _create_extra=True, frame=T.FRAME_BARY):
         self._lib = lib
         self._f = lambda name: getattr(lib, self.prefix + name)
         self.handle = ctypes.c_void_p()
@@ -82,8 +83,10 @@ class System:
                 T.ptr(np.ascontiguousarray(disk.epoch)), T.ptr(thr)]
         if _create_extra:
             args.append(ctypes.c_int(event_capacity))
+        if frame != T.FRAME_BARY:
+            args.append(ctypes.c_int(frame))
         args.append(ctypes.byref(self.handle))
-        self._call("create", *args)
+        self._call("create" if frame == T.FRAME_BARY else "create_in_frame", *args)
 
     # ------------------------------------------------------------------ plumbing
     def _msg(self):

@@ -116,9 +116,9 @@ def read_body_file(path) -> Disk:
 
 def write_parameter_file(path, *, integrator="rkf8", tolerance=None, length_yr=1.0, output_interval_yr=None,
                          ejection=None, hit_centrum=None, collision_factor=None, error_check_for_tp=False,
-                         close_encounter=False, name="synthetic", output_type=None):
+                         close_encounter=False, name="synthetic", output_type=None, frame_center="bary"):
     """key = value parameter file read by parameter::parse (parameter.cpp:55-285)."""
-    lines = [f"name = {name}", "description = seeded synthetic disk", "frame_center = bary",
+    lines = [f"name = {name}", "description = seeded synthetic disk", f"frame_center = {frame_center}",
              f"integrator = {integrator}"]
     if tolerance is not None:
         lines.append(f"tolerance = {tolerance!r}")

@@ -50,8 +50,8 @@ class System(api.System):
 
     prefix = "rg_"
 
-    def __init__(self, disk, thr, event_capacity=0):
-        super().__init__(load(), disk, thr, event_capacity=event_capacity)
+    def __init__(self, disk, thr, event_capacity=0, frame=T.FRAME_BARY):
+        super().__init__(load(), disk, thr, event_capacity=event_capacity, frame=frame)
 
     def set_gravity_mode(self, mode):
         self._call("set_gravity_mode", self.handle, int(mode))

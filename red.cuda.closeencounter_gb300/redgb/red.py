@@ -109,8 +109,13 @@ def read_parameter_file(path):
                 raise ValueError(f"Invalid value at: {key}")
             prm["output_type"] = "binary" if value == "binary" else "text"
         elif key == "frame_center":
-            if value.lower() != "bary":
-                raise ValueError("frame_center: only the barycentric frame is implemented")
+            # parameter.cpp:257-266
+            if value.lower() == "astro":
+                prm["frame"] = T.FRAME_ASTRO
+            elif value.lower() == "bary":
+                prm["frame"] = T.FRAME_BARY
+            else:
+                raise ValueError(f"Invalid value at: {key}")
         else:
             raise ValueError(f"Invalid parameter: {key}")
     return prm
@@ -136,7 +141,7 @@ def run(argv):
     thr = bodies.thresholds(ejection=prm["ejection"], hit_centrum=prm["hit_centrum"],
                             collision_factor=prm["collision_factor"])
     binary = prm["output_type"] == "binary"
-    s = lib.System(disk, thr)
+    s = lib.System(disk, thr, frame=prm.get("frame", T.FRAME_BARY))
     s.set_integrator(prm["int_type"], 0.001, prm["adaptive"], prm["tolerance"], prm["error_check_for_tp"])
     s.set_event_options(close_encounter=prm["close_encounter"], inner_steps=prm["inner_steps"])
     s.set_time(prm["start_time"])
@@ -161,7 +166,7 @@ def run(argv):
 
         snapshot()
         ps, n = 0.0, 0
-        while s.state(internal=True)[4] <= stop:  # main.cu:176-263
+        while s.time(internal=True) <= stop:  # main.cu:176-263
             if oi <= abs(ps):
                 ps = 0.0
                 snapshot()

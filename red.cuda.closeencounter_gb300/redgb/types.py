@@ -42,6 +42,7 @@ EVENT_NAMES = ("NONE", "HIT_CENTRUM", "EJECTION", "CLOSE_ENCOUNTER", "COLLISION"
 
 GRAVITY_FP64, GRAVITY_MIXED = 0, 1
 EVENT_TIME_CPU, EVENT_TIME_STAGE = 0, 1
+FRAME_ASTRO, FRAME_BARY = 0, 1  # red_type.h:38-43 frame_center_t
 
 # red.cuda/red.type/red_constants.h:21-22
 GAUSS = 1.720209895e-2
@@ -93,7 +94,8 @@ class Counters(ctypes.Structure):
 class Profile(ctypes.Structure):
     """rg_profile_t: summed device time of timed launches."""
     _fields_ = [("gravity_launches", ctypes.c_int64), ("gravity_ms", ctypes.c_double),
-                ("stage_launches", ctypes.c_int64), ("stage_ms", ctypes.c_double)]
+                ("stage_launches", ctypes.c_int64), ("stage_ms", ctypes.c_double),
+                ("other_launches", ctypes.c_int64), ("other_ms", ctypes.c_double)]
 
 
 class Tune(ctypes.Structure):

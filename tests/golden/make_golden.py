@@ -141,6 +141,23 @@ def cases():
     d = bodies.make_disk(n_pl=16, seed=11, a_range=(1.0, 3.0), sigma_e=0.3, sigma_i=0.05, n_tp=4)
     out.append(("disk_eject_hit", d, dict(integrator="rkf8", tolerance=1e-10, length_yr=3.0, output_interval_yr=0.5,
                                           ejection=3.2, hit_centrum=0.3, collision_factor=1.0)))
+    # the astrocentric frame (frame_center = astro) on a self-interacting disk -- the reference's
+    # own CPU path gives NaN once planetesimals or test particles are present (their blocks take
+    # the star at the origin as a source) -- from barycentric input, so that the astrocentric
+    # transform at load (options.cpp:217-220) moves every body to the star
+    d = bodies.make_disk(n_pl=120, pl_type=T.BODY_PROTOPLANET, seed=17, m_range=(1e-7, 1e-5),
+                         giants=((9.55e-4, 5.2, 0.05), (2.86e-4, 9.54, 0.05)), a_range=(1.0, 1.3), sigma_e=0.05,
+                         sigma_i=0.02)
+    m = d.p["mass"]
+    for f in "xyz":
+        d.r[f] -= np.sum(m * d.r[f]) / np.sum(m)
+        d.v[f] -= np.sum(m * d.v[f]) / np.sum(m)
+    out.append(("disk_si_astro_collide", d, dict(integrator="rkf8", tolerance=1e-10, length_yr=2.0,
+                                                 output_interval_yr=0.25, ejection=100.0, hit_centrum=0.05,
+                                                 collision_factor=150.0, frame_center="astro")))
+    out.append(("disk_si_astro_ce", d, dict(integrator="rkf8", tolerance=1e-10, length_yr=0.5, output_interval_yr=0.1,
+                                            ejection=100.0, hit_centrum=0.05, collision_factor=150.0,
+                                            close_encounter=True, frame_center="astro")))
     # the plain FP64 planetesimal-disk workload: star, two giants, 1024 planetesimals (seed 0),
     # RKF7(8) at 1e-10 for 1000 years with collisions, ejection (100 AU) and hit-star (0.05 AU)
     # on; snapshots every 250 years

@@ -37,6 +37,10 @@ def thresholds_of(params):
     return bodies.thresholds(ejection=ej, hit_centrum=hit, collision_factor=cf)
 
 
+def frame_of(params):
+    return T.FRAME_ASTRO if params.get("frame_center") == "astro" else T.FRAME_BARY
+
+
 def configure(system, params):
     system.set_integrator(INT_TYPES[params["integrator"]], 0.001, params.get("tolerance") is not None,
                           params.get("tolerance") or 1e-10, params.get("error_check_for_tp", False))
@@ -116,4 +120,5 @@ def compare_events(events, ref):
 
 
 FIXTURES = ["twobody_euler", "n1_massive_n3", "disk_nsi_rkf78", "disk_si_rkf78_collide", "disk_si_rkf78_ce",
-            "disk_si_rk4_fixed", "disk_si_rk4_adaptive", "disk_eject_hit", "planetesimal_disk_1000yr"]
+            "disk_si_rk4_fixed", "disk_si_rk4_adaptive", "disk_eject_hit", "planetesimal_disk_1000yr",
+            "disk_si_astro_collide", "disk_si_astro_ce"]

@@ -20,7 +20,7 @@ CPU_FIXTURES = [f for f in H.FIXTURES if f != "twobody_euler"]
 @pytest.mark.parametrize("name", CPU_FIXTURES)
 def test_oracle_reproduces_reference_run(name):
     disk, params, result, events = H.load_fixture(name)
-    s = pyoracle.OracleSystem(disk, H.thresholds_of(params))
+    s = pyoracle.OracleSystem(disk, H.thresholds_of(params), frame=H.frame_of(params))
     snaps, evs, _ = H.run_fixture(s, params)
     assert H.compare_result(H.snapshots_as_result(snaps), result) == []
     assert H.compare_events(evs, events) == []

@@ -43,6 +43,9 @@ def test_parameter_file_and_output_names(tmp_path):
     assert os.path.basename(paths["event"]) == "R_gpu_ns_as_RKF8_event.txt"
     with open(path, "a") as f:
         f.write("frame_center = astro\n")
+    assert red.read_parameter_file(str(path))["frame"] == T.FRAME_ASTRO
+    with open(path, "a") as f:
+        f.write("frame_center = galactic\n")
     with pytest.raises(ValueError):
         red.read_parameter_file(str(path))
 
