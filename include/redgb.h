@@ -98,6 +98,26 @@ RG_API int rg_create(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v,
               const rg_param_t* p, const rg_body_metadata_t* md, const double* epoch,
               const double thr[RG_THRESHOLD_N], int event_capacity, rg_ctx** out);
 
+/*
+ * rg_create in a chosen frame: frame_center is RG_FRAME_BARY (rg_create) or RG_FRAME_ASTRO,
+ * the reference's parameter-file key `frame_center` (parameter.cpp:257-266) as
+ * options::create_pp_disk applies it (options.cpp:206-220): a system whose body 0 sits at
+ * rest in the origin is moved to its barycentre in the barycentric frame; any other system
+ * is moved to body 0, the star, in the astrocentric frame (tools.cpp:180-236).  The
+ * astrocentric frame follows the reference's CPU path: the self-interacting block's sinks
+ * and sources start at body 1 (number_of_bodies.cpp:205-222), each sink starts from the
+ * star's pull and every source adds its direct term and subtracts its indirect term
+ * (pp_disk.cu:413-454), the star's own acceleration stays zero, and close-encounter
+ * elements use the coordinates as they are (pp_disk.cu:554-560).  RG_ERR_NOT_IMPLEMENTED
+ * for the astrocentric frame with super-planetesimals, planetesimals or test particles:
+ * their blocks take the star, at the origin, as a source whose indirect term is
+ * m / (0 sqrt(0)) 0, so the reference's own run turns NaN at its first step; and for
+ * mixed-precision gravity (rg_set_gravity_mode) in that frame.
+ */
+RG_API int rg_create_in_frame(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,
+                              const rg_body_metadata_t* md, const double* epoch, const double thr[RG_THRESHOLD_N],
+                              int event_capacity, int frame_center, rg_ctx** out);
+
 /* Frees every host and device buffer of the context (pp_disk::~pp_disk, pp_disk.cu:1237). */
 RG_API int rg_destroy(rg_ctx* ctx);
 
@@ -297,12 +317,16 @@ RG_API int rg_get_dt(rg_ctx* ctx, double* dt_did_day, double* dt_try_day);
 /*
  * Many independent disks integrated together on one GPU (not in the reference, which
  * runs one disk per process).  Every disk follows the reference's RKF7(8) adaptive step
- * (int_rungekutta8.cu:704-797) with its own step size and clock; one attempt of all disks
- * is one CUDA-graph launch, the step-size controller runs on the device.  Collisions,
- * ejections and hit-star events follow the reference's rules (pp_disk.cu:683-1202); a disk
- * with an event pauses until the host has applied it.  Differences from rg_advance: the
- * controller's pow is the device's (the trial steps may differ from glibc's in the last
- * bit), and inactive bodies stay in storage (no compaction; indices do not change).
+ * (int_rungekutta8.cu:704-797) with its own step size and clock; the step-size controller
+ * runs on the device.  Collisions, ejections and hit-star events follow the reference's
+ * rules (pp_disk.cu:683-1202) and are applied on the device right after the attempt that
+ * found them (merges, retirements, the event records), as are the Hill-sphere records, so
+ * rg_ens_advance is one CUDA-graph launch whose conditional while-node repeats the attempt
+ * until every disk is done (in chunks of at most 4096 attempts per launch; the host only
+ * reads whether to launch the next).  Differences from rg_advance: the controller's pow and
+ * the merged radius's pow (tools.cpp:238-243) are the device's, which may differ from
+ * glibc's in the last bit, and inactive bodies stay in storage (no compaction; indices do
+ * not change).  Each disk has its own thresholds, collision factor included.
  */
 typedef struct rg_ens rg_ens;
 
@@ -322,7 +346,9 @@ RG_API int rg_ens_set_integrator(rg_ens* ens, double dt_day, double tol, int err
 RG_API int rg_ens_set_options(rg_ens* ens, int gravity_mode, double hill_factor, int use_graph);
 
 /* Integrates every disk until its clock exceeds t_stop_day (the reference's
- * `while (t <= stop)` loop) or max_attempts attempts (<= 0: no limit) were launched. */
+ * `while (t <= stop)` loop) or max_attempts attempts (<= 0: no limit) were run.  Event
+ * records of the interval are appended to the log rg_ens_events drains (at most
+ * 16 x the body count, between 4096 and 2^18 records per call: RG_ERR_EVENT_OVERFLOW beyond). */
 RG_API int rg_ens_advance(rg_ens* ens, double t_stop_day, int64_t max_attempts, int64_t* n_attempts);
 
 /* State of disk `sys` in file units (arrays of its n_total records; any may be NULL). */
@@ -342,6 +368,14 @@ RG_API int rg_ens_step_log(rg_ens* ens, rg_step_rec_t* out, int cap, int* n);
 
 /* Energy and angular momentum of disk `sys` (as rg_energy). */
 RG_API int rg_ens_energy(rg_ens* ens, int sys, double* energy, double angmom[3]);
+
+/* Kernel timing of the ensemble (no counterpart in the reference): with `on`, every attempt
+ * is launched directly, not as a graph replay, with CUDA events on the ensemble's stream
+ * around its force evaluations (gravity), its stage combinations and error norm (stage),
+ * and its other kernels (state copy, ejection screen, controller, features: other);
+ * rg_ens_get_profile sums their device times since the last call. */
+RG_API int rg_ens_set_profiling(rg_ens* ens, int on);
+RG_API int rg_ens_get_profile(rg_ens* ens, rg_profile_t* prof);
 
 /* The stream the ensemble launches on, and its kernel-launch count. */
 RG_API int rg_ens_get_stream(rg_ens* ens, void** stream);

@@ -31,6 +31,8 @@ struct DevEvent {
     int32_t kind;   // 0: radius criterion (pp_disk.cu:265), 1: mutual Hill sphere
     int32_t i, j;   // sink, source (body indices of the whole batch)
     int32_t sys, pad;
+    int32_t id1, id2;  // ensembles' device handler: survivor and merger ids, fixed before any merge
+    int32_t swap, pad2;  // ... and whether the source is the survivor
     double d;
     double t;  // ensembles: the system's time at the attempt's start (the Hill records' time)
     double ri[3], vi[3], rj[3], vj[3], r0[3], v0[3];
@@ -79,7 +81,20 @@ struct GravArgs {
     const unsigned int* sys_attempt;
     const unsigned int* sys_f0;
     const double* sys_t;  // per system: the time at the attempt's start
+    // astrocentric frame (single disks): per body the star's pull -mu / (r^2 |r|) r (rows 0-2,
+    // a sink's starting value) and the indirect term m / (r^2 |r|) r (rows 3-5, subtracted
+    // after each source's direct term), pp_disk.cu:413-420,447-454; nullptr: barycentric
+    const double* astro;
+    long long astro_stride;
+    // ensembles: per system collision factor (THRESHOLD_RADII_ENHANCE_FACTOR); nullptr: f_rad
+    const double* sys_f_rad;
 };
+
+// the collision factor of a tile's system
+__device__ __forceinline__ double tile_f_rad(const GravArgs& g, const Tile& t)
+{
+    return g.sys_f_rad ? g.sys_f_rad[t.sys] : g.f_rad;
+}
 
 // sequence tag of a record: (attempt << 8) | stage, or the step-start number for Hill
 __device__ __forceinline__ uint32_t record_seq(const GravArgs& g, const Tile& t, int kind)

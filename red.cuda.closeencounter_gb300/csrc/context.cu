@@ -88,6 +88,8 @@ struct rg_ctx {
     double* d_dt = nullptr;
     double* d_part = nullptr;
     double* d_records = nullptr;  // r and v as vec_t records (state in / out): 8 doubles per body
+    double* d_astro = nullptr;    // astrocentric frame: per body the star's pull and indirect term (6 rows)
+    int frame = RG_FRAME_BARY;    // pp_disk::frame_center
     double* h_pin = nullptr;  // pinned: [0] dt, [1] max bits, [2..3] counts, [4..5] d_counters
     // host mirrors of the body parameters (authoritative; the state lives on the device)
     std::vector<rg_param_t> p;
@@ -204,6 +206,7 @@ void free_all(rg_ctx* c)
     cudaFree(c->d_few_row0);
     cudaFree(c->d_ev);
     cudaFree(c->d_hill);
+    cudaFree(c->d_astro);
     cudaFree(c->d_counters);
     cudaFree(c->d_ej);
     cudaFree(c->d_ej_count);
@@ -348,12 +351,19 @@ void build_tiles(rg_ctx* c)
         int s0, s1, src1, block;
     } blks[3] = {{0, nsi, nm, 0}, {nsi, nm, nsi, 1}, {nm, nt, nm, 2}};
     c->pairs_per_eval = (int64_t)nsi * (nm > 0 ? nm - 1 : 0) + (int64_t)(nm - nsi) * nsi + (int64_t)(nt - nm) * nm;
+    // the astrocentric frame starts the SI block's sinks and sources at body 1
+    // (number_of_bodies.cpp:205-222); only self-interacting systems take it
+    const int src0 = c->frame == RG_FRAME_ASTRO ? 1 : 0;
+    if (src0) {
+        blks[0].s0 = 1;
+        c->pairs_per_eval = nsi > 1 ? (int64_t)(nsi - 1) * (nm - 2) : 0;
+    }
 
     auto add_group = [&](int mode, int kind, int s0, int s1, int src1, int block, int step) {
         if (s1 <= s0) return;
         rg_ctx::Group gr{kind, c->tiles.size(), 0, c->few_rows, 0, src1, std::min(step, s1 - s0)};
         for (int s = s0; s < s1; s += step) {
-            c->tiles.push_back(Tile{s, std::min(s + step, s1), 0, src1, 0, 0, block, 0});
+            c->tiles.push_back(Tile{s, std::min(s + step, s1), block == 0 ? src0 : 0, src1, 0, 0, block, 0});
             c->heavy_mx.push_back(kind == GROUP_MIXED ? std::min(n_heavy, src1) : 0);
             if (kind == GROUP_FEW_SERIAL || kind == GROUP_DF_FEW) {
                 c->few_row0.push_back(c->few_rows);
@@ -378,6 +388,10 @@ void build_tiles(rg_ctx* c)
     for (const auto& b : blks) {
         if (b.s1 <= b.s0) continue;
         const int ns = b.s1 - b.s0;
+        if (src0) {  // the astrocentric terms are in the pair-parallel kernel only
+            add_group(0, GROUP_PAIRPAR, b.s0, b.s1, b.src1, b.block, c->pairpar_S);
+            continue;
+        }
         if (b.src1 <= c->rowseq_max_src) {  // few sources: thread per sink (same tiles in both modes)
             add_group(0, GROUP_ROWSEQ, b.s0, b.s1, b.src1, b.block, 128);
             c->plan[1].push_back(c->plan[0].back());
@@ -453,6 +467,8 @@ int sync_tiles(rg_ctx* c)
     return RG_OK;
 }
 
+double mass_of_star(const rg_ctx* c);
+
 // --------------------------------------------------------------------- one force evaluation
 // pp_disk::calc_dydx(1, ...) (pp_disk.cu:998-1041): accelerations of the stage positions
 // `pos` (3 rows) into `acc` (3 rows); `vel` (3 rows) are the stage velocities, read only
@@ -502,6 +518,14 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
     c->n_gravity_evals++;
     c->n_pairs += c->pairs_per_eval;
     const long prof = prof_begin(c, 0);
+    if (c->frame == RG_FRAME_ASTRO) {
+        rc = launch_astro_terms(g.px, g.py, g.pz, c->d_mass, c->n_massive(), mass_of_star(c), c->d_astro,
+                                (long long)cap, c->st);
+        if (rc) return rc;
+        c->n_kernels++;
+        g.astro = c->d_astro;
+        g.astro_stride = (long long)cap;
+    }
     bool split_done = false;
     // with a mixed group, the double-float row groups (a few sinks: star, giants) run on a
     // side stream beside it: they write other rows and append events atomically
@@ -710,8 +734,14 @@ int collect_events(rg_ctx* c)
             }
             if (kind == 0 && c->close_encounter) {
                 const double ms = mass_of_star(c);
-                event_elements(rs, vs, d.r0, d.v0, GAUSS2 * (ms + c->p[surv].mass), &e.oe1);
-                event_elements(rm, vm, d.r0, d.v0, GAUSS2 * (ms + c->p[merg].mass), &e.oe2);
+                // barycentric: relative to the star (transform_to_ac of a copy, pp_disk.cu:529-552);
+                // astrocentric: the coordinates as they are (pp_disk.cu:554-560)
+                static const double zero[3] = {0.0, 0.0, 0.0};
+                const bool astro = c->frame == RG_FRAME_ASTRO;
+                event_elements(rs, vs, astro ? zero : d.r0, astro ? zero : d.v0, GAUSS2 * (ms + c->p[surv].mass),
+                               &e.oe1);
+                event_elements(rm, vm, astro ? zero : d.r0, astro ? zero : d.v0, GAUSS2 * (ms + c->p[merg].mass),
+                               &e.oe2);
             }
             out.push_back(e);
         }
@@ -1295,10 +1325,16 @@ int rg_device_count(void)
 
 static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,
                        const rg_body_metadata_t* md, const double* epoch, const double thr[RG_THRESHOLD_N],
-                       int event_capacity, rg_ctx** out)
+                       int event_capacity, int frame, rg_ctx** out)
 {
     if (!n || !r || !v || !p || !md || !thr || !out) return set_error(RG_ERR_ARG, "null argument");
     *out = nullptr;
+    if (frame != RG_FRAME_BARY && frame != RG_FRAME_ASTRO) return set_error(RG_ERR_ARG, "frame_center");
+    if (frame == RG_FRAME_ASTRO && (n->n_spl > 0 || n->n_pl > 0 || n->n_tp > 0))
+        return set_error(RG_ERR_NOT_IMPLEMENTED,
+                         "the astrocentric frame with super-planetesimals, planetesimals or test particles: their "
+                         "blocks take the star at the origin as a source, whose indirect term m / (0 sqrt(0)) 0 "
+                         "makes the reference's accelerations NaN (pp_disk.cu:447-454)");
     const int32_t* cn = &n->n_s;
     int64_t tot = 0;
     for (int k = 0; k < 7; k++) {
@@ -1307,7 +1343,10 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
     }
     if (tot <= 0 || tot > (1 << 28)) return set_error(RG_ERR_ARG, "body count out of range");
     if (rg_device_count() <= 0) return set_error(RG_ERR_NO_DEVICE, "no CUDA device");
+    if (frame == RG_FRAME_ASTRO && md[0].body_type != RG_BODY_STAR)
+        return set_error(RG_ERR_ARG, "the astrocentric frame needs the star as body 0 (\"No star is included!\")");
     rg_ctx* c = new rg_ctx();
+    c->frame = frame;
     for (int k = 0; k < 7; k++) c->cnt[k] = cn[k];
     const int nt = (int)tot;
     c->cap = nt;
@@ -1354,6 +1393,14 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
     chk(dalloc(&c->d_screen_slot, nt));
     if (!rc && cudaMallocHost((void**)&c->h_pin, 8 * sizeof(double)) != cudaSuccess)
         chk(set_error(RG_ERR_NOMEM, "pinned host buffer"));
+    if (frame == RG_FRAME_ASTRO) {
+        chk(dalloc(&c->d_astro, (size_t)6 * nt));
+        // the star's row of every derivative buffer is never written in this frame
+        // (get_bound_SI starts at 1) and stays zero, as the reference's cleared host buffers do
+        for (auto& k : c->d_k)
+            if (!rc && k && cudaMemsetAsync(k, 0, (size_t)6 * nt * sizeof(double), c->st) != cudaSuccess)
+                chk(set_error(RG_ERR_CUDA, "cudaMemsetAsync"));
+    }
     if (rc) {
         free_all(c);
         delete c;
@@ -1368,8 +1415,21 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
     if (epoch)
         for (int i = 0; i < nt; i++) c->epoch[i] = epoch[i];
     for (int k = 0; k < RG_THRESHOLD_N; k++) c->thr[k] = thr[k];
-    if (0 == std::fabs(rr[0].x) && 0 == std::fabs(rr[0].y) && 0 == std::fabs(rr[0].z) && 0 == std::fabs(vv[0].x) &&
-        0 == std::fabs(vv[0].y) && 0 == std::fabs(vv[0].z)) {
+    const bool at_rest_in_origin = 0 == std::fabs(rr[0].x) && 0 == std::fabs(rr[0].y) && 0 == std::fabs(rr[0].z) &&
+                                   0 == std::fabs(vv[0].x) && 0 == std::fabs(vv[0].y) && 0 == std::fabs(vv[0].z);
+    if (!at_rest_in_origin && frame == RG_FRAME_ASTRO) {
+        // tools.cpp:180-236 get_star_bc_phase + transform_to_ac, loop j = n-1 .. 0
+        const rg_vec_t R0 = rr[0], V0 = vv[0];
+        for (int j = nt - 1; j >= 0; j--) {
+            rr[j].x -= R0.x;
+            rr[j].y -= R0.y;
+            rr[j].z -= R0.z;
+            vv[j].x -= V0.x;
+            vv[j].y -= V0.y;
+            vv[j].z -= V0.z;
+        }
+    }
+    if (at_rest_in_origin && frame == RG_FRAME_BARY) {
         // tools.cpp:109-178 compute_bc + transform_to_bc, loops j = n-1 .. 0
         rg_vec_t R0{0, 0, 0, 0}, V0{0, 0, 0, 0};
         for (int j = nt - 1; j >= 0; j--) {
@@ -1429,7 +1489,14 @@ int rg_create(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v, const 
               const rg_body_metadata_t* md, const double* epoch, const double thr[RG_THRESHOLD_N], int event_capacity,
               rg_ctx** out)
 {
-    RG_GUARD(create_impl(n, r, v, p, md, epoch, thr, event_capacity, out));
+    RG_GUARD(create_impl(n, r, v, p, md, epoch, thr, event_capacity, RG_FRAME_BARY, out));
+}
+
+int rg_create_in_frame(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,
+                       const rg_body_metadata_t* md, const double* epoch, const double thr[RG_THRESHOLD_N],
+                       int event_capacity, int frame_center, rg_ctx** out)
+{
+    RG_GUARD(create_impl(n, r, v, p, md, epoch, thr, event_capacity, frame_center, out));
 }
 
 int rg_destroy(rg_ctx* c)
@@ -1476,6 +1543,8 @@ int rg_set_event_options(rg_ctx* c, int close_encounter, int inner_steps, double
 int rg_set_gravity_mode(rg_ctx* c, int mode)
 {
     if (!c || (mode != RG_GRAVITY_FP64 && mode != RG_GRAVITY_MIXED)) return set_error(RG_ERR_ARG, "bad gravity mode");
+    if (mode == RG_GRAVITY_MIXED && c->frame == RG_FRAME_ASTRO)
+        return set_error(RG_ERR_NOT_IMPLEMENTED, "mixed-precision gravity in the astrocentric frame");
     c->gravity_mode = mode;
     return RG_OK;
 }
@@ -1764,6 +1833,8 @@ static int calc_accel_impl(rg_ctx* c, rg_vec_t* a)
     RG_CUDA_CHECK(cudaStreamSynchronize(c->st));
     if ((rc = kernel_flag_error(c, flag))) return rc;
     for (int i = 0; i < n; i++) a[i] = rg_vec_t{h[i], h[(size_t)n + i], h[(size_t)2 * n + i], 0.0};
+    // astrocentric frame: the star's row is not evaluated (its derivative stays zero)
+    if (c->frame == RG_FRAME_ASTRO && n > 0) a[0] = rg_vec_t{0.0, 0.0, 0.0, 0.0};
     return RG_OK;
 }
 
@@ -1831,9 +1902,12 @@ int rg_get_profile(rg_ctx* c, rg_profile_t* prof)
         if (c->ev_kind[k] == 0) {
             prof->gravity_launches++;
             prof->gravity_ms += ms;
-        } else {
+        } else if (c->ev_kind[k] == 1) {
             prof->stage_launches++;
             prof->stage_ms += ms;
+        } else {
+            prof->other_launches++;
+            prof->other_ms += ms;
         }
     }
     c->ev_kind.clear();

@@ -4,18 +4,21 @@
 // Layout: the disks' bodies are concatenated (disk s owns [base_s, base_s + n_s)), with the
 // same structure-of-arrays rows as a single context (common.cuh).  Per-disk scalars (clock,
 // trial step, status, error maximum, counters) live on the device, so one attempt of every
-// running disk is a fixed sequence of launches -- captured once as a CUDA graph:
+// running disk is a fixed sequence of launches:
 //
-//   stage 0 (disks that start a new step) -> 12 stage combines + force evaluations ->
-//   y_{n+1} -> error maximum per disk -> step-size controller (one thread per disk) ->
-//   accepted disks copy y_{n+1} into y and screen for ejection / hit-star -> finalize.
+//   stage 0 (disks that start a new step) -> Hill-sphere records -> 12 stage combines +
+//   force evaluations -> y_{n+1} -> error maximum per disk -> step-size controller (one
+//   thread per disk) -> accepted disks copy y_{n+1} into y and screen for ejection /
+//   hit-star -> finalize -> event handling (merges, ejections, hit-star, ens_events.cu) ->
+//   loop condition.
 //
-// Kernels take per-disk activity masks, so finished or paused disks cost nothing but an
-// early exit.  A disk whose accepted step recorded a collision (or whose new state has an
-// ejection / hit-star candidate) is held; the host then applies the reference's handlers
-// (pp_disk.cu:717-738,934-976,1078-1202) to that disk's state and releases it.  Differences
-// from the single-disk path: the controller's pow is the device's (trial steps may differ
-// from glibc's in the last bit), and inactive bodies are not compacted away.
+// That sequence is captured once as the body of a CUDA graph's conditional while-node, whose
+// last kernel sets the condition, so one graph launch runs attempt after attempt until every
+// disk is done (bounded chunks of attempts per launch).  Kernels take per-disk activity
+// masks, so finished disks cost nothing but an early exit.  Differences from the single-disk
+// path: the controller's pow and the merged radius's pow are the device's (trial steps and
+// merged radii may differ from glibc's in the last bit), and inactive bodies are not
+// compacted away.
 //
 // Built with -fmad=false: the stage combinations and the error norm keep the reference's
 // operation order.
@@ -31,6 +34,7 @@
 #include "../../include/redgb.h"
 #include "abi_guard.h"
 #include "common.cuh"
+#include "ens_events.h"
 #include "host_tools.h"
 #include "kernels.h"
 #include "rk_tables.h"
@@ -330,60 +334,42 @@ __global__ void ens_finalize_kernel(EnsSys s)
 }
 
 // features of a step start: max |a| and min (d / mutual Hill radius)^3 over the pairs of
-// every body with a massive non-star self-interacting body (float bits: positive floats
-// order like unsigned integers)
-__global__ void ens_feat_reset_kernel(EnsSys s, unsigned int* amax, unsigned int* hill3)
+// every body with a massive non-star self-interacting body, in FP32 (the features are
+// logarithms fed to an FP32 network; GB300 spends about 64 FP32 issue slots per FP64
+// operation).  One body's contribution; b is its disk's body 0, ns the disk's SI count.
+__device__ __forceinline__ void body_features(const double* y, const double* k0, const double* mass, const int* id,
+                                              long long stride, int b, int ns, int i, float& am, float& h3)
 {
-    const int d = blockIdx.x * blockDim.x + threadIdx.x;
-    if (d >= s.n || !s.active_f0[d]) return;
-    amax[d] = 0u;
-    hill3[d] = __float_as_uint(3.0e38f);
-}
-
-__global__ void ens_feat_kernel(const StageTile* tiles, const int* mask, const double* y, const double* k0,
-                                const double* mass, const int* id, const int* base_of, const int* nsi_of, int stride,
-                                unsigned int* amax, unsigned int* hill3)
-{
-    // FP32 arithmetic: the features are logarithms fed to an FP32 network, and GB300 spends
-    // about 64 FP32 issue slots per FP64 operation
-    const StageTile t = tiles[blockIdx.x];
-    if (!mask[t.sys]) return;
-    float am = 0.0f, h3 = 3.0e38f;
-    for (int i = t.b0 + threadIdx.x; i < t.b1; i += blockDim.x) {
-        if (id[i] <= 0) continue;
-        const float ax = (float)k0[3LL * stride + i], ay = (float)k0[4LL * stride + i], az = (float)k0[5LL * stride + i];
-        am = fmaxf(am, sqrtf(ax * ax + ay * ay + az * az));
-        const int b = base_of[i], ns = nsi_of[i];
-        const float M = (float)mass[b];
-        const float x0 = (float)y[b], y0 = (float)y[stride + b], z0 = (float)y[2LL * stride + b];
-        const float xi = (float)y[i] - x0, yi = (float)y[stride + i] - y0, zi = (float)y[2LL * stride + i] - z0;
-        const float ri = sqrtf(xi * xi + yi * yi + zi * zi);
-        const float mi = (float)mass[i];
-        for (int j = b + 1; j < b + ns; j++) {
-            if (j == i || id[j] <= 0) continue;
-            const float xj = (float)y[j] - x0, yj = (float)y[stride + j] - y0, zj = (float)y[2LL * stride + j] - z0;
-            const float dx = xj - xi, dy = yj - yi, dz = zj - zi;
-            const float d2 = dx * dx + dy * dy + dz * dz;
-            const float rj = sqrtf(xj * xj + yj * yj + zj * zj);
-            const float hh = 0.5f * (ri + rj);
-            const float rh3 = (mi + (float)mass[j]) / (3.0f * M) * hh * hh * hh;
-            if (rh3 > 0.0f) h3 = fminf(h3, d2 * sqrtf(d2) / rh3);
-        }
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-        am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, off));
-        h3 = fminf(h3, __shfl_xor_sync(0xffffffffu, h3, off));
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicMax(&amax[t.sys], __float_as_uint(am));
-        atomicMin(&hill3[t.sys], __float_as_uint(h3));
+    if (id[i] <= 0) return;
+    const float ax = (float)k0[3LL * stride + i], ay = (float)k0[4LL * stride + i], az = (float)k0[5LL * stride + i];
+    am = fmaxf(am, sqrtf(ax * ax + ay * ay + az * az));
+    const float M = (float)mass[b];
+    const float x0 = (float)y[b], y0 = (float)y[stride + b], z0 = (float)y[2LL * stride + b];
+    const float xi = (float)y[i] - x0, yi = (float)y[stride + i] - y0, zi = (float)y[2LL * stride + i] - z0;
+    const float ri = sqrtf(xi * xi + yi * yi + zi * zi);
+    const float mi = (float)mass[i];
+    for (int j = b + 1; j < b + ns; j++) {
+        if (j == i || id[j] <= 0) continue;
+        const float xj = (float)y[j] - x0, yj = (float)y[stride + j] - y0, zj = (float)y[2LL * stride + j] - z0;
+        const float dx = xj - xi, dy = yj - yi, dz = zj - zi;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float rj = sqrtf(xj * xj + yj * yj + zj * zj);
+        const float hh = 0.5f * (ri + rj);
+        const float rh3 = (mi + (float)mass[j]) / (3.0f * M) * hh * hh * hh;
+        if (rh3 > 0.0f) h3 = fminf(h3, d2 * sqrtf(d2) / rh3);
     }
 }
 
 struct PropArgs {
     EnsSys s;
-    const unsigned int* amax;
-    const unsigned int* hill3;
+    const double* y;
+    const double* k0;
+    const double* mass;
+    const int* id;
+    const int* base;  // per disk: body 0
+    const int* nsi;   // per disk: self-interacting bodies
+    const int* ntot;  // per disk: bodies
+    long long stride;
     const __nv_bfloat16* w;  // nullptr: features only
     float mean[8], inv_std[8];
     float safety;
@@ -399,17 +385,39 @@ __device__ __forceinline__ double dither_uniform(unsigned long long seed, int d,
     return (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
 }
 
-// one warp per disk that starts a step: features -> network -> trial step
-__global__ void __launch_bounds__(128) ens_propose_kernel(PropArgs a)
+// one CTA per disk that starts a step: features (a pass over the disk's bodies, block
+// reductions), then in the first warp the network and the trial step
+__global__ void __launch_bounds__(256) ens_propose_kernel(PropArgs a)
 {
-    const int d = blockIdx.x * 4 + (threadIdx.x >> 5);
-    const int lane = threadIdx.x & 31;
+    const int d = blockIdx.x;
     const EnsSys& s = a.s;
-    if (d >= s.n || !s.active_f0[d]) return;
+    if (!s.active_f0[d]) return;
+    __shared__ float red_am[8], red_h3[8];
+    float am = 0.0f, h3 = 3.0e38f;
+    {
+        const int b = a.base[d], ns = a.nsi[d], n = a.ntot[d];
+        for (int i = b + threadIdx.x; i < b + n; i += blockDim.x)
+            body_features(a.y, a.k0, a.mass, a.id, a.stride, b, ns, i, am, h3);
+        for (int off = 16; off > 0; off >>= 1) {
+            am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, off));
+            h3 = fminf(h3, __shfl_xor_sync(0xffffffffu, h3, off));
+        }
+        if ((threadIdx.x & 31) == 0) {
+            red_am[threadIdx.x >> 5] = am;
+            red_h3[threadIdx.x >> 5] = h3;
+        }
+        __syncthreads();
+        if (threadIdx.x >= 32) return;
+        am = threadIdx.x < (blockDim.x >> 5) ? red_am[threadIdx.x] : 0.0f;
+        h3 = threadIdx.x < (blockDim.x >> 5) ? red_h3[threadIdx.x] : 3.0e38f;
+        for (int off = 16; off > 0; off >>= 1) {
+            am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, off));
+            h3 = fminf(h3, __shfl_xor_sync(0xffffffffu, h3, off));
+        }
+    }
+    const int lane = threadIdx.x & 31;
     const float* h = s.hist + 5 * d;
     float f[8];
-    const float am = __uint_as_float(a.amax[d]);
-    const float h3 = __uint_as_float(a.hill3[d]);
     f[0] = h3 < 1.0e38f ? log10f(fmaxf(h3, 1e-30f)) / 3.0f : 6.0f;
     f[1] = log10f(fmaxf(am, 1e-30f));
     f[2] = s.dt_last[d] > 0.0 ? (float)log10(s.dt_last[d] / 1.720209895e-2) : -3.0f;
@@ -573,27 +581,48 @@ struct rg_ens {
     int *d_row_sink = nullptr, *d_row_nsrc = nullptr, *d_row_sys = nullptr;
     double* d_terms = nullptr;
     int64_t pairs_per_eval = 0;
-    // events
+    // events: raw records of one attempt, handled on the device (ens_events.cu)
     DevEvent* d_ev = nullptr;
     unsigned int* d_ev_count = nullptr;
     DevEvent* d_hill = nullptr;
     unsigned int* d_hill_count = nullptr;
     unsigned int* d_kerr = nullptr;  // set by a gravity kernel whose tile copy timed out
     unsigned int ev_cap = 0;
+    rg_param_t* d_prm = nullptr;     // authoritative body parameters (merges change them)
+    double* d_f_rad = nullptr;       // per disk collision factor
+    int *d_base = nullptr, *d_ntot = nullptr, *d_nsi = nullptr;
+    long long* d_hill_set = nullptr;  // per disk 2 x HILL_SET_CAP pair keys
+    int *d_hill_n = nullptr, *d_hill_which = nullptr;
+    EnsLogRec* d_elog = nullptr;     // the event log, drained when an advance ends
+    unsigned int* d_elog_count = nullptr;
+    unsigned int elog_cap = 0;
+    unsigned int* d_elog_seq = nullptr;
+    unsigned int* d_flags = nullptr;  // ENS_FLAG_* bits
+    unsigned int* d_hit_slots = nullptr;
+    int* d_keep = nullptr;
+    long long* d_attempts = nullptr;  // [0] attempts of the current advance, [1] its limit,
+                                      // [2] the end of the current launch's chunk
     std::vector<std::pair<int, rg_event_t>> log;
-    std::vector<std::vector<int64_t>> hill_prev;
-    std::vector<int64_t> hill_last;  // f0 index of the last processed Hill set per disk
     // options
     int has_int = 0, ectp = 0, gravity_mode = RG_GRAVITY_FP64, use_graph = 1;
     double tol = 1e-10, dt0 = 0.0, hill_factor = 0.0;
     float near_ratio = 1.0e-5f;
     int started = 0;
-    // graph
+    // graph: a conditional while-node whose body is one attempt (its last kernel sets the
+    // condition), so that one launch runs attempts until every disk is done
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
+    cudaGraphConditionalHandle cond = 0;
     bool graph_valid = false;
     int64_t n_kernels = 0, n_graph_launches = 0, n_attempts = 0;
     int64_t kernels_per_attempt = 0;
+    // profiling (rg_ens_set_profiling): CUDA events around each launch group of an attempt,
+    // by kind (0 gravity, 1 stage combination / error norm, 2 the rest); attempts are then
+    // launched directly instead of through the graph
+    int profiling = 0;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<int> ev_kind;
+    size_t ev_used = 0;
     double* d_part = nullptr;
     int* d_base_of = nullptr;  // per body: index of its disk's body 0
     rg_step_rec_t* d_log = nullptr;
@@ -607,8 +636,6 @@ struct rg_ens {
     float* d_hist = nullptr;
     int *d_proposed = nullptr, *d_step_prop_rej = nullptr, *d_prop_rej_steps = nullptr, *d_cool = nullptr;
     long long *d_nprop = nullptr, *d_nprop_acc = nullptr, *d_nfallback = nullptr;
-    unsigned int *d_amax = nullptr, *d_hill3 = nullptr;
-    int* d_nsi_of = nullptr;
     const rg_mlp* mlp = nullptr;
     float mlp_mean[8] = {0}, mlp_inv_std[8] = {1, 1, 1, 1, 1, 1, 1, 1};
     float safety = 0.95f;
@@ -634,6 +661,9 @@ constexpr double GAUSS = 1.720209895e-2;
 constexpr double GAUSS2 = 2.959122082855911025e-4;
 constexpr int STAGE_TILE = 2048;
 constexpr int ENS_FEW_BLOCK = 32;
+constexpr int HILL_SET_CAP = 256;  // pairs inside their Hill spheres per disk
+constexpr int HIT_CAP = 64;        // hit-star records per disk and check
+constexpr long long ATTEMPT_CHUNK = 4096;  // attempts per graph launch at most
 // the FP64 plan uses the first three kinds; the mixed-precision plan uses MIXED, DF_ROWSEQ
 // and DF_FEW (double-float heavy pairs)
 enum {
@@ -669,14 +699,42 @@ void free_all(rg_ens* e)
                     e->d_tiles, e->d_heavy, e->d_few_row0, e->d_row_sink, e->d_row_nsrc, e->d_row_sys, e->d_terms,
                     e->d_ev, e->d_ev_count, e->d_hill, e->d_hill_count, e->d_part, e->d_base_of, e->d_log,
                     e->d_log_count, e->d_feat, e->d_dt_last, e->d_ideal_last, e->d_hist, e->d_proposed, e->d_step_prop_rej,
-                    e->d_prop_rej_steps, e->d_cool, e->d_nprop, e->d_nprop_acc, e->d_nfallback, e->d_amax,
-                    e->d_hill3, e->d_nsi_of, e->d_kerr, e->d_rf, e->d_smax, e->d_screen_slot};
+                    e->d_prop_rej_steps, e->d_cool, e->d_nprop, e->d_nprop_acc, e->d_nfallback,
+                    e->d_kerr, e->d_rf, e->d_smax, e->d_screen_slot, e->d_prm,
+                    e->d_f_rad, e->d_base, e->d_ntot, e->d_nsi, e->d_hill_set, e->d_hill_n, e->d_hill_which,
+                    e->d_elog, e->d_elog_count, e->d_elog_seq, e->d_flags, e->d_hit_slots, e->d_keep,
+                    e->d_attempts};
     for (void* q : ptrs) cudaFree(q);
     for (auto& k : e->d_k) cudaFree(k);
     if (e->st) cudaStreamDestroy(e->st);
     if (e->st2) cudaStreamDestroy(e->st2);
     if (e->ev_fork) cudaEventDestroy(e->ev_fork);
     if (e->ev_join) cudaEventDestroy(e->ev_join);
+    for (auto ev : e->ev_pool) cudaEventDestroy(ev);
+}
+
+// ------------------------------------------------------------------- profiling
+constexpr size_t ENS_MAX_PROFILE_PAIRS = 1 << 18;
+
+// opens a timed launch group of `kind` on the ensemble's stream; returns its index or -1
+long prof_begin(rg_ens* e, int kind)
+{
+    if (!e->profiling || e->ev_used / 2 >= ENS_MAX_PROFILE_PAIRS) return -1;
+    while (e->ev_pool.size() < e->ev_used + 2) {
+        cudaEvent_t ev;
+        if (cudaEventCreate(&ev) != cudaSuccess) return -1;
+        e->ev_pool.push_back(ev);
+    }
+    cudaEventRecord(e->ev_pool[e->ev_used], e->st);
+    e->ev_kind.push_back(kind);
+    const long idx = (long)e->ev_used;
+    e->ev_used += 2;
+    return idx;
+}
+
+void prof_end(rg_ens* e, long idx)
+{
+    if (idx >= 0) cudaEventRecord(e->ev_pool[(size_t)idx + 1], e->st);
 }
 
 // ------------------------------------------------------------------- plans
@@ -842,8 +900,10 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
     g.ax = acc;
     g.ay = acc + cap;
     g.az = acc + 2 * cap;
-    // one collision factor for the ensemble (the first disk's): the kernels take a scalar
-    g.f_rad = e->thr[RG_THRESHOLD_RADII_ENHANCE_FACTOR];
+    // each disk's own collision factor (sys_f_rad); the largest decides whether any records
+    g.f_rad = 0.0;
+    for (int s2 = 0; s2 < e->n_sys; s2++) g.f_rad = std::max(g.f_rad, e->thr[5 * (size_t)s2 + 2]);
+    g.sys_f_rad = e->d_f_rad;
     g.hill_f3 = e->hill_factor * e->hill_factor * e->hill_factor;
     g.f_rad_f = (float)g.f_rad;
     g.hill_f3_f = (float)g.hill_f3;
@@ -1002,51 +1062,139 @@ int launch_stage(rg_ens* e, int form, int nterm, const int* stages, const double
     return RG_OK;
 }
 
-// The launch sequence of one attempt of every running disk (captured as a graph).
-int record_attempt(rg_ens* e)
+EnsEventArgs event_args(rg_ens* e)
+{
+    EnsEventArgs a{};
+    a.n_sys = e->n_sys;
+    a.base = e->d_base;
+    a.ntot = e->d_ntot;
+    a.nsi = e->d_nsi;
+    a.stride = e->cap;
+    a.y = e->d_y;
+    a.mass = e->d_mass;
+    a.radius = e->d_radius;
+    a.prm = e->d_prm;
+    a.id = e->d_id;
+    a.type = e->d_type;
+    a.thr = e->d_thr;
+    a.status = e->d_status;
+    a.active = e->d_active;
+    a.active_f0 = e->d_active_f0;
+    a.t = e->d_t;
+    a.t_prev = e->d_tprev;
+    a.t_stop = e->d_tstop;
+    a.dt_did = e->d_dt_did;
+    a.acc_attempt = e->d_acc_attempt;
+    a.ej = e->d_ej;
+    a.ev = e->d_ev;
+    a.ev_count = e->d_ev_count;
+    a.ev_cap = e->ev_cap;
+    a.hill = e->d_hill;
+    a.hill_count = e->d_hill_count;
+    a.hill_set = e->d_hill_set;
+    a.hill_n = e->d_hill_n;
+    a.hill_which = e->d_hill_which;
+    a.hill_set_cap = HILL_SET_CAP;
+    a.log = e->d_elog;
+    a.log_count = e->d_elog_count;
+    a.log_cap = e->elog_cap;
+    a.log_seq = e->d_elog_seq;
+    a.flags = e->d_flags;
+    a.hit_slots = e->d_hit_slots;
+    a.hit_cap = HIT_CAP;
+    for (int r = 0; r < 13; r++) a.stage_c[r] = rk8_c[r];
+    return a;
+}
+
+EnsLoopArgs loop_args(rg_ens* e, bool in_graph)
+{
+    EnsLoopArgs l{};
+    l.n_sys = e->n_sys;
+    l.status = e->d_status;
+    l.active = e->d_active;
+    l.active_f0 = e->d_active_f0;
+    l.flags = e->d_flags;
+    l.kerr = e->d_kerr;
+    l.step_log_count = e->d_log_count;
+    l.step_log_cap = e->log_cap;
+    l.ev_count = e->d_ev_count;
+    l.hill_count = e->d_hill_count;
+    l.ev_cap = e->ev_cap;
+    l.attempts = e->d_attempts;
+    l.keep = e->d_keep;
+    l.cond = e->cond;
+    l.use_cond = in_graph ? 1 : 0;
+    return l;
+}
+
+// The launch sequence of one attempt of every running disk, with the handling of its events
+// and the loop condition (captured as the body of the graph's while-node).
+int record_attempt(rg_ens* e, bool in_graph)
 {
     const size_t cap = (size_t)e->cap;
     const int ns = (int)e->stiles.size();
     const int nb = (e->n_sys + 127) / 128;
     // stage 0 for the disks that start a new step: k0 = (v, a(y))
+    long pr = prof_begin(e, 2);
     ens_copy_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active_f0, e->d_y, 3, e->d_k[0], 0, 3, e->cap);
+    prof_end(e, pr);
     RG_CUDA_CHECK(cudaGetLastError());
     e->n_kernels++;
+    pr = prof_begin(e, 0);
     int rc = ens_gravity(e, e->d_y, e->d_y + 3 * cap, e->d_k[0] + 3 * cap, 0, e->d_active_f0, e->hill_factor > 0.0);
+    prof_end(e, pr);
     if (rc) return rc;
+    pr = prof_begin(e, 2);
     if (e->d_log || e->mlp || e->dither > 0.0f) {
-        // step-start features (and, with a network attached, the proposed trial step)
-        ens_feat_reset_kernel<<<nb, 128, 0, e->st>>>(e->sys(), e->d_amax, e->d_hill3);
-        ens_feat_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active_f0, e->d_y, e->d_k[0], e->d_mass, e->d_id,
-                                              e->d_base_of, e->d_nsi_of, e->cap, e->d_amax, e->d_hill3);
+        // step-start features (and, with a network attached, the proposed trial step): one
+        // kernel, a CTA per disk
         PropArgs pa{};
         pa.s = e->sys();
-        pa.amax = e->d_amax;
-        pa.hill3 = e->d_hill3;
+        pa.y = e->d_y;
+        pa.k0 = e->d_k[0];
+        pa.mass = e->d_mass;
+        pa.id = e->d_id;
+        pa.base = e->d_base;
+        pa.nsi = e->d_nsi;
+        pa.ntot = e->d_ntot;
+        pa.stride = e->cap;
         pa.w = (const __nv_bfloat16*)mlp_device_weights(e->mlp);
         for (int q = 0; q < 8; q++) {
             pa.mean[q] = e->mlp_mean[q];
             pa.inv_std[q] = e->mlp_inv_std[q];
         }
         pa.safety = e->safety;
-        ens_propose_kernel<<<(e->n_sys + 3) / 4, 128, 0, e->st>>>(pa);
+        ens_propose_kernel<<<e->n_sys, 256, 0, e->st>>>(pa);
         RG_CUDA_CHECK(cudaGetLastError());
-        e->n_kernels += 3;
+        e->n_kernels += 1;
     }
+    if (e->hill_factor > 0.0) {  // the pairs that entered their Hill spheres at this step start
+        rc = launch_ens_hill(event_args(e), e->st);
+        if (rc) return rc;
+        e->n_kernels++;
+    }
+    prof_end(e, pr);
     for (int r = 1; r <= 12 && !rc; r++) {
         double a[9];
         for (int q = 0; q < rk8_nterm[r]; q++) a[q] = rk8_a[rk8_aidx[r][q]];
+        pr = prof_begin(e, 1);
         rc = launch_stage(e, FORM_SUM, rk8_nterm[r], rk8_stage[r], a, e->d_P, e->d_k[r]);
+        prof_end(e, pr);
+        pr = prof_begin(e, 0);
         if (!rc) rc = ens_gravity(e, e->d_P, e->d_k[r], e->d_k[r] + 3 * cap, r, e->d_active, false);
+        prof_end(e, pr);
     }
     if (rc) return rc;
     const int snp[7] = {0, 5, 6, 7, 8, 9, 10};
     const double bnp[7] = {rk8_b[0], rk8_b[5], rk8_b[6], rk8_b[8], rk8_b[10], 0.0, 0.0};
+    pr = prof_begin(e, 1);
     rc = launch_stage(e, FORM_RK8_NP1, 7, snp, bnp, e->d_yout, e->d_yout + 3 * cap);
     if (rc) return rc;
     ens_error_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active, e->d_k[0], e->d_k[10], e->d_k[11], e->d_k[12],
                                            e->cap, e->d_maxbits);
+    prof_end(e, pr);
     RG_CUDA_CHECK(cudaGetLastError());
+    pr = prof_begin(e, 2);
     ens_controller_kernel<<<nb, 128, 0, e->st>>>(e->sys());
     RG_CUDA_CHECK(cudaGetLastError());
     ens_copy_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_acc, e->d_yout, 0, e->d_y, 0, 6, e->cap);
@@ -1056,249 +1204,54 @@ int record_attempt(rg_ens* e)
     RG_CUDA_CHECK(cudaGetLastError());
     ens_finalize_kernel<<<nb, 128, 0, e->st>>>(e->sys());
     RG_CUDA_CHECK(cudaGetLastError());
-    e->n_kernels += 5;
+    // merges, ejections and hit-star merges of the held disks, then the loop condition
+    rc = launch_ens_handle(event_args(e), 0, e->st);
+    if (!rc) rc = launch_ens_loop(loop_args(e, in_graph), e->st);
+    prof_end(e, pr);
+    if (rc) return rc;
+    e->n_kernels += 7;
     return RG_OK;
 }
 
 int launch_attempt(rg_ens* e)
 {
-    if (!e->use_graph) {
-        const int64_t k0 = e->n_kernels;
-        int rc = record_attempt(e);
-        e->kernels_per_attempt = e->n_kernels - k0;
-        return rc;
-    }
-    if (!e->graph_valid) {
-        if (e->exec) cudaGraphExecDestroy(e->exec);
-        if (e->graph) cudaGraphDestroy(e->graph);
-        e->exec = nullptr;
-        e->graph = nullptr;
-        RG_CUDA_CHECK(cudaStreamBeginCapture(e->st, cudaStreamCaptureModeThreadLocal));
-        const int64_t k0 = e->n_kernels;
-        int rc = record_attempt(e);
-        e->kernels_per_attempt = e->n_kernels - k0;
-        e->n_kernels = k0;
-        cudaGraph_t g = nullptr;
-        cudaError_t err = cudaStreamEndCapture(e->st, &g);
-        if (rc) {
-            if (g) cudaGraphDestroy(g);
-            return rc;
-        }
-        if (err != cudaSuccess) return cuda_fail(err, "cudaStreamEndCapture", __FILE__, __LINE__);
-        e->graph = g;
-        RG_CUDA_CHECK(cudaGraphInstantiate(&e->exec, e->graph, 0));
-        e->graph_valid = true;
-    }
-    RG_CUDA_CHECK(cudaGraphLaunch(e->exec, e->st));
-    e->n_graph_launches++;
-    e->n_kernels += e->kernels_per_attempt;
+    const int64_t k0 = e->n_kernels;
+    int rc = record_attempt(e, false);
+    e->kernels_per_attempt = e->n_kernels - k0;
+    return rc;
+}
+
+// the graph: one conditional while-node whose body, captured from record_attempt, ends with
+// the kernel that sets the condition; rebuilt when a launch parameter it freezes changes
+int build_loop_graph(rg_ens* e)
+{
+    if (e->exec) cudaGraphExecDestroy(e->exec);
+    if (e->graph) cudaGraphDestroy(e->graph);
+    e->exec = nullptr;
+    e->graph = nullptr;
+    e->graph_valid = false;
+    RG_CUDA_CHECK(cudaGraphCreate(&e->graph, 0));
+    RG_CUDA_CHECK(cudaGraphConditionalHandleCreate(&e->cond, e->graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = e->cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    RG_CUDA_CHECK(cudaGraphAddNode(&node, e->graph, nullptr, nullptr, 0, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    RG_CUDA_CHECK(cudaStreamBeginCaptureToGraph(e->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const int64_t k0 = e->n_kernels;
+    int rc = record_attempt(e, true);
+    e->kernels_per_attempt = e->n_kernels - k0;
+    e->n_kernels = k0;
+    cudaGraph_t captured = nullptr;
+    const cudaError_t err = cudaStreamEndCapture(e->st, &captured);
+    if (rc) return rc;
+    if (err != cudaSuccess) return cuda_fail(err, "cudaStreamEndCapture", __FILE__, __LINE__);
+    RG_CUDA_CHECK(cudaGraphInstantiate(&e->exec, e->graph, 0));
+    e->graph_valid = true;
     return RG_OK;
-}
-
-// ------------------------------------------------------------------- host event handling
-rg_event_t zero_event()
-{
-    rg_event_t v;
-    std::memset(&v, 0, sizeof(v));
-    return v;
-}
-
-// one disk's state on the host while its events are applied
-struct HostDisk {
-    rg_ens* e;
-    int s, b, n;
-    std::vector<double> rows;  // 6 rows of n
-    double t;
-    double& at(int row, int i) { return rows[(size_t)row * n + (i - b)]; }
-    rg_vec_t r(int i) { return rg_vec_t{at(0, i), at(1, i), at(2, i), 0.0}; }
-    rg_vec_t v(int i) { return rg_vec_t{at(3, i), at(4, i), at(5, i), 0.0}; }
-    void set(int i, const rg_vec_t& rr, const rg_vec_t& vv)
-    {
-        at(0, i) = rr.x; at(1, i) = rr.y; at(2, i) = rr.z;
-        at(3, i) = vv.x; at(4, i) = vv.y; at(5, i) = vv.z;
-    }
-};
-
-// pp_disk::handle_collision_pair (pp_disk.cu:1151-1202) on a host disk (indices global)
-int merge_pair(HostDisk& h, rg_event_t* c)
-{
-    rg_ens* e = h.e;
-    const int surv = c->idx1 + h.b, merg = c->idx2 + h.b;
-    if (RG_BODY_SUPERPLANETESIMAL == e->md[merg].body_type)
-        return set_error(RG_ERR_NOT_IMPLEMENTED, "collision with a super-planetesimal is not implemented");
-    c->p1 = e->p[surv];
-    c->p2 = e->p[merg];
-    host::calc_position_after_collision(c->p1.mass, c->p2.mass, &c->r1, &c->r2, &c->rs);
-    host::calc_velocity_after_collision(c->p1.mass, c->p2.mass, &c->v1, &c->v2, &c->vs);
-    h.set(surv, c->rs, c->vs);
-    host::calc_physical_properties(c->p1, c->p2, &c->ps);
-    e->p[surv] = c->ps;
-    e->md[merg].id *= -1;
-    e->p[merg].mass = 0.0;
-    e->p[merg].density = 0.0;
-    e->p[merg].radius = 0.0;
-    h.set(merg, rg_vec_t{1.0e20, 0.0, 0.0, 0.0}, rg_vec_t{0.0, 0.0, 0.0, 0.0});
-    return RG_OK;
-}
-
-// applies the accepted step's collision records and the ejection / hit-star check
-int handle_disk(rg_ens* e, int s, const std::vector<DevEvent>& recs, double t_prev, double dt_did)
-{
-    HostDisk h{e, s, e->base[s], e->ntot[s], {}, 0.0};
-    h.rows.resize((size_t)6 * h.n);
-    RG_CUDA_CHECK(cudaMemcpy2DAsync(h.rows.data(), h.n * sizeof(double), e->d_y + h.b, e->cap * sizeof(double),
-                                    h.n * sizeof(double), 6, cudaMemcpyDeviceToHost, e->st));
-    RG_CUDA_CHECK(cudaMemcpyAsync(&h.t, e->d_t + s, sizeof(double), cudaMemcpyDeviceToHost, e->st));
-    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
-    const int nsi = e->n_si(s);
-    // raw records in the reference's order, then create_sp_events + handle_collision_pair
-    std::vector<rg_event_t> ev;
-    for (const DevEvent& d : recs) {
-        rg_event_t x = zero_event();
-        const int stage = (int)(d.seq & 0xff);
-        const double curr_t = t_prev + rk8_c[stage] * dt_did;
-        x.t = (d.i - h.b >= nsi) ? t_prev : curr_t;  // pp_disk.cu:576,581
-        x.d = d.d;
-        int surv = d.i, merg = d.j;
-        const double *rs = d.ri, *vs = d.vi, *rm = d.rj, *vm = d.vj;
-        if (e->p[merg].mass > e->p[surv].mass) {
-            std::swap(surv, merg);
-            std::swap(rs, rm);
-            std::swap(vs, vm);
-        }
-        x.event_name = RG_EVENT_COLLISION;
-        x.id1 = e->md[surv].id;
-        x.id2 = e->md[merg].id;
-        x.idx1 = surv - h.b;
-        x.idx2 = merg - h.b;
-        x.r1 = rg_vec_t{rs[0], rs[1], rs[2], 0.0};
-        x.v1 = rg_vec_t{vs[0], vs[1], vs[2], 0.0};
-        x.r2 = rg_vec_t{rm[0], rm[1], rm[2], 0.0};
-        x.v2 = rg_vec_t{vm[0], vm[1], vm[2], 0.0};
-        ev.push_back(x);
-    }
-    std::vector<char> done(ev.size(), 0);
-    for (size_t k = 0; k < ev.size(); k++) {
-        if (done[k]) continue;
-        done[k] = 1;
-        rg_event_t cur = ev[k];
-        for (size_t i = k + 1; i < ev.size(); i++)
-            if (cur.id1 == ev[i].id1 && cur.id2 == ev[i].id2) {
-                done[i] = 1;
-                if (cur.t > ev[i].t) cur = ev[i];
-            }
-        int rc = merge_pair(h, &cur);
-        if (rc) return rc;
-        e->log.emplace_back(s, cur);
-    }
-    // ejection / hit-star check of the new state (pp_disk.cu:934-976,1091-1109)
-    const double* th = &e->thr[5 * (size_t)s];
-    std::vector<rg_event_t> ej;
-    for (int i = h.b; i < h.b + h.n; i++) {
-        if (!(0 < e->md[i].id && RG_BODY_STAR != e->md[i].body_type)) continue;
-        const rg_vec_t ri = h.r(i);
-        const double r2 = ri.x * ri.x + ri.y * ri.y + ri.z * ri.z;
-        int name = 0;
-        if (0.0 < th[1] && th[4] < r2)
-            name = RG_EVENT_EJECTION;
-        else if (0.0 < th[0] && th[3] > r2)
-            name = RG_EVENT_HIT_CENTRUM;
-        if (!name) continue;
-        rg_event_t x = zero_event();
-        x.event_name = name;
-        x.d = std::sqrt(r2);
-        x.t = h.t;
-        x.id1 = e->md[h.b].id;
-        x.id2 = e->md[i].id;
-        x.idx1 = 0;
-        x.idx2 = i - h.b;
-        x.r1 = h.r(h.b);
-        x.v1 = h.v(h.b);
-        x.r2 = ri;
-        x.v2 = h.v(i);
-        if (name == RG_EVENT_EJECTION) {
-            x.p1 = e->p[h.b];
-            x.p2 = e->p[i];
-            x.rs = x.r1;
-            x.vs = x.v1;
-            x.ps = x.p1;
-        }
-        e->md[i].id *= -1;
-        ej.push_back(x);
-    }
-    for (auto& x : ej) {
-        if (x.event_name == RG_EVENT_HIT_CENTRUM) {
-            int rc = merge_pair(h, &x);
-            if (rc) return rc;
-        }
-        e->log.emplace_back(s, x);
-    }
-    // upload the disk
-    std::vector<double> m(h.n), R(h.n);
-    std::vector<int> id(h.n);
-    for (int i = 0; i < h.n; i++) {
-        m[i] = e->p[h.b + i].mass;
-        R[i] = e->p[h.b + i].radius;
-        id[i] = e->md[h.b + i].id;
-    }
-    RG_CUDA_CHECK(cudaMemcpy2DAsync(e->d_y + h.b, e->cap * sizeof(double), h.rows.data(), h.n * sizeof(double),
-                                    h.n * sizeof(double), 6, cudaMemcpyHostToDevice, e->st));
-    RG_CUDA_CHECK(cudaMemcpyAsync(e->d_mass + h.b, m.data(), h.n * sizeof(double), cudaMemcpyHostToDevice, e->st));
-    RG_CUDA_CHECK(cudaMemcpyAsync(e->d_radius + h.b, R.data(), h.n * sizeof(double), cudaMemcpyHostToDevice, e->st));
-    RG_CUDA_CHECK(cudaMemcpyAsync(e->d_id + h.b, id.data(), h.n * sizeof(int), cudaMemcpyHostToDevice, e->st));
-    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
-    return RG_OK;
-}
-
-// Hill-sphere records -> log entries (a pair is logged when it enters the sphere)
-void handle_hill(rg_ens* e, std::vector<DevEvent>& recs, const std::vector<unsigned int>& nf0)
-{
-    std::sort(recs.begin(), recs.end(), [](const DevEvent& a, const DevEvent& b) {
-        if (a.sys != b.sys) return a.sys < b.sys;
-        if (a.seq != b.seq) return a.seq < b.seq;
-        if (a.i != b.i) return a.i < b.i;
-        return a.j < b.j;
-    });
-    size_t k = 0;
-    while (k < recs.size()) {
-        const int s = recs[k].sys;
-        const int64_t f0 = recs[k].seq;
-        std::vector<int64_t> cur;
-        size_t q = k;
-        for (; q < recs.size() && recs[q].sys == s && (int64_t)recs[q].seq == f0; q++) {
-            const DevEvent& d = recs[q];
-            const int64_t key = ((int64_t)(uint32_t)e->md[d.i].id << 32) | (int64_t)(uint32_t)e->md[d.j].id;
-            const bool seen = (e->hill_last[s] == f0 - 1) &&
-                              std::find(e->hill_prev[s].begin(), e->hill_prev[s].end(), key) != e->hill_prev[s].end();
-            if (!seen) {
-                rg_event_t x = zero_event();
-                x.event_name = RG_EVENT_CLOSE_ENCOUNTER;
-                x.t = d.t;  // the step start, where the pair was found inside the sphere
-                x.d = d.d;
-                x.id1 = e->md[d.i].id;
-                x.id2 = e->md[d.j].id;
-                x.idx1 = d.i - e->base[s];
-                x.idx2 = d.j - e->base[s];
-                x.p1 = e->p[d.i];
-                x.p2 = e->p[d.j];
-                x.r1 = rg_vec_t{d.ri[0], d.ri[1], d.ri[2], 0.0};
-                x.v1 = rg_vec_t{d.vi[0], d.vi[1], d.vi[2], 0.0};
-                x.r2 = rg_vec_t{d.rj[0], d.rj[1], d.rj[2], 0.0};
-                x.v2 = rg_vec_t{d.vj[0], d.vj[1], d.vj[2], 0.0};
-                e->log.emplace_back(s, x);
-            }
-            cur.push_back(key);
-        }
-        e->hill_prev[s].swap(cur);
-        e->hill_last[s] = f0;
-        k = q;
-    }
-    // disks whose later step-start evaluations found no pair have left every sphere
-    for (int s = 0; s < e->n_sys; s++)
-        if ((int64_t)nf0[s] > e->hill_last[s] + 1) {
-            e->hill_prev[s].clear();
-            e->hill_last[s] = (int64_t)nf0[s] - 1;
-        }
 }
 
 }  // namespace
@@ -1420,14 +1373,29 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     chk(dalloc(&e->d_nprop, ns));
     chk(dalloc(&e->d_nprop_acc, ns));
     chk(dalloc(&e->d_nfallback, ns));
-    chk(dalloc(&e->d_amax, ns));
-    chk(dalloc(&e->d_hill3, ns));
-    chk(dalloc(&e->d_nsi_of, nt));
     chk(dalloc(&e->d_ev, e->ev_cap));
     chk(dalloc(&e->d_ev_count, 1));
     chk(dalloc(&e->d_hill, e->ev_cap));
     chk(dalloc(&e->d_hill_count, 1));
     chk(dalloc(&e->d_kerr, 1));
+    chk(dalloc(&e->d_prm, nt));
+    chk(dalloc(&e->d_f_rad, ns));
+    chk(dalloc(&e->d_base, ns));
+    chk(dalloc(&e->d_ntot, ns));
+    chk(dalloc(&e->d_nsi, ns));
+    chk(dalloc(&e->d_hill_set, 2 * (size_t)HILL_SET_CAP * ns));
+    chk(dalloc(&e->d_hill_n, ns));
+    chk(dalloc(&e->d_hill_which, ns));
+    // the event log holds every record of one advance: 16 per body, at least 4096, at most
+    // 2^18 (128 MiB); more records end the advance with RG_ERR_EVENT_OVERFLOW
+    e->elog_cap = (unsigned int)std::min<int64_t>(1 << 18, std::max<int64_t>(4096, 16 * tot));
+    chk(dalloc(&e->d_elog, e->elog_cap));
+    chk(dalloc(&e->d_elog_count, 1));
+    chk(dalloc(&e->d_elog_seq, ns));
+    chk(dalloc(&e->d_flags, 1));
+    chk(dalloc(&e->d_hit_slots, (size_t)HIT_CAP * ns));
+    chk(dalloc(&e->d_keep, 1));
+    chk(dalloc(&e->d_attempts, 3));
     if (rc) {
         free_all(e);
         delete e;
@@ -1436,8 +1404,6 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     e->p.assign(p, p + nt);
     e->md.assign(md, md + nt);
     e->thr.assign(thr, thr + 5 * ns);
-    e->hill_prev.assign(ns, {});
-    e->hill_last.assign(ns, -2);
     // per disk: barycentric transform and time rescale as rg_create does
     std::vector<double> h(6 * nt);
     std::vector<int> base_of(nt);
@@ -1487,15 +1453,24 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     chk(upload(e, e->d_type, ty));
     chk(upload(e, e->d_base_of, base_of));
     {
-        std::vector<int> nsi_of(nt);
-        for (int s2 = 0; s2 < n_sys; s2++)
-            for (int j = 0; j < e->ntot[s2]; j++) nsi_of[(size_t)e->base[s2] + j] = e->n_si(s2);
-        chk(upload(e, e->d_nsi_of, nsi_of));
         std::vector<float> zf(8 * ns, 0.0f), zh(5 * ns, 0.0f);
         chk(upload(e, e->d_feat, zf));
         chk(upload(e, e->d_hist, zh));
     }
     chk(upload(e, e->d_thr, e->thr));
+    chk(upload(e, e->d_prm, e->p));
+    {
+        std::vector<double> fr(ns);
+        std::vector<int> nsi(ns);
+        for (int s2 = 0; s2 < n_sys; s2++) {
+            fr[s2] = e->thr[5 * (size_t)s2 + RG_THRESHOLD_RADII_ENHANCE_FACTOR];
+            nsi[s2] = e->n_si(s2);
+        }
+        chk(upload(e, e->d_f_rad, fr));
+        chk(upload(e, e->d_base, e->base));
+        chk(upload(e, e->d_ntot, e->ntot));
+        chk(upload(e, e->d_nsi, nsi));
+    }
     std::vector<int> zi(ns, 0);
     std::vector<double> zd(ns, 0.0);
     std::vector<long long> zl(ns, 0);
@@ -1527,6 +1502,13 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     if (!rc && cudaMemsetAsync(e->d_ev_count, 0, sizeof(unsigned int), e->st) != cudaSuccess) chk(RG_ERR_CUDA);
     if (!rc && cudaMemsetAsync(e->d_hill_count, 0, sizeof(unsigned int), e->st) != cudaSuccess) chk(RG_ERR_CUDA);
     if (!rc && cudaMemsetAsync(e->d_kerr, 0, sizeof(unsigned int), e->st) != cudaSuccess) chk(RG_ERR_CUDA);
+    for (auto z : {std::make_pair((void*)e->d_hill_n, ns * sizeof(int)),
+                   std::make_pair((void*)e->d_hill_which, ns * sizeof(int)),
+                   std::make_pair((void*)e->d_elog_count, sizeof(unsigned int)),
+                   std::make_pair((void*)e->d_elog_seq, ns * sizeof(unsigned int)),
+                   std::make_pair((void*)e->d_flags, sizeof(unsigned int)),
+                   std::make_pair((void*)e->d_attempts, 3 * sizeof(long long))})
+        if (!rc && cudaMemsetAsync(z.first, 0, z.second, e->st) != cudaSuccess) chk(RG_ERR_CUDA);
     if (!rc && cudaStreamSynchronize(e->st) != cudaSuccess) chk(set_error(RG_ERR_CUDA, "upload"));
     if (rc) {
         free_all(e);
@@ -1584,88 +1566,68 @@ int drain_log(rg_ens* e)
     return RG_OK;
 }
 
-int drain(rg_ens* e, double stop)
+// After an advance: the device's event log (ordered per disk by record number), the body
+// parameters and ids the merges changed (host mirrors), and the error bits.
+int collect(rg_ens* e)
 {
-    int lrc = drain_log(e);
-    if (lrc) return lrc;
-    unsigned int counts[3];
-    RG_CUDA_CHECK(cudaMemcpyAsync(&counts[0], e->d_ev_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
-    RG_CUDA_CHECK(cudaMemcpyAsync(&counts[1], e->d_hill_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
-    RG_CUDA_CHECK(cudaMemcpyAsync(&counts[2], e->d_kerr, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
-    std::vector<int> status;
-    std::vector<unsigned int> nf0;
-    int rc = download(e, status, e->d_status, e->n_sys);
-    if (!rc) rc = download(e, nf0, e->d_nf0, e->n_sys);
+    int rc = drain_log(e);
+    if (rc) return rc;
+    unsigned int flags = 0, kerr = 0, n_log = 0;
+    RG_CUDA_CHECK(cudaMemcpyAsync(&flags, e->d_flags, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&kerr, e->d_kerr, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
+    RG_CUDA_CHECK(cudaMemcpyAsync(&n_log, e->d_elog_count, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
+    std::vector<rg_param_t> prm;
+    std::vector<int> id;
+    rc = download(e, prm, e->d_prm, (size_t)e->cap);
+    if (!rc) rc = download(e, id, e->d_id, (size_t)e->cap);
     if (rc) return rc;
     RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
-    if (counts[2]) {
+    for (int i = 0; i < e->cap; i++) {
+        e->p[i] = prm[i];
+        e->md[i].id = id[i];
+    }
+    const unsigned int m = std::min(n_log, e->elog_cap);
+    if (m > 0) {
+        std::vector<EnsLogRec> recs;
+        rc = download(e, recs, e->d_elog, m);
+        if (rc) return rc;
+        RG_CUDA_CHECK(cudaMemsetAsync(e->d_elog_count, 0, sizeof(unsigned int), e->st));
+        RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+        std::stable_sort(recs.begin(), recs.end(), [](const EnsLogRec& a, const EnsLogRec& b) {
+            return a.sys != b.sys ? a.sys < b.sys : a.seqno < b.seqno;
+        });
+        for (const EnsLogRec& r : recs) e->log.emplace_back(r.sys, r.ev);
+    }
+    if (kerr) {
         RG_CUDA_CHECK(cudaMemsetAsync(e->d_kerr, 0, sizeof(unsigned int), e->st));
         return set_error(RG_ERR_CUDA, "a gravity tile copy did not arrive within the wait limit");
     }
-    if (counts[0] > e->ev_cap || counts[1] > e->ev_cap)
-        return set_error(RG_ERR_EVENT_OVERFLOW, "ensemble event buffer full between two host synchronisations");
-    if (counts[1] > 0) {
-        std::vector<DevEvent> hill;
-        rc = download(e, hill, e->d_hill, counts[1]);
+    if (flags) {
+        RG_CUDA_CHECK(cudaMemsetAsync(e->d_flags, 0, sizeof(unsigned int), e->st));
         RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
-        handle_hill(e, hill, nf0);
-        RG_CUDA_CHECK(cudaMemsetAsync(e->d_hill_count, 0, sizeof(unsigned int), e->st));
-    } else if (e->hill_factor > 0.0) {
-        std::vector<DevEvent> none;
-        handle_hill(e, none, nf0);
+        if (flags & ENS_FLAG_SUPERPLANETESIMAL)
+            return set_error(RG_ERR_NOT_IMPLEMENTED, "collision with a super-planetesimal is not implemented");
+        if (flags & ENS_FLAG_EVENT_OVERFLOW)
+            return set_error(RG_ERR_EVENT_OVERFLOW, "more collision records in one attempt than the event buffer holds");
+        if (flags & ENS_FLAG_HILL_OVERFLOW)
+            return set_error(RG_ERR_EVENT_OVERFLOW, "more Hill records in one step start than the event buffer holds");
+        if (flags & ENS_FLAG_LOG_OVERFLOW)
+            return set_error(RG_ERR_EVENT_OVERFLOW, "the ensemble's event log is full (drain it with rg_ens_events)");
+        if (flags & ENS_FLAG_HILL_SET)
+            return set_error(RG_ERR_EVENT_OVERFLOW, "more pairs inside their Hill spheres than a disk's set holds");
+        if (flags & ENS_FLAG_HIT_OVERFLOW)
+            return set_error(RG_ERR_EVENT_OVERFLOW, "more hit-star records in one check than a disk's list holds");
+        if (flags & ENS_FLAG_STEP_LOG_OVERFLOW)
+            return set_error(RG_ERR_EVENT_OVERFLOW, "the attempt log is full (drain it with rg_ens_step_log)");
+        return set_error(RG_ERR_STATE, "ensemble error flag");
     }
-    std::vector<int> held;
-    for (int s = 0; s < e->n_sys; s++)
-        if (status[s] == RG_SYS_HELD) held.push_back(s);
-    if (!held.empty()) {
-        std::vector<DevEvent> recs;
-        std::vector<double> tprev, dtdid, t;
-        std::vector<unsigned int> acc_attempt;
-        rc = download(e, recs, e->d_ev, counts[0]);
-        if (!rc) rc = download(e, tprev, e->d_tprev, e->n_sys);
-        if (!rc) rc = download(e, dtdid, e->d_dt_did, e->n_sys);
-        if (!rc) rc = download(e, t, e->d_t, e->n_sys);
-        if (!rc) rc = download(e, acc_attempt, e->d_acc_attempt, e->n_sys);
-        if (rc) return rc;
-        RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
-        std::sort(recs.begin(), recs.end(), [](const DevEvent& a, const DevEvent& b) {
-            if (a.sys != b.sys) return a.sys < b.sys;
-            if (a.seq != b.seq) return a.seq < b.seq;
-            if (a.i != b.i) return a.i < b.i;
-            return a.j < b.j;
-        });
-        for (int s : held) {
-            std::vector<DevEvent> mine;
-            for (const DevEvent& d : recs)
-                if (d.sys == s && (d.seq >> 8) == acc_attempt[s]) mine.push_back(d);
-            rc = handle_disk(e, s, mine, tprev[s], dtdid[s]);
-            if (rc) return rc;
-            status[s] = (t[s] <= stop) ? RG_SYS_RUNNING : RG_SYS_DONE;
-        }
-        // every record was of a rejected attempt or of a disk handled now
-        RG_CUDA_CHECK(cudaMemsetAsync(e->d_ev_count, 0, sizeof(unsigned int), e->st));
-        rc = upload(e, e->d_status, status);
-        std::vector<int> active(e->n_sys), f0(e->n_sys);
-        std::vector<int> cur_f0;
-        if (!rc) rc = download(e, cur_f0, e->d_active_f0, e->n_sys);
-        RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
-        for (int s = 0; s < e->n_sys; s++) {
-            active[s] = status[s] == RG_SYS_RUNNING;
-            const bool was_held = std::find(held.begin(), held.end(), s) != held.end();
-            f0[s] = active[s] && (was_held || cur_f0[s]);
-        }
-        if (!rc) rc = upload(e, e->d_active, active);
-        if (!rc) rc = upload(e, e->d_active_f0, f0);
-        if (!rc) RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
-    } else if (counts[0] > 0) {
-        RG_CUDA_CHECK(cudaMemsetAsync(e->d_ev_count, 0, sizeof(unsigned int), e->st));
-    }
-    return rc;
+    return RG_OK;
 }
 
 int advance_impl(rg_ens* e, double t_stop_day, int64_t max_attempts, int64_t* n_attempts)
 {
     if (!e->has_int) return set_error(RG_ERR_STATE, "no integrator set (rg_ens_set_integrator)");
+    if (n_attempts) *n_attempts = 0;
     const double stop = t_stop_day * GAUSS;
     std::vector<int> status;
     std::vector<double> t;
@@ -1684,44 +1646,66 @@ int advance_impl(rg_ens* e, double t_stop_day, int64_t max_attempts, int64_t* n_
         ens_eject_screen_kernel<<<(int)e->stiles.size(), 256, 0, e->st>>>(e->d_stiles, e->d_active, e->d_y, e->cap,
                                                                           e->d_id, e->d_type, e->d_thr, e->d_ej);
         RG_CUDA_CHECK(cudaGetLastError());
-        e->n_kernels++;
-        std::vector<int> ej;
-        rc = download(e, ej, e->d_ej, e->n_sys);
-        RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
-        for (int s = 0; s < e->n_sys && !rc; s++)
-            if (ej[s]) rc = handle_disk(e, s, {}, 0.0, 0.0);
-        std::vector<int> zero(e->n_sys, 0);
-        if (!rc) rc = upload(e, e->d_ej, zero);
+        rc = launch_ens_handle(event_args(e), 1, e->st);
         if (rc) return rc;
+        e->n_kernels += 2;
         e->started = 1;
     }
-    int64_t k = 0;
-    const int per_sync = 8;
-    while (max_attempts <= 0 || k < max_attempts) {
-        const int batch = max_attempts > 0 ? (int)std::min<int64_t>(per_sync, max_attempts - k) : per_sync;
-        for (int b = 0; b < batch; b++) {
-            rc = launch_attempt(e);
+    // attempts in bounded chunks: a graph launch (or, with graphs off, a run of direct
+    // launches) ends after ATTEMPT_CHUNK attempts at most, and the host starts the next chunk
+    // while disks are running -- reading three words, handling nothing
+    const long long limit = max_attempts > 0 ? (long long)max_attempts : 0;
+    long long att = 0;
+    for (;;) {
+        const long long ctl[3] = {att, limit, att + ATTEMPT_CHUNK};
+        const int one = 1;
+        RG_CUDA_CHECK(cudaMemcpyAsync(e->d_attempts, ctl, sizeof(ctl), cudaMemcpyHostToDevice, e->st));
+        RG_CUDA_CHECK(cudaMemcpyAsync(e->d_keep, &one, sizeof(int), cudaMemcpyHostToDevice, e->st));
+        if (e->use_graph && !e->profiling) {
+            // one launch: the while-node repeats the attempt until its last kernel clears the
+            // condition (every disk done, an error bit, a limit)
+            if (!e->graph_valid) rc = build_loop_graph(e);
             if (rc) return rc;
+            RG_CUDA_CHECK(cudaGraphLaunch(e->exec, e->st));
+            e->n_graph_launches++;
+        } else {
+            int keep = 1;
+            while (keep) {  // direct launches, the condition read after each attempt
+                rc = launch_attempt(e);
+                if (rc) return rc;
+                RG_CUDA_CHECK(cudaMemcpyAsync(&keep, e->d_keep, sizeof(int), cudaMemcpyDeviceToHost, e->st));
+                RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+            }
         }
-        k += batch;
-        e->n_attempts += batch;
-        rc = drain(e, stop);
-        if (rc) return rc;
-        rc = download(e, status, e->d_status, e->n_sys);
+        long long now = 0;
+        int keep = 0;
+        RG_CUDA_CHECK(cudaMemcpyAsync(&now, e->d_attempts, sizeof(long long), cudaMemcpyDeviceToHost, e->st));
+        RG_CUDA_CHECK(cudaMemcpyAsync(&keep, e->d_keep, sizeof(int), cudaMemcpyDeviceToHost, e->st));
+        RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+        if (e->use_graph && !e->profiling) e->n_kernels += e->kernels_per_attempt * (now - att);
+        att = now;
+        // the loop stopped at the chunk's end only when nothing else stopped it
+        if (keep || att < ctl[2] || (limit > 0 && att >= limit)) break;
+        unsigned int flags = 0;
+        std::vector<int> st;
+        RG_CUDA_CHECK(cudaMemcpyAsync(&flags, e->d_flags, sizeof(unsigned int), cudaMemcpyDeviceToHost, e->st));
+        rc = download(e, st, e->d_status, e->n_sys);
         if (rc) return rc;
         RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
-        bool running = false, error = false;
-        for (int s = 0; s < e->n_sys; s++) {
-            running = running || status[s] == RG_SYS_RUNNING;
-            error = error || status[s] == RG_SYS_ERROR;
-        }
-        if (error) {
-            if (n_attempts) *n_attempts = k;
-            return set_error(RG_ERR_DT_NONFINITE, "a disk's step-size controller produced a non-finite or zero step");
-        }
-        if (!running) break;
+        bool running = false;
+        for (int s = 0; s < e->n_sys; s++) running = running || st[s] == RG_SYS_RUNNING;
+        if (!running || flags) break;
     }
-    if (n_attempts) *n_attempts = k;
+    e->n_attempts += att;
+    if (n_attempts) *n_attempts = att;
+    rc = collect(e);
+    if (rc) return rc;
+    rc = download(e, status, e->d_status, e->n_sys);
+    if (rc) return rc;
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    for (int s = 0; s < e->n_sys; s++)
+        if (status[s] == RG_SYS_ERROR)
+            return set_error(RG_ERR_DT_NONFINITE, "a disk's step-size controller produced a non-finite or zero step");
     return RG_OK;
 }
 
@@ -2059,6 +2043,37 @@ int rg_ens_autotune(rg_ens* e, int reps, rg_tune_t* out)
 {
     if (!e || reps < 1) return set_error(RG_ERR_ARG, "bad argument");
     RG_GUARD(ens_autotune_impl(e, reps, out));
+}
+
+int rg_ens_set_profiling(rg_ens* e, int on)
+{
+    if (!e) return set_error(RG_ERR_ARG, "null ensemble");
+    e->profiling = on ? 1 : 0;
+    return RG_OK;
+}
+
+int rg_ens_get_profile(rg_ens* e, rg_profile_t* prof)
+{
+    if (!e || !prof) return set_error(RG_ERR_ARG, "bad argument");
+    std::memset(prof, 0, sizeof(*prof));
+    RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
+    for (size_t k = 0; k < e->ev_kind.size(); k++) {
+        float ms = 0.0f;
+        RG_CUDA_CHECK(cudaEventElapsedTime(&ms, e->ev_pool[2 * k], e->ev_pool[2 * k + 1]));
+        if (e->ev_kind[k] == 0) {
+            prof->gravity_launches++;
+            prof->gravity_ms += ms;
+        } else if (e->ev_kind[k] == 1) {
+            prof->stage_launches++;
+            prof->stage_ms += ms;
+        } else {
+            prof->other_launches++;
+            prof->other_ms += ms;
+        }
+    }
+    e->ev_kind.clear();
+    e->ev_used = 0;
+    return RG_OK;
 }
 
 int rg_ens_kernel_count(rg_ens* e, int64_t* n_kernels, int64_t* n_graph_launches)

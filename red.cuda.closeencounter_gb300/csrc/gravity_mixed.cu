@@ -231,7 +231,7 @@ __device__ __forceinline__ void exact_event_tests(const GravArgs& g, const Tile&
     const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
     const double d = sqrt(r2);
     const int li = i - tile.base, lj = j - tile.base;
-    const bool rad = g.record && li > 0 && li > lj && d < __dmul_rn(g.f_rad, __dadd_rn(Ri, g.radius[j]));
+    const bool rad = g.record && li > 0 && li > lj && d < __dmul_rn(tile_f_rad(g, tile), __dadd_rn(Ri, g.radius[j]));
     bool hill = false;
     if (g.hill && tile.block != 2 && li > 0 && li > lj && lj > 0) {
         const double h = __dmul_rn(0.5, __dadd_rn(rhoi, g.rho[j]));
@@ -413,7 +413,7 @@ __device__ __forceinline__ void df_screen(const GravArgs& g, const Tile& tile, i
     const float margin = 1.001f;
     bool cand = false;
     if (g.record) {
-        const float lim = g.f_rad_f * (Ri + Rj) * margin;
+        const float lim = (g.sys_f_rad ? (float)g.sys_f_rad[tile.sys] : g.f_rad_f) * (Ri + Rj) * margin;
         cand = r2f < lim * lim;
     }
     if (g.hill && tile.block != 2 && lj > 0) {
@@ -442,7 +442,7 @@ __device__ __forceinline__ float screen_cut2(const GravArgs& g, const Tile& tile
     const float margin = 1.001f;
     float c = 0.0f;
     if (g.record) {
-        const float lim = g.f_rad_f * (Ri + __uint_as_float(sm[0])) * margin;
+        const float lim = (g.sys_f_rad ? (float)g.sys_f_rad[tile.sys] : g.f_rad_f) * (Ri + __uint_as_float(sm[0])) * margin;
         c = lim * lim;
     }
     if (g.hill) {
@@ -471,7 +471,7 @@ __device__ __noinline__ void mixed_screen_pair(const GravArgs& g, const Tile& ti
     const float margin = 1.001f;
     bool cand = false;
     if (g.record) {
-        const float lim = g.f_rad_f * (sf.x + Rj) * margin;
+        const float lim = (g.sys_f_rad ? (float)g.sys_f_rad[tile.sys] : g.f_rad_f) * (sf.x + Rj) * margin;
         cand = r2 < lim * lim;
     }
     if (g.hill && tile.block != 2 && lj > 0) {

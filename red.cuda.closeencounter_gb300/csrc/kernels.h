@@ -74,6 +74,8 @@ struct EnergyArgs {
 int launch_energy(const EnergyArgs& a, cudaStream_t st);
 
 int launch_grav_fp64_pairpar(const GravArgs& g, int S, cudaStream_t st);
+int launch_astro_terms(const double* x, const double* y, const double* z, const double* mass, int n, double m_star,
+                       double* out, long long stride, cudaStream_t st);
 int launch_grav_fp64_rowseq(const GravArgs& g, cudaStream_t st);
 constexpr int FEW_SINKS_MAX = 8;  // sinks per few-sink tile
 int launch_grav_fp64_few(const GravArgs& g, const int* tile_row0, int max_src, double* terms, int rows,

@@ -33,6 +33,7 @@ UNITS = {
     "ensemble.cu": ["-fmad=false"],
     "mlp.cu": [],
     "noalloc.cu": ["-fmad=false"],
+    "ens_events.cu": ["-fmad=false"],
     "icgen.cu": ["-fmad=false"],
 }
 

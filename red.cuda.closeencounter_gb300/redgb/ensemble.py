@@ -29,6 +29,8 @@ def _bind(L):
         "rg_ens_get_stream": [vp, ctypes.POINTER(vp)],
         "rg_ens_kernel_count": [vp, ctypes.POINTER(i64), ctypes.POINTER(i64)],
         "rg_ens_autotune": [vp, ci, ctypes.POINTER(T.Tune)],
+        "rg_ens_set_profiling": [vp, ci],
+        "rg_ens_get_profile": [vp, ctypes.POINTER(T.Profile)],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -133,6 +135,16 @@ class Ensemble:
         t = T.Tune()
         self._call("rg_ens_autotune", self.handle, int(reps), ctypes.byref(t))
         return {f: getattr(t, f) for f, _ in t._fields_}
+
+    def set_profiling(self, on=True):
+        """Time each launch group of every attempt with CUDA events (direct launches)."""
+        self._call("rg_ens_set_profiling", self.handle, int(bool(on)))
+
+    def profile(self):
+        """Summed device times since the last call: gravity, stage and other kernels."""
+        prof = T.Profile()
+        self._call("rg_ens_get_profile", self.handle, ctypes.byref(prof))
+        return {f: getattr(prof, f) for f, _ in prof._fields_}
 
     def kernel_count(self):
         a, b = ctypes.c_int64(), ctypes.c_int64()

@@ -141,10 +141,11 @@ def set_dither(ensemble, sigma, seed=0):
         raise RedError("rg_ens_set_dither", rc, L.rg_last_error().decode())
 
 
-def dataset_from_log(log, tol, min_step=4):
+def dataset_from_log(log, tol, min_step=4, with_groups=False):
     """(X, Y) training pairs from an attempt log: one sample per accepted step, the target
-    being log(ideal step / the previous accepted step's ideal step)."""
-    X, Y = [], []
+    being log(ideal step / the previous accepted step's ideal step).  with_groups: also the
+    disk of every sample."""
+    X, Y, G = [], [], []
     order = np.argsort(log["sys"], kind="stable")
     log = log[order]
     for s in np.unique(log["sys"]):
@@ -157,33 +158,62 @@ def dataset_from_log(log, tol, min_step=4):
         keep = (acc["step"][1:] >= min_step) & (acc["err"][1:] > 0) & (acc["err"][:-1] > 0)
         X.append(acc["feat"][1:][keep])
         Y.append(y[keep])
+        G.append(np.full(int(keep.sum()), s, np.int32))
     X = np.concatenate(X).astype(np.float32).reshape(-1, N_IN) if X else np.zeros((0, N_IN), np.float32)
     Y = np.concatenate(Y).astype(np.float32) if Y else np.zeros(0, np.float32)
+    G = np.concatenate(G) if G else np.zeros(0, np.int32)
     ok = np.isfinite(Y) & np.all(np.isfinite(X), axis=1)
-    return X[ok], Y[ok]
+    return (X[ok], Y[ok], G[ok]) if with_groups else (X[ok], Y[ok])
 
 
-def fit(x, y, seed=0, epochs=30, batch=512, lr=2e-3, holdout=0.1, quantile=0.02):
+def best_safety(res, retry=0.9, grid=np.linspace(0.90, 1.0, 201)):
+    """The safety factor s that minimises the expected attempts per unit of simulated time
+    on held-out residuals res = y - prediction: a proposal s * ideal_last * exp(prediction)
+    passes the error test when it does not exceed the ideal step, i.e. when log s <= res;
+    a rejected proposal costs one more attempt, retried at about `retry` times the ideal
+    step (the plain controller's rule).  Cost(s) = (1 + P) / (s (1 - P) + retry P),
+    P = P(res < log s)."""
+    res = np.sort(np.asarray(res, np.float64))
+    best, best_cost = float(grid[0]), np.inf
+    for s_ in grid:
+        p = np.searchsorted(res, np.log(s_)) / max(len(res), 1)
+        cost = (1.0 + p) / (s_ * (1.0 - p) + retry * p)
+        if cost < best_cost:
+            best, best_cost = float(s_), cost
+    return best, best_cost
+
+
+def fit(x, y, seed=0, epochs=30, batch=512, lr=2e-3, holdout=0.1, quantile=None, groups=None):
     """A new network standardised on (x, y)'s inputs and trained on the GPU.
 
-    A random `holdout` fraction is kept out of training; the returned network's `safety`
-    is exp(the `quantile` of the held-out residuals y - prediction), so that a proposal
-    overshoots the ideal step on about that fraction of steps, and `residual_std` is their
-    spread."""
+    A `holdout` fraction is kept out of training -- whole disks when `groups` (the disk of
+    each sample) is given, since the samples of one disk are correlated in time.  The
+    returned network's `safety` minimises the expected attempts per unit time on the held-out
+    residuals y - prediction (best_safety), or with `quantile` is exp(that quantile of
+    them); `residual_std` is their spread."""
     rng = np.random.RandomState(seed)
-    perm = rng.permutation(len(x))
-    n_hold = int(len(x) * holdout)
-    hold, train = perm[:n_hold], perm[n_hold:]
+    if groups is not None and len(np.unique(groups)) > 2:
+        disks = np.unique(groups)
+        held = rng.choice(disks, size=max(1, int(round(len(disks) * holdout))), replace=False)
+        is_hold = np.isin(groups, held)
+        hold, train = np.flatnonzero(is_hold), np.flatnonzero(~is_hold)
+    else:
+        perm = rng.permutation(len(x))
+        n_hold = int(len(x) * holdout)
+        hold, train = perm[:n_hold], perm[n_hold:]
     p = Proposer(seed)
     mean = x[train].mean(axis=0)
     std = x[train].std(axis=0)
     std[std < 1e-6] = 1.0
     p.set_normalisation(mean, std)
     loss = p.train(x[train], y[train], epochs=epochs, batch=batch, lr=lr, seed=seed)
-    if n_hold > 0:
+    if len(hold) > 0:
         res = y[hold] - p.forward(x[hold])
         p.residual_std = float(np.std(res))
-        p.safety = float(min(1.0, np.exp(np.quantile(res, quantile))))
+        if quantile is not None:
+            p.safety = float(min(1.0, np.exp(np.quantile(res, quantile))))
+        else:
+            p.safety, p.expected_cost = best_safety(res)
     else:
         p.residual_std = float("nan")
         p.safety = 0.9

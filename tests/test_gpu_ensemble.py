@@ -77,15 +77,21 @@ def test_ensemble_autotune(gpulib):
 
 
 def test_ensemble_collisions_match_oracle(gpulib):
-    """The reference's collision-merge run as a one-disk ensemble next to a second disk:
-    merges, their event records and the resulting states match the oracle."""
+    """The reference's collision-merge run as a one-disk ensemble next to a second disk with
+    its own (smaller) collision factor: merges, their event records and the resulting states
+    match the oracle; the merges are applied on the device inside one graph launch (the host
+    handles nothing until the interval ends).  A merged radius is the device's pow of the
+    merged volume, so radii are compared to 2 ulp; everything else bit for bit."""
     disk, params, _, ref_events = H.load_fixture("disk_si_rkf78_collide")
     other = bodies.make_disk(n_pl=64, seed=9)
-    thr = np.stack([H.thresholds_of(params), H.thresholds_of(params)])
+    thr = np.stack([H.thresholds_of(params), bodies.thresholds(collision_factor=1.0)])
     ens = Ensemble([disk, other], thr)
     ens.set_integrator(0.001, 1e-10)
     ens.set_step_log(1 << 18)
-    ens.advance(0.5 * T.YEAR)
+    _, g0 = ens.kernel_count()
+    n_att = ens.advance(0.5 * T.YEAR)
+    _, g1 = ens.kernel_count()
+    assert g1 - g0 == (n_att + 4095) // 4096
     log = ens.step_log()
     ev, sysv = ens.events()
     mine = ev[sysv == 0]
@@ -109,6 +115,9 @@ def test_ensemble_collisions_match_oracle(gpulib):
     assert np.array_equal(mg["id"][act_g], mo["id"][act_o])
     for f in "xyz":
         assert H.same(rg[f][act_g], ro[f][act_o])
+    assert H.same(pg["mass"][act_g], po["mass"][act_o])
+    assert np.allclose(pg["radius"][act_g], po["radius"][act_o], rtol=4.5e-16, atol=0.0)
+    assert all(int(e["event_name"]) != T.EVENT_COLLISION for e in ev[sysv == 1])  # R1 + R2: none
 
 
 def test_ensemble_mixed_and_energy(gpulib):
@@ -199,3 +208,43 @@ def test_proposer_fallback_keeps_the_run_correct(gpulib):
     assert sum(x["n_proposed"] for x in st) > sum(x["n_proposal_accepted"] for x in st)
     for s in range(len(disks)):
         assert abs((ens.energy(s)[0] - E0[s]) / E0[s]) < 1e-10
+
+
+@pytest.mark.parametrize("mode", [T.GRAVITY_FP64, T.GRAVITY_MIXED])
+def test_graph_replay_equals_direct_launches(gpulib, mode):
+    """One attempt of every running disk is captured once as a CUDA graph and replayed; the
+    graph freezes the kernels' arguments (row stride, tile lists, control-array pointers,
+    thresholds).  The configuration in which an earlier, discarded form of the stage
+    combination faulted only inside the graph -- Hill-sphere detection on, with merges
+    changing masses, radii and ids between replays -- must give bit for bit the same states,
+    event records, step counts and energies as the same attempts launched directly."""
+    coll, params, _, _ = H.load_fixture("disk_si_rkf78_collide")
+    disks = [coll, bodies.config_disk("ensemble_member", seed=11, n=700),
+             bodies.make_disk(n_pl=90, pl_type=T.BODY_PROTOPLANET, seed=12, m_range=(1e-9, 1e-7), giants=())]
+    thr = np.stack([H.thresholds_of(params), bodies.thresholds(collision_factor=1.0),
+                    bodies.thresholds(collision_factor=1.0)])
+    runs = []
+    for use_graph in (True, False):
+        ens = Ensemble(disks, thr)
+        ens.set_integrator(0.001, 1e-10)
+        ens.set_options(gravity_mode=mode, hill_factor=3.0, use_graph=use_graph)
+        ens.advance(0.25 * T.YEAR)
+        ev, sysv = ens.events()
+        states = [ens.state(s) for s in range(len(disks))]
+        stats = [ens.stats(s) for s in range(len(disks))]
+        energy = [ens.energy(s) for s in range(len(disks))]
+        _, n_graph = ens.kernel_count()
+        runs.append((ev, sysv, states, stats, energy, n_graph))
+        ens.close()
+    (ev_g, sys_g, st_g, stat_g, en_g, ng_g), (ev_d, sys_d, st_d, stat_d, en_d, ng_d) = runs
+    assert ng_g > 0 and ng_d == 0
+    assert sum(e["event_name"] == T.EVENT_COLLISION for e in ev_g) >= 5
+    assert np.array_equal(sys_g, sys_d) and ev_g.tobytes() == ev_d.tobytes()
+    for a, b in zip(st_g, st_d):
+        for x, y in zip(a[:4], b[:4]):
+            assert x.tobytes() == y.tobytes()
+        assert a[4] == b[4]
+    for a, b in zip(stat_g, stat_d):
+        assert (a["n_tried_step"], a["n_passed_step"], a["t_day"]) == (b["n_tried_step"], b["n_passed_step"], b["t_day"])
+    for (ea, la), (eb, lb) in zip(en_g, en_d):
+        assert ea == eb and np.array_equal(la, lb)

@@ -24,7 +24,7 @@ def test_reference_runs_bit_exact(gpulib, name):
     """Whole reference runs: RKF7(8) with merges and compactions, close-encounter
     records with orbital elements, ejection / hit-star, RK4 fixed and adaptive."""
     disk, params, result, events = H.load_fixture(name)
-    s = gpu_system(disk, H.thresholds_of(params))
+    s = gpu_system(disk, H.thresholds_of(params), frame=H.frame_of(params))
     snaps, evs, _ = H.run_fixture(s, params)
     assert H.compare_result(H.snapshots_as_result(snaps), result) == []
     assert H.compare_events(evs, events) == []
@@ -99,16 +99,20 @@ def test_acceleration_bit_exact(gpulib, n):
 
 
 def test_acceleration_full_size_sampled(gpulib):
-    """16384 self-gravitating bodies + star: sampled rows against the oracle."""
+    """16384 self-gravitating bodies + star (the gravity-throughput workload): 1 088 rows
+    against the oracle -- the star, every pair-parallel tile boundary region sampled in 17
+    runs of 64 consecutive sinks spread over the whole disk (each row sums all 16 384
+    sources), and the last rows."""
     disk = bodies.config_disk("self_gravitating")
     g = gpu_system(disk, bodies.thresholds())
     ag = g.calc_accel()
     r = g.state(internal=True)[0]
-    rows = np.r_[0:3, 4000:4003, disk.n_total - 3:disk.n_total]
-    for i in rows:
-        ao = pyoracle.grav_accel_rows(disk, r, int(i), int(i) + 1)
+    n = disk.n_total
+    starts = np.linspace(0, n - 64, 17).astype(int)
+    for i0 in starts:
+        ao = pyoracle.grav_accel_rows(disk, r, int(i0), int(i0) + 64)
         for f in "xyz":
-            assert H.same(ag[f][i], ao[f][0]), (i, f)
+            assert H.same(ag[f][i0:i0 + 64], ao[f]), (i0, f)
 
 
 def test_inactive_and_zero_mass_bodies(gpulib):
@@ -156,6 +160,72 @@ def test_hill_close_encounters_match_oracle(gpulib):
     assert [H.event_key(e) for e in eg] == [H.event_key(e) for e in eo]
     assert H.same(eg["d"], eo["d"]) and H.same(eg["t"], eo["t"])
     _assert_same_state(g, o)
+
+
+def test_planetesimal_disk_1000yr_hill_events(gpulib, planetesimal_disk_1000yr_oracle):
+    """The plain FP64 planetesimal-disk workload (star, two giants, 1024 planetesimals, seed
+    0) over its full 1000 years through rg_advance (main.cu:176-263), with close encounters
+    logged at 3 mutual Hill radii as the workload asks: the GPU's event list (every field of
+    every record), step count and final state equal the oracle's bit for bit.  The same
+    disk's snapshots against the reference's own run are test_reference_runs_bit_exact."""
+    disk, thr, params, n_o, eo, o = planetesimal_disk_1000yr_oracle
+    g = gpu_system(disk, thr)
+    g.set_integrator(T.INT_RKF78, 0.001, True, params["tolerance"])
+    g.set_event_options(hill_factor=3.0)
+    assert g.advance(params["length_yr"] * T.YEAR) == n_o
+    eg = g.events()
+    assert len(eo) >= 20
+    assert eg.tobytes() == eo.tobytes()
+    _assert_same_state(g, o)
+    assert g.counters()["n_tried_step"] == o.counters()["n_tried_step"]
+
+
+def test_astrocentric_frame_refusals(gpulib):
+    """The astrocentric frame takes self-interacting systems only: with planetesimals or
+    test particles the reference's own CPU path turns NaN at the first step (their blocks
+    take the star at the origin as a source, pp_disk.cu:447-454), so the context refuses
+    them, as the oracle does; mixed-precision gravity is refused in that frame; the
+    astrocentric transform needs the star as body 0."""
+    thr = bodies.thresholds()
+    for disk in (bodies.make_disk(n_pl=20, seed=6), bodies.make_disk(n_pl=20, pl_type=T.BODY_PROTOPLANET, seed=6,
+                                                                     n_tp=3)):
+        with pytest.raises(RedError) as ei:
+            gpu_system(disk, thr, frame=T.FRAME_ASTRO)
+        assert ei.value.status == -6
+        with pytest.raises(RedError) as ei:
+            pyoracle.OracleSystem(disk, thr, frame=T.FRAME_ASTRO)
+        assert ei.value.status == -6
+    si = bodies.make_disk(n_pl=30, pl_type=T.BODY_PROTOPLANET, seed=6, m_range=(1e-8, 1e-6))
+    s = gpu_system(si, thr, frame=T.FRAME_ASTRO)
+    with pytest.raises(RedError) as ei:
+        s.set_gravity_mode(T.GRAVITY_MIXED)
+    assert ei.value.status == -6
+    bad = si.copy()
+    bad.md["body_type"][0] = T.BODY_GIANTPLANET
+    bad.r["x"][0] = 0.01  # not at rest in the origin: the transform looks for the star
+    with pytest.raises(RedError):
+        gpu_system(bad, thr, frame=T.FRAME_ASTRO)
+
+
+def test_astrocentric_steps_bit_exact(gpulib):
+    """Accelerations and RKF7(8) steps in the astrocentric frame against the oracle, state by
+    state: the star's starting pull, direct and indirect terms in source order, the star
+    pinned at the origin."""
+    disk = bodies.make_disk(n_pl=300, pl_type=T.BODY_PROTOPLANET, seed=31, m_range=(1e-9, 1e-6),
+                            embryos=((1e-6, 1.5, 0.05),))
+    thr = bodies.thresholds(collision_factor=0.0)
+    g = gpu_system(disk, thr, frame=T.FRAME_ASTRO)
+    o = pyoracle.OracleSystem(disk, thr, frame=T.FRAME_ASTRO)
+    ag, ao = g.calc_accel(), o.calc_accel()
+    for f in "xyz":
+        assert H.same(ag[f], ao[f]), f
+    for s in (g, o):
+        s.set_integrator(T.INT_RKF78, 1.0, True, 1e-12)
+    for _ in range(5):
+        assert g.step() == o.step()
+        _assert_same_state(g, o)
+    r = g.state(internal=True)[0]
+    assert r["x"][0] == 0.0 and r["y"][0] == 0.0 and r["z"][0] == 0.0
 
 
 def test_state_records_in_and_out(gpulib):
