@@ -156,6 +156,19 @@ struct rg_ctx {
     int* d_few_row0 = nullptr;  // per tile
     int64_t pairs_per_eval = 0;
     bool tiles_dirty = true;
+    int64_t tiles_version = 0;  // bumped by every upload of the tile plan
+    // CUDA graphs of the RKF7(8) step: the step-start evaluation and one attempt, each kept
+    // for both parities of the y / y_out swap, rebuilt when anything they freeze changes
+    struct StepGraph {
+        cudaGraphExec_t exec = nullptr;
+        std::vector<double> sig;  // the frozen launch parameters (graph_signature)
+        int64_t kernels = 0, evals = 0, pairs = 0;  // host counters one replay advances
+    };
+    StepGraph g_stage0[2], g_attempt[2];
+    bool capturing = false;     // launches are being captured (no allocation may happen)
+    bool capture_failed = false;
+    unsigned int* d_attempt_no = nullptr;  // the attempt's number for the event records (graphs)
+    int use_graphs = 1;
 
     int n_si() const { return cnt[0] + cnt[1] + cnt[2] + cnt[3]; }
     int n_nsi() const { return cnt[4] + cnt[5]; }
@@ -207,6 +220,11 @@ void free_all(rg_ctx* c)
     cudaFree(c->d_ev);
     cudaFree(c->d_hill);
     cudaFree(c->d_astro);
+    cudaFree(c->d_attempt_no);
+    for (int p = 0; p < 2; p++) {
+        if (c->g_stage0[p].exec) cudaGraphExecDestroy(c->g_stage0[p].exec);
+        if (c->g_attempt[p].exec) cudaGraphExecDestroy(c->g_attempt[p].exec);
+    }
     cudaFree(c->d_counters);
     cudaFree(c->d_ej);
     cudaFree(c->d_ej_count);
@@ -464,6 +482,7 @@ int sync_tiles(rg_ctx* c)
     }
     RG_CUDA_CHECK(cudaStreamSynchronize(c->st));
     c->tiles_dirty = false;
+    c->tiles_version++;
     return RG_OK;
 }
 
@@ -501,6 +520,10 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
     g.record = (record && c->inner_steps && g.f_rad > 0.0) ? 1 : 0;
     g.hill = hill ? 1 : 0;
     g.seq = ((uint32_t)attempt << 8) | (uint32_t)stage;
+    if (c->capturing && stage > 0) {  // a replayed attempt reads its number from the device
+        g.seq = (uint32_t)stage;
+        g.sys_attempt = c->d_attempt_no;
+    }
     g.ev = EventBuf{c->d_ev, c->d_ev_count, c->ev_cap};
     g.hv = EventBuf{c->d_hill, c->d_hill_count, c->ev_cap};
     if (hill) {
@@ -601,7 +624,10 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
                     chunk = (src_tiles + n - 1) / n * MIXED_SOURCE_TILE;
                 }
                 const int chunks = (src + chunk - 1) / chunk;
-                if (chunks > 1 && (size_t)chunks * 3 * c->cap > c->partial_cap) {
+                if (chunks > 1 && (size_t)chunks * 3 * c->cap > c->partial_cap && c->capturing) {
+                    c->capture_failed = true;  // allocate outside a capture (the next direct run)
+                    rc = RG_ERR_STATE;
+                } else if (chunks > 1 && (size_t)chunks * 3 * c->cap > c->partial_cap) {
                     cudaFree(c->d_partial);
                     c->d_partial = nullptr;
                     c->partial_cap = 0;
@@ -1038,38 +1064,131 @@ int step_rk5(rg_ctx* c)
 }
 
 // ---- RKF7(8) (int_rungekutta8.cu:704-797)
+// Everything a captured step graph freezes into its launches: buffer addresses, sizes, the
+// tile plan, the gravity and event options, the integrator's shape.
+std::vector<double> graph_signature(const rg_ctx* c)
+{
+    return {(double)(uintptr_t)c->d_y,  (double)(uintptr_t)c->d_yout, (double)c->cap,
+            (double)c->n_total(),       (double)c->tiles_version,      (double)(uintptr_t)c->d_tiles,
+            (double)c->gravity_mode,    c->hill_factor,                c->thr[RG_THRESHOLD_RADII_ENHANCE_FACTOR],
+            (double)c->inner_steps,     (double)c->close_encounter,    (double)c->int_type,
+            (double)c->adaptive,        (double)c->r_max,              (double)c->ectp,
+            (double)c->pairpar_S,       (double)c->rowseq_max_src,     (double)c->mixed_chunk_src,
+            (double)c->near_ratio,      (double)(uintptr_t)c->d_partial, (double)c->partial_cap,
+            (double)(uintptr_t)c->d_terms, (double)c->few_pitch,       (double)c->few_rows,
+            (double)(uintptr_t)c->d_astro};
+}
+
+// Captures `body` (launches on the context's stream) into `sg`; false: capture not possible
+// now (the body needed an allocation, or CUDA refused), the caller launches directly.
+template <class F>
+bool capture_step_graph(rg_ctx* c, rg_ctx::StepGraph& sg, F body)
+{
+    if (sg.exec) cudaGraphExecDestroy(sg.exec);
+    sg.exec = nullptr;
+    const int64_t k0 = c->n_kernels, e0 = c->n_gravity_evals, p0 = c->n_pairs;
+    if (cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    c->capturing = true;
+    c->capture_failed = false;
+    const int rc = body();
+    c->capturing = false;
+    cudaGraph_t graph = nullptr;
+    const cudaError_t err = cudaStreamEndCapture(c->st, &graph);
+    sg.kernels = c->n_kernels - k0;
+    sg.evals = c->n_gravity_evals - e0;
+    sg.pairs = c->n_pairs - p0;
+    c->n_kernels = k0;
+    c->n_gravity_evals = e0;
+    c->n_pairs = p0;
+    bool ok = rc == RG_OK && !c->capture_failed && err == cudaSuccess && graph;
+    if (ok && cudaGraphInstantiate(&sg.exec, graph, 0) != cudaSuccess) {
+        sg.exec = nullptr;
+        ok = false;
+    }
+    if (graph) cudaGraphDestroy(graph);
+    if (!ok) cudaGetLastError();  // a refused capture leaves no sticky error; launch directly
+    sg.sig = ok ? graph_signature(c) : std::vector<double>{};
+    return ok;
+}
+
+// Replays `sg` (capturing it first if its frozen parameters changed); false: launch directly.
+template <class F>
+bool replay_step_graph(rg_ctx* c, rg_ctx::StepGraph& sg, F body, int* rc)
+{
+    *rc = RG_OK;
+    if (!c->use_graphs || c->profiling || c->hold_tile_copies) return false;
+    if ((*rc = sync_tiles(c))) return false;
+    if (!sg.exec || sg.sig != graph_signature(c))
+        if (!capture_step_graph(c, sg, body)) return false;
+    const cudaError_t err = cudaGraphLaunch(sg.exec, c->st);
+    if (err != cudaSuccess) {
+        *rc = cuda_fail(err, "cudaGraphLaunch", __FILE__, __LINE__);
+        return true;
+    }
+    c->n_kernels += sg.kernels;
+    c->n_gravity_evals += sg.evals;
+    c->n_pairs += sg.pairs;
+    return true;
+}
+
 int step_rkf78(rg_ctx* c)
 {
     const size_t cap = (size_t)c->cap;
     c->attempt_dt.clear();
-    int rc = stage_zero(c);
+    const int parity = c->d_y < c->d_yout ? 0 : 1;
+    int rc = RG_OK;
+    if (!replay_step_graph(c, c->g_stage0[parity], [&] { return stage_zero(c); }, &rc)) rc = rc ? rc : stage_zero(c);
     if (rc) return rc;
     double max_err = 0.0;
     int iter = 0, attempt = 0;
-    do {
+    // one attempt's device work: stage rows, y_{n+1}, error maximum and the read-back of the
+    // error and event count into pinned memory (the attempt's number and trial step come
+    // from pinned memory too, so a captured attempt is replayed as it stands)
+    auto attempt_body = [&]() {
         // events of a previous attempt (and of stage 0) are dropped (int_rungekutta8.cu:730-733)
         RG_CUDA_CHECK(cudaMemsetAsync(c->d_ev_count, 0, sizeof(unsigned int), c->st));
-        c->dt_did = c->dt_try;
-        c->attempt_dt.push_back(c->dt_try);
-        rc = set_dt(c, c->dt_try);
+        RG_CUDA_CHECK(cudaMemcpyAsync(c->d_dt, &c->h_pin[0], sizeof(double), cudaMemcpyHostToDevice, c->st));
+        RG_CUDA_CHECK(cudaMemcpyAsync(c->d_attempt_no, &c->h_pin[6], sizeof(unsigned int), cudaMemcpyHostToDevice,
+                                      c->st));
+        int r2 = RG_OK;
         auto row = [&](int r) {
             double a[9];
             for (int q = 0; q < rk8_nterm[r]; q++) a[q] = rk8_a[rk8_aidx[r][q]];
             return ytemp_stage(c, FORM_SUM, r, rk8_stage[r], a, rk8_nterm[r], attempt);
         };
-        for (int r = 1; r <= 10 && !rc; r++) rc = row(r);
+        for (int r = 1; r <= 10 && !r2; r++) r2 = row(r);
         const int snp[7] = {0, 5, 6, 7, 8, 9, 10};
         const double bnp[7] = {rk8_b[0], rk8_b[5], rk8_b[6], rk8_b[8], rk8_b[10], 0.0, 0.0};  // c[0..4] used
-        if (!rc) rc = combine(c, FORM_RK8_NP1, snp, bnp, 7, c->d_yout, c->d_yout + 3 * cap);
+        if (!r2) r2 = combine(c, FORM_RK8_NP1, snp, bnp, 7, c->d_yout, c->d_yout + 3 * cap);
+        if (!r2 && c->adaptive) {
+            for (int r = 11; r < c->r_max && !r2; r++) r2 = row(r);
+            const int se[4] = {0, 10, 11, 12};
+            if (!r2) r2 = error_max(c, ERR_RK8, se, nullptr, 4);
+            if (!r2) {
+                RG_CUDA_CHECK(cudaMemcpyAsync(&c->h_pin[1], c->d_maxbits, sizeof(unsigned long long),
+                                              cudaMemcpyDeviceToHost, c->st));
+                RG_CUDA_CHECK(cudaMemcpyAsync((unsigned int*)&c->h_pin[2], c->d_ev_count, sizeof(unsigned int),
+                                              cudaMemcpyDeviceToHost, c->st));
+            }
+        }
+        return r2;
+    };
+    do {
+        c->dt_did = c->dt_try;
+        c->attempt_dt.push_back(c->dt_try);
+        c->h_pin[0] = c->dt_try;
+        *(unsigned int*)&c->h_pin[6] = (unsigned int)attempt;
+        if (!replay_step_graph(c, c->g_attempt[parity], attempt_body, &rc)) rc = rc ? rc : attempt_body();
         if (rc) return rc;
         if (c->adaptive) {
-            for (int r = 11; r < c->r_max && !rc; r++) rc = row(r);
-            const int se[4] = {0, 10, 11, 12};
-            if (!rc) rc = error_max(c, ERR_RK8, se, nullptr, 4);
+            RG_CUDA_CHECK(cudaStreamSynchronize(c->st));
+            unsigned long long bits;
+            std::memcpy(&bits, &c->h_pin[1], sizeof(bits));
             double raw;
-            unsigned int nev;
-            if (!rc) rc = read_attempt(c, &raw, &nev);
-            if (rc) return rc;
+            std::memcpy(&raw, &bits, sizeof(raw));
             max_err = std::fabs(c->dt_try * (41.0 / 840.0) * raw);
             c->dt_try *= 0.9 * std::pow(c->tol / max_err, 1.0 / (c->order + 1));
         }
@@ -1385,6 +1504,7 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
     chk(dalloc(&c->d_ej_count, 1));
     chk(dalloc(&c->d_maxbits, 1));
     chk(dalloc(&c->d_dt, 1));
+    chk(dalloc(&c->d_attempt_no, 1));
     chk(dalloc(&c->d_part, (size_t)5 * nt));
     chk(dalloc(&c->d_records, (size_t)8 * nt));
     chk(dalloc((char**)&c->d_split, SPLIT_POS_BYTES * (size_t)nt));

@@ -34,6 +34,7 @@
 #include "../../include/redgb.h"
 #include "abi_guard.h"
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "ens_events.h"
 #include "host_tools.h"
 #include "kernels.h"
@@ -64,31 +65,13 @@ struct EnsStageArgs {
     double* out_hi;       // rows 3..5
 };
 
-// FORM_SUM (stage rows) or FORM_RK8_NP1 (y_{n+1}), one CTA per stage tile.
-// FUSED = false: the reference's operation order, y + dt * (c_0 k_0 + c_1 k_1 + ...),
-// without contraction (the bit-exact FP64 mode).  FUSED = true (mixed-precision mode): the
-// per-disk coefficients dt * c_q are formed once per CTA and the sum is contracted,
-// y + fma(dt c_q, k_q, ...), half the FP64 operations -- GB300 retires about two FP64
-// operations per SM and clock, so these kernels are bound by FP64 issue, not by HBM.
-template <int FORM, int NTERM, bool FUSED>
-__device__ __forceinline__ double ens_combine_one(const EnsStageArgs& a, const double* w, double dt, long long e)
+// FORM_SUM (stage rows) or FORM_RK8_NP1 (y_{n+1}), one CTA per stage tile, in the
+// reference's operation order, y + dt * (c_0 k_0 + c_1 k_1 + ...), without contraction (the
+// bit-exact FP64 mode).
+template <int FORM, int NTERM>
+__device__ __forceinline__ double ens_combine_one(const EnsStageArgs& a, double dt, long long e)
 {
     const double y = a.y[e];
-    if (FUSED) {
-        double sum;
-        if (FORM == FORM_SUM) {
-            sum = w[0] * a.k[0][e];
-#pragma unroll
-            for (int q = 1; q < NTERM; q++) sum = fma(w[q], a.k[q][e], sum);
-        } else {
-            sum = w[0] * a.k[0][e];
-            sum = fma(w[1], a.k[1][e], sum);
-            sum = fma(w[2], a.k[2][e] + a.k[3][e], sum);
-            sum = fma(w[3], a.k[4][e] + a.k[5][e], sum);
-            sum = fma(w[4], a.k[6][e], sum);
-        }
-        return y + sum;
-    }
     if (FORM == FORM_SUM) {
         double sum = a.c[0] * a.k[0][e];
 #pragma unroll
@@ -101,32 +84,69 @@ __device__ __forceinline__ double ens_combine_one(const EnsStageArgs& a, const d
 
 // Rows one after another, two independent elements per thread and iteration (their loads
 // and FP64 chains interleave: these kernels are bound by FP64 issue and load latency).
-template <int FORM, int NTERM, bool FUSED>
+template <int FORM, int NTERM>
 __global__ void __launch_bounds__(256) ens_combine_kernel(EnsStageArgs a)
 {
     const StageTile t = a.tiles[blockIdx.x];
     if (!a.active[t.sys]) return;
     const double dt = a.dt[t.sys];
-    double w[MAXT];
-    if (FUSED) {
-#pragma unroll
-        for (int q = 0; q < MAXT; q++) w[q] = dt * a.c[q];
-    }
     const int nb = t.b1 - t.b0;
     for (int row = 0; row < 6; row++) {
         const long long base = (long long)row * a.stride + t.b0;
         double* out = row < 3 ? a.out_lo + base : a.out_hi + base - 3LL * a.stride;
         for (int i = threadIdx.x; i < nb; i += 2 * blockDim.x) {
             const int i2 = i + blockDim.x;
-            const double o1 = ens_combine_one<FORM, NTERM, FUSED>(a, w, dt, base + i);
+            const double o1 = ens_combine_one<FORM, NTERM>(a, dt, base + i);
             if (i2 < nb) {
-                const double o2 = ens_combine_one<FORM, NTERM, FUSED>(a, w, dt, base + i2);
+                const double o2 = ens_combine_one<FORM, NTERM>(a, dt, base + i2);
                 out[i] = o1;
                 out[i2] = o2;
             } else {
                 out[i] = o1;
             }
         }
+    }
+}
+
+// Mixed-precision mode: the stage sum delta = sum_q (dt c_q) k_q in double-float on the FP32
+// pipes -- each k_q split exactly into hi + lo on its bit pattern (integer operations), the
+// products and the running sum kept to about 2^-46 of delta -- then y + delta with a single
+// FP64 addition.  |delta| is a small fraction of |y| for every stage of a step the controller
+// accepts, so delta's double-float error stays far below y's own rounding; the FP64 form keeps
+// the reference's operation order (ens_combine_one).  Two FP64 operations per element instead
+// of NTERM + 1 on GB300's FP64 pipe, which bounded these kernels.
+template <int FORM, int NTERM>
+__device__ __forceinline__ double ens_combine_df(const EnsStageArgs& a, const DF* w, long long e)
+{
+    DF acc;
+    if (FORM == FORM_SUM) {
+        acc = df_mul(w[0], split_df(a.k[0][e]));
+#pragma unroll
+        for (int q = 1; q < NTERM; q++) acc = df_add(acc, df_mul(w[q], split_df(a.k[q][e])));
+    } else {
+        acc = df_mul(w[0], split_df(a.k[0][e]));
+        acc = df_add(acc, df_mul(w[1], split_df(a.k[1][e])));
+        acc = df_add(acc, df_mul(w[2], df_add(split_df(a.k[2][e]), split_df(a.k[3][e]))));
+        acc = df_add(acc, df_mul(w[3], df_add(split_df(a.k[4][e]), split_df(a.k[5][e]))));
+        acc = df_add(acc, df_mul(w[4], split_df(a.k[6][e])));
+    }
+    return a.y[e] + df_to_double(acc);
+}
+
+template <int FORM, int NTERM>
+__global__ void __launch_bounds__(256) ens_combine_df_kernel(EnsStageArgs a)
+{
+    const StageTile t = a.tiles[blockIdx.x];
+    if (!a.active[t.sys]) return;
+    const double dt = a.dt[t.sys];
+    DF w[MAXT];
+#pragma unroll
+    for (int q = 0; q < MAXT; q++) w[q] = split_df(dt * a.c[q]);
+    const int nb = t.b1 - t.b0;
+    for (int row = 0; row < 6; row++) {
+        const long long base = (long long)row * a.stride + t.b0;
+        double* out = row < 3 ? a.out_lo + base : a.out_hi + base - 3LL * a.stride;
+        for (int i = threadIdx.x; i < nb; i += blockDim.x) out[i] = ens_combine_df<FORM, NTERM>(a, w, base + i);
     }
 }
 
@@ -1037,9 +1057,9 @@ int launch_stage(rg_ens* e, int form, int nterm, const int* stages, const double
 #define RG_ENS(F, T)                                                     \
     do {                                                                 \
         if (fused)                                                       \
-            ens_combine_kernel<F, T, true><<<g, 256, 0, e->st>>>(a);     \
+            ens_combine_df_kernel<F, T><<<g, 256, 0, e->st>>>(a);        \
         else                                                             \
-            ens_combine_kernel<F, T, false><<<g, 256, 0, e->st>>>(a);    \
+            ens_combine_kernel<F, T><<<g, 256, 0, e->st>>>(a);           \
     } while (0)
     if (form == FORM_RK8_NP1) {
         RG_ENS(FORM_RK8_NP1, 7);

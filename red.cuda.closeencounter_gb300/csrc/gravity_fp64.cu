@@ -85,8 +85,14 @@ __device__ __forceinline__ void pair_term(const GravArgs& g, const Tile& tile, i
 // astrocentric frame of the reference's CPU path -- each sink starts from the star's pull
 // and, for every source it interacts with, adds the direct term and then subtracts the
 // source's indirect term (pp_disk.cu:413-454), in source order.
+// resident CTAs per SM the register budget is cut for (the pair term's integer square root and
+// division hold many values; more resident warps hide their latency)
+#ifndef RG_PAIRPAR_MIN_BLOCKS
+#define RG_PAIRPAR_MIN_BLOCKS 3
+#endif
+
 template <int S, bool ASTRO>
-__global__ void __launch_bounds__(256) grav_fp64_pairpar(GravArgs g)
+__global__ void __launch_bounds__(256, RG_PAIRPAR_MIN_BLOCKS) grav_fp64_pairpar(GravArgs g)
 {
     constexpr int NT = 256;
     constexpr int J = 1024 / S;

@@ -31,6 +31,7 @@
 
 #include "../../include/redgb.h"
 #include "common.cuh"
+#include "dfloat.cuh"
 #include "kernels.h"
 
 namespace redgb {
@@ -48,39 +49,6 @@ struct SplitPos {
 // active with m = 0 until the next ejection check): |r|^2 then stays finite in FP32, so
 // the pair loop needs no clamp either, and such a body's zero mass gives a zero term.
 //
-// The split is done on the bit patterns, with integer operations only (a conversion
-// FP64 -> FP32 runs on GB300's scarce FP64 pipe): hi = v rounded to 24 significant bits
-// (round half up on the dropped 29 bits; a carry into the exponent is the correct next
-// value), lo = the signed remainder rounded to FP32, so |v - (hi + lo)| <= 2^-48 |v| and hi
-// carries no bias.  |v| < 2^-74 gives lo = 0 and |v| < 2^-126 gives hi = lo = 0.
-__device__ __forceinline__ void split_bits(double v, float& hi, float& lo)
-{
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
-    const unsigned sign = (unsigned)(b >> 32) & 0x80000000u;
-    const int e = (int)((b >> 52) & 0x7ffu);
-    const int ef = e - 896;  // FP32 biased exponent
-    if (ef <= 0) {
-        hi = lo = 0.0f;
-        return;
-    }
-    if (ef >= 254) {  // at or beyond FP32's largest binade, or inf / NaN
-        hi = (float)v;
-        lo = 0.0f;
-        return;
-    }
-    const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
-    unsigned hb = sign | ((unsigned)ef << 23) | (unsigned)(mant >> 29);
-    int r = (int)(mant & 0x1FFFFFFFu);  // the dropped bits, in units of 2^(e - 1075)
-    if (r >= (1 << 28)) {
-        hb += 1u;
-        r -= 1 << 29;
-    }
-    hi = __uint_as_float(hb);
-    const int es = e - 948;  // FP32 biased exponent of 2^(e - 1075)
-    const float l = es > 0 ? __int2float_rn(r) * __uint_as_float((unsigned)es << 23) : 0.0f;
-    lo = sign ? -l : l;
-}
-
 __device__ __forceinline__ void split_coord(double v, float& hi, float& lo)
 {
     split_bits(v, hi, lo);
@@ -282,68 +250,6 @@ __device__ __forceinline__ void exact_event_tests(const GravArgs& g, const Tile&
 // double-float until one conversion to FP64 per sink and component.  Event decisions are
 // screened in FP32 with the same 1e-3 margin as the mixed kernel and re-taken in FP64.
 
-struct DF {
-    float hi, lo;
-};
-
-__device__ __forceinline__ DF df_two_sum(float a, float b)
-{
-    const float s = a + b;
-    const float bb = s - a;
-    return DF{s, (a - (s - bb)) + (b - bb)};
-}
-
-// |a| >= |b| (or a == 0)
-__device__ __forceinline__ DF df_fast_sum(float a, float b)
-{
-    const float s = a + b;
-    return DF{s, b - (s - a)};
-}
-
-__device__ __forceinline__ DF df_two_prod(float a, float b)
-{
-    const float p = a * b;
-    return DF{p, fmaf(a, b, -p)};
-}
-
-__device__ __forceinline__ DF df_add(DF a, DF b)
-{
-    DF s = df_two_sum(a.hi, b.hi);
-    const DF t = df_two_sum(a.lo, b.lo);
-    s.lo += t.hi;
-    s = df_fast_sum(s.hi, s.lo);
-    s.lo += t.lo;
-    return df_fast_sum(s.hi, s.lo);
-}
-
-__device__ __forceinline__ DF df_mul(DF a, DF b)
-{
-    DF p = df_two_prod(a.hi, b.hi);
-    p.lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
-    return df_fast_sum(p.hi, p.lo);
-}
-
-// (ah + al) - (bh + bl) of two split coordinates
-__device__ __forceinline__ DF df_diff(float ah, float al, float bh, float bl)
-{
-    const DF s = df_two_sum(ah, -bh);
-    return df_two_sum(s.hi, (al - bl) + s.lo);
-}
-
-// FP32 -> FP64 on the bit pattern (exact; no FP64-pipe conversion); FP32 denormals -> 0
-__device__ __forceinline__ double f2d_bits(float f)
-{
-    const unsigned u = __float_as_uint(f);
-    const unsigned ef = (u >> 23) & 0xffu;
-    if (ef == 0) return 0.0;
-    if (ef == 255) return (double)f;
-    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                 ((unsigned long long)(ef + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)b);
-}
-
-__device__ __forceinline__ double df_to_double(DF a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }
-
 // a double-float term into a compensated FP32 accumulator
 __device__ __forceinline__ void acc_df(Acc2& acc, DF t)
 {
@@ -376,13 +282,6 @@ __device__ __forceinline__ void df_term(const SplitPos& si, const SplitPos& pj, 
 {
     df_term_disp(df_diff(pj.xy.x, pj.xy.y, si.xy.x, si.xy.y), df_diff(pj.xy.z, pj.xy.w, si.xy.z, si.xy.w),
                  df_diff(pj.zm.x, pj.zm.y, si.zm.x, si.zm.y), pj.zm.z, pj.zm.w, tx, ty, tz, r2f);
-}
-
-__device__ __forceinline__ DF split_df(double v)
-{
-    DF d;
-    split_bits(v, d.hi, d.lo);
-    return d;
 }
 
 // r^2 below which a pair of this sink takes the FP64 displacement: beyond it the split
