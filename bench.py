@@ -53,7 +53,7 @@ FLOP_PER_PAIR = 36  # the reference's own count (pp_disk.cu:170-184,293)
 # DRAM bytes (read + write) of one launch of each gravity kernel of the default workload, from
 # one ncu capture of one launch (`-k <kernel> -c 1`) of
 # `python bench.py --no-ensemble --no-dense-ring --no-cpu-baseline --no-planetesimal-disk --steps 3 --warmup 3`
-NCU_TRAFFIC = {("self_gravitating_16384_rk4", "mixed"): 1332224, ("self_gravitating_16384_rk4", "fp64"): 819712}
+NCU_TRAFFIC = {("self_gravitating_16384_rk4", "mixed"): 1332224, ("self_gravitating_16384_rk4", "fp64"): 820480}
 
 def _hbm_peak():
     """The measured HBM copy bandwidth of the GB300s (MEASURED_PEAKS.json, written
