@@ -688,7 +688,7 @@ def ensemble_section(args):
     plain_mixed, ev_m = batched(T.GRAVITY_MIXED, None)
     plain_fp64, ev_f = batched(T.GRAVITY_FP64, None)
 
-    def profiled(mode, attempts=16):
+    def profiled(mode, attempts=16, proposer=None):
         """Device time by kernel class over `attempts` attempts launched directly with CUDA
         events (rg_ens_set_profiling), every disk running: the stage-combine and error-norm
         kernels against the measured HBM peak at the reference's algorithmic bytes
@@ -698,6 +698,8 @@ def ensemble_section(args):
         e.set_options(gravity_mode=mode, hill_factor=hill)
         if not args.no_autotune:
             e.autotune(2)
+        if proposer is not None:
+            proposer.attach(e)
         e.advance(warm_day)
         e.set_profiling(True)
         e.profile()
@@ -715,7 +717,8 @@ def ensemble_section(args):
                                    "launches": p["stage_launches"],
                                    "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy)"}}
 
-    kernel_time = {"mixed": profiled(T.GRAVITY_MIXED), "fp64": profiled(T.GRAVITY_FP64)}
+    kernel_time = {"learned_mixed": profiled(T.GRAVITY_MIXED, proposer=net), "mixed": profiled(T.GRAVITY_MIXED),
+                   "fp64": profiled(T.GRAVITY_FP64)}
 
     # the plain FP64 form, one disk at a time through the single-disk API
     sample = disks[::max(1, len(disks) // args.sequential_sample)][:args.sequential_sample]

@@ -2,8 +2,7 @@
 // floats: Knuth's two-sum, the FMA two-product, and the double-double add / multiply of
 // Hida, Li and Bailey (2001) carried out in float), and exact FP64 <-> FP32 conversions done
 // on the bit patterns with integer operations (a conversion on the FP64 pipe would cost as
-// much issue as about 64 FP32 operations).  Used by the mixed-precision gravity kernels and by
-// the ensemble's mixed-precision stage combinations.
+// much issue as about 64 FP32 operations).  Used by the mixed-precision gravity kernels.
 #pragma once
 
 #include <cuda_runtime.h>

@@ -144,6 +144,38 @@ __device__ __forceinline__ bool mine(const EnsEventArgs& a, int s, const DevEven
 }  // namespace
 
 // ------------------------------------------------------------------- Hill-sphere records
+constexpr int HILL_LOCAL = 48;  // a disk's records gathered in one pass (more: repeated scans)
+
+__device__ void log_hill(const EnsEventArgs& a, int s, int b, const DevEvent& d, const long long* prev, int n_prev,
+                         long long* next, int& n_next)
+{
+    const long long key = pair_key(a.id[d.i], a.id[d.j]);
+    bool seen = false;
+    for (int q = 0; q < n_prev && !seen; q++) seen = prev[q] == key;
+    if (!seen) {
+        rg_event_t* x = log_slot(a, s);
+        if (x) {
+            x->event_name = RG_EVENT_CLOSE_ENCOUNTER;
+            x->t = d.t;  // the step start, where the pair was found inside the sphere
+            x->d = d.d;
+            x->id1 = a.id[d.i];
+            x->id2 = a.id[d.j];
+            x->idx1 = d.i - b;
+            x->idx2 = d.j - b;
+            x->p1 = a.prm[d.i];
+            x->p2 = a.prm[d.j];
+            x->r1 = rg_vec_t{d.ri[0], d.ri[1], d.ri[2], 0.0};
+            x->v1 = rg_vec_t{d.vi[0], d.vi[1], d.vi[2], 0.0};
+            x->r2 = rg_vec_t{d.rj[0], d.rj[1], d.rj[2], 0.0};
+            x->v2 = rg_vec_t{d.vj[0], d.vj[1], d.vj[2], 0.0};
+        }
+    }
+    if (n_next < a.hill_set_cap)
+        next[n_next++] = key;
+    else
+        atomicOr(a.flags, ENS_FLAG_HILL_SET);
+}
+
 __global__ void ens_hill_kernel(EnsEventArgs a)
 {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -155,48 +187,50 @@ __global__ void ens_hill_kernel(EnsEventArgs a)
     long long* next = a.hill_set + ((long long)s * 2 + (cur ^ 1)) * a.hill_set_cap;
     const int n_prev = a.hill_n[s];
     int n_next = 0;
-    // records of this disk in (sink, source) order: repeatedly the smallest key above the last
-    long long last = -1;
-    for (;;) {
-        long long best = 0x7fffffffffffffffll;
-        unsigned int bk = 0xffffffffu;
-        for (unsigned int k = 0; k < n; k++) {
-            const DevEvent& d = a.hill[k];
-            if (d.sys != s || d.kind != 1) continue;
-            const long long key = ((long long)d.i << 32) | (long long)(unsigned int)d.j;
-            if (key > last && key < best) {
-                best = key;
-                bk = k;
-            }
+    // this disk's records in (sink, source) order: one pass gathers them (insertion-sorted by
+    // key); a disk with more than HILL_LOCAL records repeats the scan for the rest
+    long long key[HILL_LOCAL];
+    unsigned int idx[HILL_LOCAL];
+    int m = 0;
+    bool more = false;
+    for (unsigned int k = 0; k < n; k++) {
+        const DevEvent& d = a.hill[k];
+        if (d.sys != s || d.kind != 1) continue;
+        if (m == HILL_LOCAL) {
+            more = true;
+            break;
         }
-        if (bk == 0xffffffffu) break;
-        last = best;
-        const DevEvent& d = a.hill[bk];
-        const long long key = pair_key(a.id[d.i], a.id[d.j]);
-        bool seen = false;
-        for (int q = 0; q < n_prev && !seen; q++) seen = prev[q] == key;
-        if (!seen) {
-            rg_event_t* x = log_slot(a, s);
-            if (x) {
-                x->event_name = RG_EVENT_CLOSE_ENCOUNTER;
-                x->t = d.t;  // the step start, where the pair was found inside the sphere
-                x->d = d.d;
-                x->id1 = a.id[d.i];
-                x->id2 = a.id[d.j];
-                x->idx1 = d.i - b;
-                x->idx2 = d.j - b;
-                x->p1 = a.prm[d.i];
-                x->p2 = a.prm[d.j];
-                x->r1 = rg_vec_t{d.ri[0], d.ri[1], d.ri[2], 0.0};
-                x->v1 = rg_vec_t{d.vi[0], d.vi[1], d.vi[2], 0.0};
-                x->r2 = rg_vec_t{d.rj[0], d.rj[1], d.rj[2], 0.0};
-                x->v2 = rg_vec_t{d.vj[0], d.vj[1], d.vj[2], 0.0};
-            }
+        const long long kk = ((long long)d.i << 32) | (long long)(unsigned int)d.j;
+        int p = m++;
+        while (p > 0 && key[p - 1] > kk) {
+            key[p] = key[p - 1];
+            idx[p] = idx[p - 1];
+            p--;
         }
-        if (n_next < a.hill_set_cap)
-            next[n_next++] = key;
-        else
-            atomicOr(a.flags, ENS_FLAG_HILL_SET);
+        key[p] = kk;
+        idx[p] = k;
+    }
+    if (!more) {
+        for (int q = 0; q < m; q++) log_hill(a, s, b, a.hill[idx[q]], prev, n_prev, next, n_next);
+    } else {
+        // repeatedly the smallest key above the last
+        long long last = -1;
+        for (;;) {
+            long long best = 0x7fffffffffffffffll;
+            unsigned int bk = 0xffffffffu;
+            for (unsigned int k = 0; k < n; k++) {
+                const DevEvent& d = a.hill[k];
+                if (d.sys != s || d.kind != 1) continue;
+                const long long kk = ((long long)d.i << 32) | (long long)(unsigned int)d.j;
+                if (kk > last && kk < best) {
+                    best = kk;
+                    bk = k;
+                }
+            }
+            if (bk == 0xffffffffu) break;
+            last = best;
+            log_hill(a, s, b, a.hill[bk], prev, n_prev, next, n_next);
+        }
     }
     a.hill_n[s] = n_next;
     a.hill_which[s] = cur ^ 1;

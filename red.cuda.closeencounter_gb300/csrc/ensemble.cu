@@ -108,45 +108,55 @@ __global__ void __launch_bounds__(256) ens_combine_kernel(EnsStageArgs a)
     }
 }
 
-// Mixed-precision mode: the stage sum delta = sum_q (dt c_q) k_q in double-float on the FP32
-// pipes -- each k_q split exactly into hi + lo on its bit pattern (integer operations), the
-// products and the running sum kept to about 2^-46 of delta -- then y + delta with a single
-// FP64 addition.  |delta| is a small fraction of |y| for every stage of a step the controller
-// accepts, so delta's double-float error stays far below y's own rounding; the FP64 form keeps
-// the reference's operation order (ens_combine_one).  Two FP64 operations per element instead
-// of NTERM + 1 on GB300's FP64 pipe, which bounded these kernels.
+// Mixed-precision mode: the per-disk coefficients dt * c_q are formed once per CTA and the sum
+// is contracted, y + fma(dt c_q, k_q, ...): NTERM + 1 FP64 operations per element, half the
+// bit-exact form's.  (The same sum in double-float on the FP32 pipes, with one FP64 addition
+// onto y, was measured slower on GB300: 2.35 against 1.41 ms of stage kernels per attempt of
+// the 256-disk ensemble, the FP32 / integer work of the splits and double-float products
+// outweighing the FP64 operations it saves.)
 template <int FORM, int NTERM>
-__device__ __forceinline__ double ens_combine_df(const EnsStageArgs& a, const DF* w, long long e)
+__device__ __forceinline__ double ens_combine_fma(const EnsStageArgs& a, const double* w, long long e)
 {
-    DF acc;
+    const double y = a.y[e];
+    double sum;
     if (FORM == FORM_SUM) {
-        acc = df_mul(w[0], split_df(a.k[0][e]));
+        sum = w[0] * a.k[0][e];
 #pragma unroll
-        for (int q = 1; q < NTERM; q++) acc = df_add(acc, df_mul(w[q], split_df(a.k[q][e])));
+        for (int q = 1; q < NTERM; q++) sum = fma(w[q], a.k[q][e], sum);
     } else {
-        acc = df_mul(w[0], split_df(a.k[0][e]));
-        acc = df_add(acc, df_mul(w[1], split_df(a.k[1][e])));
-        acc = df_add(acc, df_mul(w[2], df_add(split_df(a.k[2][e]), split_df(a.k[3][e]))));
-        acc = df_add(acc, df_mul(w[3], df_add(split_df(a.k[4][e]), split_df(a.k[5][e]))));
-        acc = df_add(acc, df_mul(w[4], split_df(a.k[6][e])));
+        sum = w[0] * a.k[0][e];
+        sum = fma(w[1], a.k[1][e], sum);
+        sum = fma(w[2], a.k[2][e] + a.k[3][e], sum);
+        sum = fma(w[3], a.k[4][e] + a.k[5][e], sum);
+        sum = fma(w[4], a.k[6][e], sum);
     }
-    return a.y[e] + df_to_double(acc);
+    return y + sum;
 }
 
 template <int FORM, int NTERM>
-__global__ void __launch_bounds__(256) ens_combine_df_kernel(EnsStageArgs a)
+__global__ void __launch_bounds__(256) ens_combine_fma_kernel(EnsStageArgs a)
 {
     const StageTile t = a.tiles[blockIdx.x];
     if (!a.active[t.sys]) return;
     const double dt = a.dt[t.sys];
-    DF w[MAXT];
+    double w[MAXT];
 #pragma unroll
-    for (int q = 0; q < MAXT; q++) w[q] = split_df(dt * a.c[q]);
+    for (int q = 0; q < MAXT; q++) w[q] = dt * a.c[q];
     const int nb = t.b1 - t.b0;
     for (int row = 0; row < 6; row++) {
         const long long base = (long long)row * a.stride + t.b0;
         double* out = row < 3 ? a.out_lo + base : a.out_hi + base - 3LL * a.stride;
-        for (int i = threadIdx.x; i < nb; i += blockDim.x) out[i] = ens_combine_df<FORM, NTERM>(a, w, base + i);
+        for (int i = threadIdx.x; i < nb; i += 2 * blockDim.x) {
+            const int i2 = i + blockDim.x;
+            const double o1 = ens_combine_fma<FORM, NTERM>(a, w, base + i);
+            if (i2 < nb) {
+                const double o2 = ens_combine_fma<FORM, NTERM>(a, w, base + i2);
+                out[i] = o1;
+                out[i2] = o2;
+            } else {
+                out[i] = o1;
+            }
+        }
     }
 }
 
@@ -355,27 +365,47 @@ __global__ void ens_finalize_kernel(EnsSys s)
 
 // features of a step start: max |a| and min (d / mutual Hill radius)^3 over the pairs of
 // every body with a massive non-star self-interacting body, in FP32 (the features are
-// logarithms fed to an FP32 network; GB300 spends about 64 FP32 issue slots per FP64
-// operation).  One body's contribution; b is its disk's body 0, ns the disk's SI count.
+// logarithms fed to an FP32 network).  FP64 values become FP32 on their bit patterns
+// (split_bits, integer operations): a hardware conversion runs on GB300's FP64 pipe.
+constexpr int FEAT_MAX_SI = 16;  // self-interacting bodies per disk staged in shared memory
+
+__device__ __forceinline__ float to_f32(double v)
+{
+    float hi, lo;
+    split_bits(v, hi, lo);
+    return hi;
+}
+
+// one body's contribution; si: the disk's first FEAT_MAX_SI SI bodies (positions relative to
+// body 0, masses, distance from body 0) in shared memory, ns of them in all (the rest are read
+// from the state rows), M = body 0's mass
 __device__ __forceinline__ void body_features(const double* y, const double* k0, const double* mass, const int* id,
-                                              long long stride, int b, int ns, int i, float& am, float& h3)
+                                              long long stride, int b, int ns, const float4* si, const float* si_r,
+                                              float x0, float y0, float z0, float M, int i, float& am, float& h3)
 {
     if (id[i] <= 0) return;
-    const float ax = (float)k0[3LL * stride + i], ay = (float)k0[4LL * stride + i], az = (float)k0[5LL * stride + i];
+    const float ax = to_f32(k0[3LL * stride + i]), ay = to_f32(k0[4LL * stride + i]), az = to_f32(k0[5LL * stride + i]);
     am = fmaxf(am, sqrtf(ax * ax + ay * ay + az * az));
-    const float M = (float)mass[b];
-    const float x0 = (float)y[b], y0 = (float)y[stride + b], z0 = (float)y[2LL * stride + b];
-    const float xi = (float)y[i] - x0, yi = (float)y[stride + i] - y0, zi = (float)y[2LL * stride + i] - z0;
+    const float xi = to_f32(y[i]) - x0, yi = to_f32(y[stride + i]) - y0, zi = to_f32(y[2LL * stride + i]) - z0;
     const float ri = sqrtf(xi * xi + yi * yi + zi * zi);
-    const float mi = (float)mass[i];
-    for (int j = b + 1; j < b + ns; j++) {
-        if (j == i || id[j] <= 0) continue;
-        const float xj = (float)y[j] - x0, yj = (float)y[stride + j] - y0, zj = (float)y[2LL * stride + j] - z0;
-        const float dx = xj - xi, dy = yj - yi, dz = zj - zi;
+    const float mi = to_f32(mass[i]);
+    for (int q = 1; q < ns; q++) {
+        const int j = b + q;
+        float4 sj;
+        float rj;
+        if (q < FEAT_MAX_SI) {
+            sj = si[q];
+            rj = si_r[q];
+        } else {
+            sj = make_float4(to_f32(y[j]) - x0, to_f32(y[stride + j]) - y0, to_f32(y[2LL * stride + j]) - z0,
+                             id[j] > 0 ? to_f32(mass[j]) : -1.0f);
+            rj = sqrtf(sj.x * sj.x + sj.y * sj.y + sj.z * sj.z);
+        }
+        if (j == i || !(sj.w >= 0.0f)) continue;  // inactive SI bodies carry w = -1
+        const float dx = sj.x - xi, dy = sj.y - yi, dz = sj.z - zi;
         const float d2 = dx * dx + dy * dy + dz * dz;
-        const float rj = sqrtf(xj * xj + yj * yj + zj * zj);
         const float hh = 0.5f * (ri + rj);
-        const float rh3 = (mi + (float)mass[j]) / (3.0f * M) * hh * hh * hh;
+        const float rh3 = (mi + sj.w) / (3.0f * M) * hh * hh * hh;
         if (rh3 > 0.0f) h3 = fminf(h3, d2 * sqrtf(d2) / rh3);
     }
 }
@@ -413,11 +443,22 @@ __global__ void __launch_bounds__(256) ens_propose_kernel(PropArgs a)
     const EnsSys& s = a.s;
     if (!s.active_f0[d]) return;
     __shared__ float red_am[8], red_h3[8];
+    __shared__ float4 si[FEAT_MAX_SI];
+    __shared__ float si_r[FEAT_MAX_SI];
     float am = 0.0f, h3 = 3.0e38f;
     {
-        const int b = a.base[d], ns = a.nsi[d], n = a.ntot[d];
+        const int b = a.base[d], n = a.ntot[d], ns = a.nsi[d];
+        const float x0 = to_f32(a.y[b]), y0 = to_f32(a.y[a.stride + b]), z0 = to_f32(a.y[2LL * a.stride + b]);
+        const float M = to_f32(a.mass[b]);
+        if ((int)threadIdx.x < min(ns, FEAT_MAX_SI)) {
+            const int j = b + threadIdx.x;
+            const float xj = to_f32(a.y[j]) - x0, yj = to_f32(a.y[a.stride + j]) - y0, zj = to_f32(a.y[2LL * a.stride + j]) - z0;
+            si[threadIdx.x] = make_float4(xj, yj, zj, a.id[j] > 0 ? to_f32(a.mass[j]) : -1.0f);
+            si_r[threadIdx.x] = sqrtf(xj * xj + yj * yj + zj * zj);
+        }
+        __syncthreads();
         for (int i = b + threadIdx.x; i < b + n; i += blockDim.x)
-            body_features(a.y, a.k0, a.mass, a.id, a.stride, b, ns, i, am, h3);
+            body_features(a.y, a.k0, a.mass, a.id, a.stride, b, ns, si, si_r, x0, y0, z0, M, i, am, h3);
         for (int off = 16; off > 0; off >>= 1) {
             am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, off));
             h3 = fminf(h3, __shfl_xor_sync(0xffffffffu, h3, off));
@@ -1057,7 +1098,7 @@ int launch_stage(rg_ens* e, int form, int nterm, const int* stages, const double
 #define RG_ENS(F, T)                                                     \
     do {                                                                 \
         if (fused)                                                       \
-            ens_combine_df_kernel<F, T><<<g, 256, 0, e->st>>>(a);        \
+            ens_combine_fma_kernel<F, T><<<g, 256, 0, e->st>>>(a);       \
         else                                                             \
             ens_combine_kernel<F, T><<<g, 256, 0, e->st>>>(a);           \
     } while (0)

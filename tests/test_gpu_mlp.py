@@ -87,27 +87,48 @@ def test_dither_spreads_error_ratios(gpulib):
 
 
 def test_trained_proposer_gain(gpulib):
-    """Trained on dithered attempt logs of disks with seeds 1-16, evaluated on seeds 65-70:
-    the proposer must keep the accuracy (|dE/E| <= 1e-10 over the interval) and take fewer
-    attempts than the plain controller; the measured gain is printed."""
+    """Trained on dithered attempt logs of disks with seeds 1-16 (held-out residuals from whole
+    disks choose the safety factor), evaluated on seeds 65-72: the proposer must keep the
+    accuracy (|dE/E| <= 1e-10 over the interval), take fewer attempts than the plain
+    controller, and deliver more simulated years per second of wall time on the same disks
+    (each form's interval is one graph launch, timed after a warm-up interval)."""
+    import time
+    import torch
     train = [bodies.config_disk("ensemble_member", seed=s, n=512) for s in range(1, 17)]
-    ens, _, _ = _run(train, 20.0, log=True, dither=0.15)
-    x, y = dataset_from_log(ens.step_log(), 1e-10)
+    ens, _, _ = _run(train, 60.0, log=True, dither=0.15)
+    x, y, grp = dataset_from_log(ens.step_log(), 1e-10, with_groups=True)
     assert len(x) > 5000
-    net, loss = fit(x, y, seed=0, epochs=40)
-    # the network explains part of the ideal step's drift
-    assert net.residual_std < np.std(y)
-    evald = [bodies.config_disk("ensemble_member", seed=s, n=512) for s in range(65, 71)]
-    _, plain, dE_plain = _run(evald, 10.0)
-    _, learned, dE_learned = _run(evald, 10.0, proposer=net)
-    att_plain = sum(s["n_tried_step"] for s in plain)
-    att_learned = sum(s["n_tried_step"] for s in learned)
-    rej_plain = sum(s["n_failed_step"] for s in plain) / att_plain
-    rej_learned = sum(s["n_failed_step"] for s in learned) / att_learned
-    print(f"attempts plain {att_plain} learned {att_learned} ({att_plain / att_learned:.3f}x); rejected "
-          f"{rej_plain:.3%} vs {rej_learned:.3%}; dE/E {dE_plain:.2e} vs {dE_learned:.2e}; train loss {loss:.2e}; "
-          f"drift std {np.std(y):.4f} residual std {net.residual_std:.4f} safety {net.safety:.4f}")
-    assert all(s["status"] == T.SYS_DONE for s in learned)
+    net, loss = fit(x, y, seed=0, epochs=40, groups=grp)
+    evald = [bodies.config_disk("ensemble_member", seed=s, n=512) for s in range(65, 73)]
+
+    def timed(proposer):
+        e = Ensemble(evald, bodies.thresholds(collision_factor=0.0))
+        e.set_integrator(0.001, 1e-10)
+        e.set_options(gravity_mode=T.GRAVITY_MIXED, hill_factor=0.0)
+        if proposer is not None:
+            proposer.attach(e)
+        e.advance(2.0 * T.YEAR)  # warm-up: the network needs a few steps of history
+        E0 = [e.energy(s)[0] for s in range(len(evald))]
+        st0 = [e.stats(s) for s in range(len(evald))]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e.advance(12.0 * T.YEAR)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        st = [e.stats(s) for s in range(len(evald))]
+        years = sum(a["t_day"] - b["t_day"] for a, b in zip(st, st0)) / T.YEAR
+        dE = max(abs((e.energy(s)[0] - E0[s]) / E0[s]) for s in range(len(evald)))
+        att = sum(a["n_tried_step"] - b["n_tried_step"] for a, b in zip(st, st0))
+        return years / secs, att, dE, st
+
+    timed(None)  # first use of this shape: graph capture, caches
+    rate_plain, att_plain, dE_plain, _ = timed(None)
+    rate_learned, att_learned, dE_learned, st_l = timed(net)
+    print(f"sim-yr/s plain {rate_plain:.1f} learned {rate_learned:.1f} ({rate_learned / rate_plain:.3f}x); attempts "
+          f"{att_plain} vs {att_learned} ({att_plain / att_learned:.3f}x); dE/E {dE_plain:.2e} vs {dE_learned:.2e}; "
+          f"train loss {loss:.2e}; residual std {net.residual_std:.4f}; safety {net.safety:.4f}")
+    assert all(s["status"] == T.SYS_DONE for s in st_l)
     assert dE_learned <= 1e-10
     assert att_learned < att_plain
-    assert sum(s["n_proposed"] for s in learned) > 0
+    assert rate_learned > rate_plain
+    assert sum(s["n_proposed"] for s in st_l) > 0
