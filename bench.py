@@ -576,6 +576,38 @@ def _compare_events(a, b, n_disks):
             "differing_records": diffs[:40]}
 
 
+def ensemble_attempts(args):
+    """Profiling aid: the benchmark ensemble (`--ensemble-disks` disks) in one form, attempts
+    launched directly rather than from the graph (so that a profiler sees every kernel), with
+    the device time of each kernel class.  A proposer form uses an untrained network (its
+    launches and their cost are those of a trained one)."""
+    from redgb.ensemble import Ensemble
+    from redgb.proposer import Proposer
+
+    thr = bodies.thresholds(ejection=100.0, hit_centrum=0.05, collision_factor=1.0)
+    disks = [bodies.config_disk("ensemble_member", seed=s) for s in range(65, 65 + args.ensemble_disks)]
+    e = Ensemble(disks, thr)
+    e.set_integrator(0.001, 1e-10)
+    e.set_options(gravity_mode=T.GRAVITY_FP64 if args.ensemble_form == "fp64" else T.GRAVITY_MIXED, hill_factor=3.0,
+                  use_graph=False)
+    net = None
+    if args.ensemble_form == "learned":
+        net = Proposer(seed=0)
+        net.set_normalisation([0.0] * 8, [1.0] * 8)
+        net.attach(e, safety=0.98)
+    e.advance(1e9, max_attempts=args.ensemble_attempts)
+    e.set_profiling(True)
+    e.profile()
+    e.advance(1e9, max_attempts=args.ensemble_attempts)
+    p = e.profile()
+    e.close()
+    k = args.ensemble_attempts
+    return {"form": args.ensemble_form, "disks": len(disks), "bodies": int(sum(d.n_total for d in disks)),
+            "attempts": k, "ms_per_attempt": (p["gravity_ms"] + p["stage_ms"] + p["other_ms"]) / k,
+            "gravity_ms_per_attempt": p["gravity_ms"] / k, "stage_ms_per_attempt": p["stage_ms"] / k,
+            "other_ms_per_attempt": p["other_ms"] / k}
+
+
 def ensemble_section(args):
     """The batched / mixed / learned forms against the plain FP64 form (module docstring)."""
     import torch
@@ -783,6 +815,12 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch shapes")
     ap.add_argument("--only-ensemble", action="store_true", help="the ensemble section alone (profiling)")
     ap.add_argument("--only-dense-ring", action="store_true", help="the dense-ring section alone (profiling)")
+    ap.add_argument("--only-planetesimal-disk", action="store_true",
+                    help="the planetesimal-disk section alone (profiling; see --c0-years)")
+    ap.add_argument("--ensemble-attempts", type=int, default=0,
+                    help="profiling: the ensemble's attempts launched directly (no graph), after as many "
+                         "warm-up attempts, in the form --ensemble-form; prints their device times")
+    ap.add_argument("--ensemble-form", default="mixed", choices=["mixed", "learned", "fp64"])
     ap.add_argument("--ensemble-disks", type=int, default=256)
     ap.add_argument("--ensemble-years", type=float, default=10.0)
     ap.add_argument("--train-years", type=float, default=450.0,
@@ -803,6 +841,12 @@ def main():
         return
     if args.only_dense_ring:
         print(json.dumps({"dense_ring": dense_ring_section(args)}))
+        return
+    if args.only_planetesimal_disk:
+        print(json.dumps({"planetesimal_disk": planetesimal_disk_section(args)}))
+        return
+    if args.ensemble_attempts > 0:
+        print(json.dumps({"ensemble_attempts": ensemble_attempts(args)}))
         return
     if args.impl == "reference":
         rank, ws = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))

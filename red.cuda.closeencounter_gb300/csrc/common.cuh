@@ -114,4 +114,6 @@ __device__ __forceinline__ uint32_t record_seq(const GravArgs& g, const Tile& t,
 
 namespace redgb {
 int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+// GB300's SM count, for launch-shape choices only (no correctness depends on it)
+constexpr int NUM_SMS_HINT = 152;
 }

@@ -411,7 +411,10 @@ void build_tiles(rg_ctx* c)
             continue;
         }
         if (b.src1 <= c->rowseq_max_src) {  // few sources: thread per sink (same tiles in both modes)
-            add_group(0, GROUP_ROWSEQ, b.s0, b.s1, b.src1, b.block, 128);
+            // tiles of up to 128 sinks; narrower ones when that leaves SMs idle (a thread's few
+            // serial pair terms are latency-bound, so more SMs beat fuller CTAs)
+            const int rs_step = ns >= 2 * 128 * c->n_sm ? 128 : (ns >= 2 * 64 * c->n_sm ? 64 : 32);
+            add_group(0, GROUP_ROWSEQ, b.s0, b.s1, b.src1, b.block, rs_step);
             c->plan[1].push_back(c->plan[0].back());
             c->plan[1].back().kind = GROUP_DF_ROWSEQ;
             continue;

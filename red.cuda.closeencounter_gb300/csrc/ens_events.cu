@@ -176,41 +176,53 @@ __device__ void log_hill(const EnsEventArgs& a, int s, int b, const DevEvent& d,
         atomicOr(a.flags, ENS_FLAG_HILL_SET);
 }
 
-__global__ void ens_hill_kernel(EnsEventArgs a)
+// one CTA per disk: its threads scan the step start's Hill records together and gather the
+// disk's (at most HILL_LOCAL of them; a disk with more repeats the scan for the rest, one
+// record at a time), then one thread logs them in (sink, source) order
+constexpr int HILL_THREADS = 64;
+
+__global__ void __launch_bounds__(HILL_THREADS) ens_hill_kernel(EnsEventArgs a)
 {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= a.n_sys || !a.active_f0[s]) return;
+    const int s = blockIdx.x;
+    if (!a.active_f0[s]) return;  // uniform over the CTA
+    __shared__ long long key[HILL_LOCAL];
+    __shared__ unsigned int idx[HILL_LOCAL];
+    __shared__ int m_sh;
+    if (threadIdx.x == 0) m_sh = 0;
+    __syncthreads();
     const unsigned int n = min(*a.hill_count, a.ev_cap);
+    for (unsigned int k = threadIdx.x; k < n; k += HILL_THREADS) {
+        const DevEvent& d = a.hill[k];
+        if (d.sys != s || d.kind != 1) continue;
+        const int p = atomicAdd(&m_sh, 1);
+        if (p < HILL_LOCAL) {
+            key[p] = ((long long)d.i << 32) | (long long)(unsigned int)d.j;
+            idx[p] = k;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    const int m = m_sh;
     const int b = a.base[s];
     const int cur = a.hill_which[s];
     const long long* prev = a.hill_set + ((long long)s * 2 + cur) * a.hill_set_cap;
     long long* next = a.hill_set + ((long long)s * 2 + (cur ^ 1)) * a.hill_set_cap;
     const int n_prev = a.hill_n[s];
     int n_next = 0;
-    // this disk's records in (sink, source) order: one pass gathers them (insertion-sorted by
-    // key); a disk with more than HILL_LOCAL records repeats the scan for the rest
-    long long key[HILL_LOCAL];
-    unsigned int idx[HILL_LOCAL];
-    int m = 0;
-    bool more = false;
-    for (unsigned int k = 0; k < n; k++) {
-        const DevEvent& d = a.hill[k];
-        if (d.sys != s || d.kind != 1) continue;
-        if (m == HILL_LOCAL) {
-            more = true;
-            break;
+    if (m <= HILL_LOCAL) {
+        // the gathered records in (sink, source) order (the keys are distinct)
+        for (int q = 1; q < m; q++) {
+            const long long kk = key[q];
+            const unsigned int kx = idx[q];
+            int p = q;
+            while (p > 0 && key[p - 1] > kk) {
+                key[p] = key[p - 1];
+                idx[p] = idx[p - 1];
+                p--;
+            }
+            key[p] = kk;
+            idx[p] = kx;
         }
-        const long long kk = ((long long)d.i << 32) | (long long)(unsigned int)d.j;
-        int p = m++;
-        while (p > 0 && key[p - 1] > kk) {
-            key[p] = key[p - 1];
-            idx[p] = idx[p - 1];
-            p--;
-        }
-        key[p] = kk;
-        idx[p] = k;
-    }
-    if (!more) {
         for (int q = 0; q < m; q++) log_hill(a, s, b, a.hill[idx[q]], prev, n_prev, next, n_next);
     } else {
         // repeatedly the smallest key above the last
@@ -396,7 +408,8 @@ __global__ void ens_loop_kernel(EnsLoopArgs a)
 
 int launch_ens_hill(const EnsEventArgs& a, cudaStream_t st)
 {
-    ens_hill_kernel<<<(a.n_sys + 63) / 64, 64, 0, st>>>(a);
+    if (a.n_sys <= 0) return 0;
+    ens_hill_kernel<<<a.n_sys, HILL_THREADS, 0, st>>>(a);
     RG_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

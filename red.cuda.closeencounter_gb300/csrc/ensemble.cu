@@ -368,6 +368,7 @@ __global__ void ens_finalize_kernel(EnsSys s)
 // logarithms fed to an FP32 network).  FP64 values become FP32 on their bit patterns
 // (split_bits, integer operations): a hardware conversion runs on GB300's FP64 pipe.
 constexpr int FEAT_MAX_SI = 16;  // self-interacting bodies per disk staged in shared memory
+constexpr unsigned int FEAT_H3_NONE_BITS = 0x7f61b1e6u;  // 3e38f: no pair seen
 
 __device__ __forceinline__ float to_f32(double v)
 {
@@ -378,17 +379,23 @@ __device__ __forceinline__ float to_f32(double v)
 
 // one body's contribution; si: the disk's first FEAT_MAX_SI SI bodies (positions relative to
 // body 0, masses, distance from body 0) in shared memory, ns of them in all (the rest are read
-// from the state rows), M = body 0's mass
+// from the state rows), M = body 0's mass.  The body's values are loaded before any test, so
+// that the loads of consecutive bodies overlap.
 __device__ __forceinline__ void body_features(const double* y, const double* k0, const double* mass, const int* id,
                                               long long stride, int b, int ns, const float4* si, const float* si_r,
                                               float x0, float y0, float z0, float M, int i, float& am, float& h3)
 {
-    if (id[i] <= 0) return;
-    const float ax = to_f32(k0[3LL * stride + i]), ay = to_f32(k0[4LL * stride + i]), az = to_f32(k0[5LL * stride + i]);
+    const int idi = id[i];
+    const double kx = k0[3LL * stride + i], ky = k0[4LL * stride + i], kz = k0[5LL * stride + i];
+    const double px = y[i], py = y[stride + i], pz = y[2LL * stride + i];
+    const double pm = mass[i];
+    if (idi <= 0) return;
+    const float ax = to_f32(kx), ay = to_f32(ky), az = to_f32(kz);
     am = fmaxf(am, sqrtf(ax * ax + ay * ay + az * az));
-    const float xi = to_f32(y[i]) - x0, yi = to_f32(y[stride + i]) - y0, zi = to_f32(y[2LL * stride + i]) - z0;
+    const float xi = to_f32(px) - x0, yi = to_f32(py) - y0, zi = to_f32(pz) - z0;
     const float ri = sqrtf(xi * xi + yi * yi + zi * zi);
-    const float mi = to_f32(mass[i]);
+    const float mi = to_f32(pm);
+    const float inv3M = 1.0f / (3.0f * M);
     for (int q = 1; q < ns; q++) {
         const int j = b + q;
         float4 sj;
@@ -405,13 +412,16 @@ __device__ __forceinline__ void body_features(const double* y, const double* k0,
         const float dx = sj.x - xi, dy = sj.y - yi, dz = sj.z - zi;
         const float d2 = dx * dx + dy * dy + dz * dz;
         const float hh = 0.5f * (ri + rj);
-        const float rh3 = (mi + sj.w) / (3.0f * M) * hh * hh * hh;
+        const float rh3 = (mi + sj.w) * inv3M * hh * hh * hh;
         if (rh3 > 0.0f) h3 = fminf(h3, d2 * sqrtf(d2) / rh3);
     }
 }
 
 struct PropArgs {
     EnsSys s;
+    const StageTile* tiles;  // the stage tiles (a disk's tiles are consecutive)
+    const int* tiles_of;     // per disk: its stage tiles
+    unsigned int* red;       // per disk: max |a| bits, min h3 bits, tiles done (reset by the last)
     const double* y;
     const double* k0;
     const double* mass;
@@ -435,19 +445,30 @@ __device__ __forceinline__ double dither_uniform(unsigned long long seed, int d,
     return (double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0;
 }
 
-// one CTA per disk that starts a step: features (a pass over the disk's bodies, block
-// reductions), then in the first warp the network and the trial step
-__global__ void __launch_bounds__(256) ens_propose_kernel(PropArgs a)
+// one CTA per stage tile of the disks that start a step: the tile's feature partials (max |a|,
+// min (d / mutual Hill radius)^3) go to the disk's slots by atomics; the disk's last tile to
+// finish (a ticket per disk, no waiting) takes the disk's features, resets the slots for the
+// next launch, and in its first warp evaluates the network and sets the trial step.  That CTA
+// stages the network's weights in shared memory first (as float, W2 transposed so that the
+// lanes of a warp read consecutive words).
+constexpr int PROP_THREADS = 256;
+
+__global__ void __launch_bounds__(PROP_THREADS) ens_propose_kernel(PropArgs a)
 {
-    const int d = blockIdx.x;
+    const StageTile tile = a.tiles[blockIdx.x];
+    const int d = tile.sys;
     const EnsSys& s = a.s;
-    if (!s.active_f0[d]) return;
-    __shared__ float red_am[8], red_h3[8];
+    if (!s.active_f0[d]) return;  // uniform over the CTA
+    __shared__ float red_am[PROP_THREADS / 32], red_h3[PROP_THREADS / 32];
     __shared__ float4 si[FEAT_MAX_SI];
     __shared__ float si_r[FEAT_MAX_SI];
+    __shared__ float sw1[MLP_HIDDEN * MLP_IN], sb1[MLP_HIDDEN], sw2t[MLP_HIDDEN * MLP_HIDDEN], sb2[MLP_HIDDEN],
+        sw3[MLP_HIDDEN];
+    __shared__ int last_sh;
+    __shared__ float feat_sh[2];
     float am = 0.0f, h3 = 3.0e38f;
     {
-        const int b = a.base[d], n = a.ntot[d], ns = a.nsi[d];
+        const int b = a.base[d], ns = a.nsi[d];
         const float x0 = to_f32(a.y[b]), y0 = to_f32(a.y[a.stride + b]), z0 = to_f32(a.y[2LL * a.stride + b]);
         const float M = to_f32(a.mass[b]);
         if ((int)threadIdx.x < min(ns, FEAT_MAX_SI)) {
@@ -457,7 +478,8 @@ __global__ void __launch_bounds__(256) ens_propose_kernel(PropArgs a)
             si_r[threadIdx.x] = sqrtf(xj * xj + yj * yj + zj * zj);
         }
         __syncthreads();
-        for (int i = b + threadIdx.x; i < b + n; i += blockDim.x)
+#pragma unroll 2
+        for (int i = tile.b0 + threadIdx.x; i < tile.b1; i += blockDim.x)
             body_features(a.y, a.k0, a.mass, a.id, a.stride, b, ns, si, si_r, x0, y0, z0, M, i, am, h3);
         for (int off = 16; off > 0; off >>= 1) {
             am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, off));
@@ -468,27 +490,59 @@ __global__ void __launch_bounds__(256) ens_propose_kernel(PropArgs a)
             red_h3[threadIdx.x >> 5] = h3;
         }
         __syncthreads();
-        if (threadIdx.x >= 32) return;
-        am = threadIdx.x < (blockDim.x >> 5) ? red_am[threadIdx.x] : 0.0f;
-        h3 = threadIdx.x < (blockDim.x >> 5) ? red_h3[threadIdx.x] : 3.0e38f;
-        for (int off = 16; off > 0; off >>= 1) {
-            am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, off));
-            h3 = fminf(h3, __shfl_xor_sync(0xffffffffu, h3, off));
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < PROP_THREADS / 32; w++) {
+                am = fmaxf(am, red_am[w]);
+                h3 = fminf(h3, red_h3[w]);
+            }
+            // non-negative floats order as their bit patterns
+            unsigned int* r = a.red + 3 * d;
+            atomicMax(r, __float_as_uint(am));
+            atomicMin(r + 1, __float_as_uint(h3));
+            __threadfence();
+            const unsigned int done = atomicAdd(r + 2, 1u);
+            last_sh = done + 1 == (unsigned int)a.tiles_of[d];
+            if (last_sh) {
+                __threadfence();
+                feat_sh[0] = __uint_as_float(atomicExch(r, 0u));
+                feat_sh[1] = __uint_as_float(atomicExch(r + 1, FEAT_H3_NONE_BITS));
+                atomicExch(r + 2, 0u);
+            }
         }
+        __syncthreads();
+        if (!last_sh) return;
+        am = feat_sh[0];
+        h3 = feat_sh[1];
     }
+    const bool use_net = a.w && !(s.cool[d] > 0 || s.n_passed[d] < 4 || !(s.ideal_last[d] > 0.0));
+    if (use_net) {
+        for (int k = threadIdx.x; k < MLP_HIDDEN * MLP_HIDDEN; k += blockDim.x) {
+            const int u = k / MLP_HIDDEN, v = k % MLP_HIDDEN;  // W2[u][v] -> sw2t[v][u]
+            sw2t[v * MLP_HIDDEN + u] = __bfloat162float(a.w[MLP_OFF_W2 + k]);
+        }
+        for (int k = threadIdx.x; k < MLP_HIDDEN * MLP_IN; k += blockDim.x)
+            sw1[k] = __bfloat162float(a.w[MLP_OFF_W1 + k]);
+        for (int k = threadIdx.x; k < MLP_HIDDEN; k += blockDim.x) {
+            sb1[k] = __bfloat162float(a.w[MLP_OFF_B1 + k]);
+            sb2[k] = __bfloat162float(a.w[MLP_OFF_B2 + k]);
+            sw3[k] = __bfloat162float(a.w[MLP_OFF_W3 + k]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x >= 32) return;
     const int lane = threadIdx.x & 31;
     const float* h = s.hist + 5 * d;
     float f[8];
     f[0] = h3 < 1.0e38f ? log10f(fmaxf(h3, 1e-30f)) / 3.0f : 6.0f;
     f[1] = log10f(fmaxf(am, 1e-30f));
-    f[2] = s.dt_last[d] > 0.0 ? (float)log10(s.dt_last[d] / 1.720209895e-2) : -3.0f;
+    f[2] = s.dt_last[d] > 0.0 ? log10f(to_f32(s.dt_last[d]) * (1.0f / 1.720209895e-2f)) : -3.0f;
     f[3] = h[0];
     f[4] = h[1];
     f[5] = h[2];
     f[6] = h[3];
     f[7] = h[4];
     if (lane < 8) s.feat[8 * d + lane] = f[lane];
-    if (!a.w || s.cool[d] > 0 || s.n_passed[d] < 4 || !(s.ideal_last[d] > 0.0)) {
+    if (!use_net) {
         if (lane == 0 && s.dither > 0.0f)
             s.dt_try[d] *= exp((double)s.dither * dither_uniform(s.dither_seed, d, s.n_passed[d]));
         return;
@@ -501,30 +555,31 @@ __global__ void __launch_bounds__(256) ens_propose_kernel(PropArgs a)
 #pragma unroll
     for (int r = 0; r < 2; r++) {
         const int u = lane + 32 * r;
-        float z = __bfloat162float(a.w[MLP_OFF_B1 + u]);
+        float z = sb1[u];
 #pragma unroll
-        for (int q = 0; q < 8; q++) z = fmaf(__bfloat162float(a.w[MLP_OFF_W1 + u * 8 + q]), x[q], z);
+        for (int q = 0; q < 8; q++) z = fmaf(sw1[u * 8 + q], x[q], z);
         h1[r] = z / (1.0f + __expf(-z));
     }
     float h2[2];
 #pragma unroll
     for (int r = 0; r < 2; r++) {
         const int u = lane + 32 * r;
-        float z = __bfloat162float(a.w[MLP_OFF_B2 + u]);
+        float z = sb2[u];
+#pragma unroll 16
         for (int v = 0; v < 64; v++) {
             const float hv = __shfl_sync(0xffffffffu, h1[v >> 5], v & 31);
-            z = fmaf(__bfloat162float(a.w[MLP_OFF_W2 + u * 64 + v]), hv, z);
+            z = fmaf(sw2t[v * MLP_HIDDEN + u], hv, z);
         }
         h2[r] = z / (1.0f + __expf(-z));
     }
-    float o = __bfloat162float(a.w[MLP_OFF_W3 + lane]) * h2[0] + __bfloat162float(a.w[MLP_OFF_W3 + lane + 32]) * h2[1];
+    float o = sw3[lane] * h2[0] + sw3[lane + 32] * h2[1];
     for (int off = 16; off > 0; off >>= 1) o += __shfl_xor_sync(0xffffffffu, o, off);
     o += __bfloat162float(a.w[MLP_OFF_B3]);
     if (lane == 0 && isfinite(o)) {
         // the network predicts log(ideal step / last ideal step); the plain controller bounds
         // the proposal to [1/2, 2] of its own estimate
         const double plain = s.dt_try[d];
-        double dt = (double)a.safety * s.ideal_last[d] * exp((double)o);
+        double dt = (double)a.safety * s.ideal_last[d] * (double)expf(o);
         dt = fmin(fmax(dt, 0.5 * plain), 2.0 * plain);
         if (isfinite(dt) && dt > 0.0) {
             s.dt_try[d] = dt;
@@ -623,6 +678,10 @@ struct rg_ens {
     // stage tiles
     std::vector<StageTile> stiles;
     StageTile* d_stiles = nullptr;
+    std::vector<int> tiles_of;      // per disk: its stage tiles
+    int* d_tiles_of = nullptr;
+    unsigned int* d_feat_red = nullptr;  // per disk: max |a| bits, min h3 bits, tiles done
+    std::vector<unsigned int> feat_red_init;
     // gravity plan
     struct Group {
         int kind;
@@ -764,7 +823,7 @@ void free_all(rg_ens* e)
                     e->d_kerr, e->d_rf, e->d_smax, e->d_screen_slot, e->d_prm,
                     e->d_f_rad, e->d_base, e->d_ntot, e->d_nsi, e->d_hill_set, e->d_hill_n, e->d_hill_which,
                     e->d_elog, e->d_elog_count, e->d_elog_seq, e->d_flags, e->d_hit_slots, e->d_keep,
-                    e->d_attempts};
+                    e->d_attempts, e->d_tiles_of, e->d_feat_red};
     for (void* q : ptrs) cudaFree(q);
     for (auto& k : e->d_k) cudaFree(k);
     if (e->st) cudaStreamDestroy(e->st);
@@ -802,12 +861,14 @@ void prof_end(rg_ens* e, long idx)
 void build_stage_tiles(rg_ens* e)
 {
     e->stiles.clear();
+    e->tiles_of.assign(e->n_sys, 0);
     for (int s = 0; s < e->n_sys; s++) {
         const int b = e->base[s], n = e->ntot[s];
         const int nerr = e->ectp ? n : e->n_massive(s);
         for (int o = 0; o < n; o += STAGE_TILE) {
             const int b0 = b + o, b1 = b + std::min(n, o + STAGE_TILE);
             e->stiles.push_back(StageTile{s, b0, b1, std::max(b0, std::min(b1, b + nerr))});
+            e->tiles_of[s]++;
         }
     }
 }
@@ -909,11 +970,14 @@ int upload_plans(rg_ens* e)
     cudaFree(e->d_row_nsrc);
     cudaFree(e->d_row_sys);
     cudaFree(e->d_terms);
+    cudaFree(e->d_tiles_of);
     e->d_stiles = nullptr;
+    e->d_tiles_of = nullptr;
     e->d_tiles = nullptr;
     e->d_heavy = e->d_few_row0 = e->d_row_sink = e->d_row_nsrc = e->d_row_sys = nullptr;
     e->d_terms = nullptr;
     chk(dalloc(&e->d_stiles, e->stiles.size()));
+    chk(dalloc(&e->d_tiles_of, e->tiles_of.size()));
     chk(dalloc(&e->d_tiles, nt));
     chk(dalloc(&e->d_heavy, nt));
     chk(dalloc(&e->d_few_row0, nt));
@@ -929,6 +993,7 @@ int upload_plans(rg_ens* e)
         }
     };
     up(e->d_stiles, e->stiles.data(), e->stiles.size() * sizeof(StageTile));
+    up(e->d_tiles_of, e->tiles_of.data(), e->tiles_of.size() * sizeof(int));
     up(e->d_tiles, e->tiles.data(), nt * sizeof(Tile));
     up(e->d_heavy, e->heavy.data(), nt * sizeof(int));
     up(e->d_screen_slot, e->screen_slot.data(), e->screen_slot.size() * sizeof(int));
@@ -1225,7 +1290,10 @@ int record_attempt(rg_ens* e, bool in_graph)
             pa.inv_std[q] = e->mlp_inv_std[q];
         }
         pa.safety = e->safety;
-        ens_propose_kernel<<<e->n_sys, 256, 0, e->st>>>(pa);
+        pa.tiles = e->d_stiles;
+        pa.tiles_of = e->d_tiles_of;
+        pa.red = e->d_feat_red;
+        ens_propose_kernel<<<(int)e->stiles.size(), PROP_THREADS, 0, e->st>>>(pa);
         RG_CUDA_CHECK(cudaGetLastError());
         e->n_kernels += 1;
     }
@@ -1424,6 +1492,7 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     chk(dalloc(&e->d_acc_attempt, ns));
     chk(dalloc(&e->d_nf0, ns));
     chk(dalloc(&e->d_feat, 8 * ns));
+    chk(dalloc(&e->d_feat_red, 3 * ns));
     chk(dalloc(&e->d_dt_last, ns));
     chk(dalloc(&e->d_ideal_last, ns));
     chk(dalloc(&e->d_hist, 5 * ns));
@@ -1517,6 +1586,9 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
         std::vector<float> zf(8 * ns, 0.0f), zh(5 * ns, 0.0f);
         chk(upload(e, e->d_feat, zf));
         chk(upload(e, e->d_hist, zh));
+        e->feat_red_init.assign(3 * ns, 0u);
+        for (int d = 0; d < ns; d++) e->feat_red_init[3 * d + 1] = FEAT_H3_NONE_BITS;
+        chk(upload(e, e->d_feat_red, e->feat_red_init));
     }
     chk(upload(e, e->d_thr, e->thr));
     chk(upload(e, e->d_prm, e->p));

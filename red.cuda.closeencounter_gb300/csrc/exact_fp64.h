@@ -230,6 +230,74 @@ XF_HD bool sqrt_rn_fast(double x, double* out)
     return true;
 }
 
+// ---------------------------------------------------------------------------------------
+// Serial sums.  Inside one binade [2^(ea-1023), 2^(ea-1022)) the doubles are the multiples of
+// the quantum Q = 2^(ea-1075), so while a running sum acc stays in its binade, the correctly
+// rounded acc + t is acc + (t rounded to a multiple of Q) -- ties to even, where a tie is a t
+// at an odd multiple of Q/2.  The terms of a serial FP64 sum can therefore be rounded to
+// quanta independently and added as integers, which is exact and associative, as long as
+// every running sum stays strictly inside the binade and no term is a tie; the first term
+// that breaks this is added by the FP64 pipe and the binade is taken afresh.
+
+// t / Q rounded to the nearest integer, for the quantum Q = 2^(ea - 1075) of the binade with
+// biased exponent ea (1..2046); false for a tie, a subnormal, an infinite or NaN t, or a t of
+// 2^5 binades or more above the accumulator's (|r| then stays below 2^58, so 32 of them add
+// without overflow).
+XF_HD bool quantize(double t, int ea, int64_t* r)
+{
+    const uint64_t ut = dbits(t);
+    const int et = (int)((ut >> 52) & 0x7ff);
+    const uint64_t mant = ut & M52;
+    if (et == 0) {
+        if (mant != 0) return false;  // subnormal
+        *r = 0;                        // +-0 adds nothing to a nonzero accumulator
+        return true;
+    }
+    if (et == 2047) return false;
+    const uint64_t M = mant | H52;
+    const int sh = et - ea;
+    uint64_t mag;
+    if (sh >= 0) {
+        if (sh > 4) return false;
+        mag = M << sh;
+    } else if (-sh >= 64) {
+        mag = 0;  // |t| < 2^-11 Q
+    } else {
+        const int k = -sh;
+        const uint64_t q0 = M >> k;
+        const uint64_t rem = M - (q0 << k);
+        const uint64_t half = 1ull << (k - 1);
+        if (rem == half) return false;  // a tie: the result's parity decides
+        mag = q0 + (rem > half ? 1u : 0u);
+    }
+    *r = (ut >> 63) ? -(int64_t)mag : (int64_t)mag;
+    return true;
+}
+
+// the accumulator's signed significand in quanta of its own binade (2^52 <= |A| < 2^53)
+XF_HD int64_t quanta_of(double acc)
+{
+    const uint64_t ua = dbits(acc);
+    const int64_t A = (int64_t)((ua & M52) | H52);
+    return (ua >> 63) ? -A : A;
+}
+
+// S quanta of the binade ea (2^52 < |S| < 2^53) as a double
+XF_HD double from_quanta(int64_t S, int ea)
+{
+    const uint64_t sign = S < 0 ? (1ull << 63) : 0ull;
+    const uint64_t mag = S < 0 ? (uint64_t)(-S) : (uint64_t)S;
+    return bitsd(sign | ((uint64_t)ea << 52) | (mag & M52));
+}
+
+// whether S quanta (a running sum of an accumulator with significand A quanta) lies strictly
+// inside the binade, on A's side of zero: then the rounded sum is the binade's S Q, and the
+// exact sum, within Q/2 of it, lies inside the binade too
+XF_HD bool inside_binade(int64_t A, int64_t S)
+{
+    return A > 0 ? (S > (int64_t)H52 && S < (int64_t)(H52 << 1)) : (S < -(int64_t)H52 && S > -(int64_t)(H52 << 1));
+}
+
 }  // namespace xf
 }  // namespace redgb
 
@@ -248,6 +316,59 @@ __device__ __forceinline__ double rn_div(double a, double b)
 {
     double r;
     return xf::div_rn_fast(a, b, &r) ? r : __ddiv_rn(a, b);
+}
+
+// acc + t_0 + t_1 + ... + t_(m-1), rounded to nearest after every addition in that order --
+// the bits of the serial FP64 loop -- computed by the 32 lanes of a warp together: lane k
+// holds t_k (m <= 32; every lane of the warp calls this with the same acc and m).  The terms
+// are rounded to quanta of the accumulator's binade in parallel and added by a warp prefix sum
+// (xf::quantize); the first term whose running sum leaves the binade, or that is a tie or
+// special, is added by the FP64 pipe together with the next SERIAL_BURST - 1 terms (where one
+// term leaves the binade, its neighbours often do too: a sum crossing zero), and the rest of
+// the round starts again after them.  Each pass consumes at least one term, so the loop ends
+// after at most m passes; in a typical gravity row (a few large terms, then many small ones)
+// one pass takes all 32.  The latency of a pass is a few integer operations, five shuffles and
+// a ballot, against 32 dependent FP64 additions of the serial loop.
+constexpr int SERIAL_BURST = 4;
+
+__device__ __forceinline__ double warp_serial_sum(double acc, double tk, int m)
+{
+    const int lane = threadIdx.x & 31;
+    int pos = 0;
+    while (pos < m) {
+        const int ea = (int)((xf::dbits(acc) >> 52) & 0x7ff);
+        if (ea != 0 && ea != 2047) {
+            int64_t r = 0;
+            bool ok = true;
+            const bool mine = lane >= pos && lane < m;
+            if (mine) ok = xf::quantize(tk, ea, &r);
+            if (!ok) r = 0;
+            int64_t P = r;  // inclusive prefix over the lanes
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const long long o = __shfl_up_sync(0xffffffffu, (long long)P, off);
+                if (lane >= off) P += o;
+            }
+            const int64_t A = xf::quanta_of(acc);
+            const int64_t S = A + P;
+            const unsigned bad = __ballot_sync(0xffffffffu, mine && !(ok && xf::inside_binade(A, S)));
+            const int stop = bad ? __ffs(bad) - 1 : m;
+            if (stop > pos) {
+                const long long Sc = __shfl_sync(0xffffffffu, (long long)S, stop - 1);
+                acc = xf::from_quanta(Sc, ea);
+                pos = stop;
+            }
+            if (pos >= m) break;
+        }
+        double tp[SERIAL_BURST];
+#pragma unroll
+        for (int k = 0; k < SERIAL_BURST; k++) tp[k] = __shfl_sync(0xffffffffu, tk, min(pos + k, 31));
+#pragma unroll
+        for (int k = 0; k < SERIAL_BURST; k++)
+            if (pos + k < m) acc = __dadd_rn(acc, tp[k]);
+        pos += SERIAL_BURST;
+    }
+    return acc;
 }
 
 }  // namespace redgb

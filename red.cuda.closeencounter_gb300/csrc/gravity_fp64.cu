@@ -232,7 +232,7 @@ __global__ void star_distance(const double* __restrict__ x, const double* __rest
     if (i >= n) return;
     const int b = base_of ? base_of[i] : 0;
     const double dx = x[i] - x[b], dy = y[i] - y[b], dz = z[i] - z[b];
-    rho[i] = sqrt(dx * dx + dy * dy + dz * dz);
+    rho[i] = rn_sqrt(dx * dx + dy * dy + dz * dz);  // sqrt.rn's bits, off the FP64 pipe
 }
 
 // ---------------------------------------------------------------------------------------
@@ -304,8 +304,10 @@ struct FewSumArgs {
 };
 
 // exact: one warp per (row, component).  The warp streams the row through shared memory
-// in coalesced chunks (the next chunk's loads are in flight while lane 0 adds the current
-// one) and lane 0 adds the terms in ascending source order -- the reference's serial sum.
+// in coalesced chunks (the next chunk's loads are in flight while the current one is added)
+// and adds the terms in ascending source order with the bits of the reference's serial sum:
+// warp_serial_sum (exact_fp64.h) takes 32 terms per pass on the integer pipes, where a chain
+// of dependent FP64 additions would wait on GB300's FP64 latency for each term.
 constexpr int SUM_CHUNK = 256;
 
 __global__ void __launch_bounds__(128) few_sum_serial(FewSumArgs a)
@@ -335,16 +337,10 @@ __global__ void __launch_bounds__(128) few_sum_serial(FewSumArgs a)
         for (int k = 0; k < SUM_CHUNK / 32; k++) B[cur][k * 32 + lane] = reg[k];
         __syncwarp();
         if (c0 + SUM_CHUNK < n) load(c0 + SUM_CHUNK);
-        if (lane == 0) {
-            const int m = min(SUM_CHUNK, n - c0);
-            int q = 0;
-            for (; q + 8 <= m; q += 8) {
-                const double t0 = B[cur][q], t1 = B[cur][q + 1], t2 = B[cur][q + 2], t3 = B[cur][q + 3];
-                const double t4 = B[cur][q + 4], t5 = B[cur][q + 5], t6 = B[cur][q + 6], t7 = B[cur][q + 7];
-                acc = acc + t0; acc = acc + t1; acc = acc + t2; acc = acc + t3;
-                acc = acc + t4; acc = acc + t5; acc = acc + t6; acc = acc + t7;
-            }
-            for (; q < m; q++) acc = acc + B[cur][q];
+        const int m = min(SUM_CHUNK, n - c0);
+        for (int b = 0; b < m; b += 32) {
+            const int mb = min(32, m - b);
+            acc = warp_serial_sum(acc, lane < mb ? B[cur][b + lane] : 0.0, mb);
         }
         __syncwarp();
         cur ^= 1;
@@ -435,7 +431,9 @@ int launch_grav_fp64_few(const GravArgs& g, const int* tile_row0, int max_src, d
 {
     if (g.n_tiles <= 0 || rows <= 0 || group_rows <= 0 || max_src <= 0) return 0;
     FewArgs a{g, tile_row0, terms, rows, pitch};
-    grav_fp64_few_terms<<<dim3((max_src + 255) / 256, g.n_tiles), 256, 0, st>>>(a);
+    // 256 sources per CTA, or 64 when that would leave most SMs idle (one disk's few heavy rows)
+    const int nt = (long long)((max_src + 255) / 256) * g.n_tiles < 2 * NUM_SMS_HINT ? 64 : 256;
+    grav_fp64_few_terms<<<dim3((max_src + nt - 1) / nt, g.n_tiles), nt, 0, st>>>(a);
     RG_CUDA_CHECK(cudaGetLastError());
     FewSumArgs b{terms, rows, group_row0, group_rows, pitch, dev_row_sink, dev_row_nsrc, dev_row_sys, g.sys_active,
                  g.ax, g.ay, g.az};

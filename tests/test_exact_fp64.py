@@ -1,7 +1,10 @@
 """The FP64 square root and division the bit-exact gravity kernels compute on the integer
 pipes (csrc/exact_fp64.h) against IEEE 754: correctly rounded, the same bits as the host's
 sqrt and '/' (CPU, with the FP32 seeds perturbed) and as the GPU's sqrt.rn / div.rn on
-random, near-midpoint and pair-term-like operands."""
+random, near-midpoint and pair-term-like operands.  And the warp-parallel form of the serial
+FP64 sum (warp_serial_sum: terms rounded to quanta of the accumulator's binade and added as
+integers) against the plain serial loop, on gravity-like, wide, tie-rich, cancelling and
+special-value rows."""
 import os
 import re
 import shutil
@@ -44,3 +47,27 @@ def test_exact_sqrt_and_division_on_the_gpu(tmp_path):
         assert int(fast_sqrt) == int(cases)
         if fam != "0":  # family 0 draws exponents over the whole range, some quotients leave it
             assert int(fast_div) == int(cases)
+
+
+def test_exact_serial_sum_on_the_cpu(tmp_path):
+    exe = _build(tmp_path, "g++", "serial_sum_check.cpp", ["-O2", "-std=c++17", "-ffp-contract=off"])
+    r = subprocess.run([exe, "20000"], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    rows, terms, bad, fast, slow, qbad = map(int, re.search(
+        r"rows (\d+) terms (\d+) bad (\d+) fast (\d+) fallback (\d+) qbad (\d+)", r.stdout).groups())
+    assert bad == 0 and qbad == 0
+    assert terms > 7e7
+    f0 = re.search(r"family 0 fast (\d+) fallback (\d+)", r.stdout)
+    assert int(f0.group(1)) > 100 * int(f0.group(2))  # gravity-like rows take the integer path
+
+
+@pytest.mark.gpu
+def test_exact_serial_sum_on_the_gpu(tmp_path):
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    exe = _build(tmp_path, nvcc, "serial_sum_gpu.cu",
+                 ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17", "-fmad=false"])
+    r = subprocess.run([exe, "20000"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    rows = re.findall(r"family (\d) rows (\d+) bad (\d+)", r.stdout)
+    assert len(rows) == 5
+    assert all(int(bad) == 0 for _, _, bad in rows), r.stdout
