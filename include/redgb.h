@@ -224,6 +224,16 @@ RG_API int rg_calc_accel(rg_ctx* ctx, rg_vec_t* a);
  */
 RG_API int rg_autotune(rg_ctx* ctx, int reps, rg_tune_t* out);
 
+/*
+ * Sets the launch shape directly (not in the reference): `shape->pairpar_sinks` (8, 12, 16,
+ * 18, 24, 32 or 36; 8, 16 or 32 in the astrocentric frame), `rowseq_max_src` (>= 1) and
+ * `mixed_chunks` (0 = from the SM count, else a positive multiple of 256 sources); the other
+ * fields are ignored.  For a run that reuses the shape an earlier rg_autotune chose on the
+ * same kind of disk without timing the candidates again.  FP64 results do not depend on the
+ * shape.  RG_ERR_ARG for a value outside those sets.
+ */
+RG_API int rg_set_launch_shape(rg_ctx* ctx, const rg_tune_t* shape);
+
 /* Synthetic disks generated on the GPU (the seeded initial-condition generator of this
  * project; the reference's own generator is the separate red.cuda.initial program): disk s
  * gets the records [off_s, off_s + n_total_s) of r, v (AU, AU/day, heliocentric), p and md,

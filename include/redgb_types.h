@@ -142,7 +142,7 @@ typedef struct rg_mmsn_component {
 
 /* launch shape of a context's force evaluation (rg_autotune) */
 typedef struct rg_tune {
-    int32_t pairpar_sinks;   /* FP64 mode: sinks per pair-parallel CTA (8, 16 or 32)             */
+    int32_t pairpar_sinks;   /* FP64 mode: sinks per pair-parallel CTA (8, 12, 16, 18, 24, 32, 36) */
     int32_t rowseq_max_src;  /* blocks with at most this many sources use the row kernel         */
     int32_t mixed_chunks;    /* mixed mode: sources per grid.y chunk -- of the mixed kernel
                                 (rg_autotune) or the few-sink kernel (rg_ens_autotune); 0: chosen

@@ -1445,6 +1445,34 @@ int rg_device_count(void)
     return n;
 }
 
+// The default sinks per pair-parallel CTA: every CTA of the self-interacting block runs all of
+// its sources, so a launch takes (waves of resident CTAs) x (one CTA's time, proportional to
+// S); the S of the candidate set with the fewest wave-sinks, the larger S on a tie (fewer
+// barriers per pair).  16 385 sinks on 152 SMs x 3 CTAs: S = 36, one wave of 456 CTAs.
+// rg_autotune times the candidates instead.
+static int wave_best_sinks(const rg_ctx* c)
+{
+    const int ns = c->n_si() - (c->frame == RG_FRAME_ASTRO ? 1 : 0);
+    if (ns <= 0) return 16;
+    const long long slots = (long long)std::max(c->n_sm, 1) * RG_PAIRPAR_RESIDENT;
+    static const int astro_s[] = {8, 16, 32};
+    static const int bary_s[] = {8, 12, 16, 18, 24, 32, 36};
+    const int* cand = c->frame == RG_FRAME_ASTRO ? astro_s : bary_s;
+    const int nc = c->frame == RG_FRAME_ASTRO ? 3 : 7;
+    int best = 16;
+    long long best_cost = -1;
+    for (int k = 0; k < nc; k++) {
+        const int S = cand[k];
+        const long long ctas = (ns + S - 1) / S;
+        const long long cost = (ctas + slots - 1) / slots * S;
+        if (best_cost < 0 || cost < best_cost || (cost == best_cost && S > best)) {
+            best_cost = cost;
+            best = S;
+        }
+    }
+    return best;
+}
+
 static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* v, const rg_param_t* p,
                        const rg_body_metadata_t* md, const double* epoch, const double thr[RG_THRESHOLD_N],
                        int event_capacity, int frame, rg_ctx** out)
@@ -1603,6 +1631,7 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
         delete c;
         return rc;
     }
+    c->pairpar_S = wave_best_sinks(c);
     build_tiles(c);
     *out = c;
     return RG_OK;
@@ -1921,9 +1950,14 @@ static int autotune_impl(rg_ctx* c, int reps, rg_tune_t* out)
         for (int k : ks) cand.push_back({best.S, best.rowseq, k * MIXED_SOURCE_TILE});
         run(cand);
     } else {
-        const int ss[3] = {8, 16, 32};
-        for (int r : rows)
-            for (int S : ss) cand.push_back({S, r, c->mixed_chunk_src});
+        // sinks per pair-parallel CTA (the astrocentric kernel has 8, 16 and 32), then the
+        // row-kernel source limit at the best of them
+        std::vector<int> ss = {8, 16, 32};
+        if (c->frame != RG_FRAME_ASTRO) ss = {8, 12, 16, 18, 24, 32, 36};
+        for (int S : ss) cand.push_back({S, c->rowseq_max_src, c->mixed_chunk_src});
+        run(cand);
+        cand.clear();
+        for (int r : rows) cand.push_back({best.S, r, c->mixed_chunk_src});
         run(cand);
     }
     c->n_gravity_evals = evals;
@@ -1978,6 +2012,30 @@ int rg_autotune(rg_ctx* c, int reps, rg_tune_t* out)
 {
     if (!c || reps <= 0) return set_error(RG_ERR_ARG, "bad argument");
     RG_GUARD(autotune_impl(c, reps, out));
+}
+
+static int set_launch_shape_impl(rg_ctx* c, const rg_tune_t* t)
+{
+    const int S = t->pairpar_sinks;
+    const bool astro = c->frame == RG_FRAME_ASTRO;
+    const bool s_ok = astro ? (S == 8 || S == 16 || S == 32)
+                            : (S == 8 || S == 12 || S == 16 || S == 18 || S == 24 || S == 32 || S == 36);
+    if (!s_ok) return set_error(RG_ERR_ARG, "pairpar_sinks: 8, 12, 16, 18, 24, 32 or 36 (8, 16 or 32 in the "
+                                            "astrocentric frame)");
+    if (t->rowseq_max_src < 1) return set_error(RG_ERR_ARG, "rowseq_max_src must be positive");
+    if (t->mixed_chunks < 0 || t->mixed_chunks % MIXED_SOURCE_TILE != 0)
+        return set_error(RG_ERR_ARG, "mixed_chunks: 0 or a positive multiple of 256 sources");
+    c->pairpar_S = S;
+    c->rowseq_max_src = t->rowseq_max_src;
+    c->mixed_chunk_src = t->mixed_chunks;
+    build_tiles(c);
+    return RG_OK;
+}
+
+int rg_set_launch_shape(rg_ctx* c, const rg_tune_t* shape)
+{
+    if (!c || !shape) return set_error(RG_ERR_ARG, "bad argument");
+    RG_GUARD(set_launch_shape_impl(c, shape));
 }
 
 int rg_get_counters(rg_ctx* c, rg_counters_t* o)

@@ -318,56 +318,82 @@ __device__ __forceinline__ double rn_div(double a, double b)
     return xf::div_rn_fast(a, b, &r) ? r : __ddiv_rn(a, b);
 }
 
-// acc + t_0 + t_1 + ... + t_(m-1), rounded to nearest after every addition in that order --
-// the bits of the serial FP64 loop -- computed by the 32 lanes of a warp together: lane k
-// holds t_k (m <= 32; every lane of the warp calls this with the same acc and m).  The terms
-// are rounded to quanta of the accumulator's binade in parallel and added by a warp prefix sum
-// (xf::quantize); the first term whose running sum leaves the binade, or that is a tie or
-// special, is added by the FP64 pipe together with the next SERIAL_BURST - 1 terms (where one
-// term leaves the binade, its neighbours often do too: a sum crossing zero), and the rest of
-// the round starts again after them.  Each pass consumes at least one term, so the loop ends
-// after at most m passes; in a typical gravity row (a few large terms, then many small ones)
-// one pass takes all 32.  The latency of a pass is a few integer operations, five shuffles and
-// a ballot, against 32 dependent FP64 additions of the serial loop.
-constexpr int SERIAL_BURST = 4;
+// acc + T[0] + T[1] + ... + T[m-1], rounded to nearest after every addition in that order --
+// the bits of the serial FP64 loop -- computed by the 32 lanes of a warp together (m <= 32;
+// every lane of the warp calls this with the same acc, T, m and state; lane k reads T[k]).
+//
+// Fast passes: the terms are rounded to quanta of the accumulator's binade in parallel and
+// added by a warp prefix sum (xf::quantize); if the running sum stays in its binade and no
+// term is a tie or special, one pass takes all the terms -- a few integer operations, five
+// shuffles and a ballot, about 21 cycles per term on GB300 against 71 for each dependent FP64
+// addition of the serial loop.  The first term that breaks this is added by lane 0 on the
+// FP64 pipe; after a pass that took at least SERIAL_GOOD_PASS terms another pass follows,
+// otherwise lane 0 adds the rest of the round in order (one active lane: the FP64 pipe's cost
+// of a one-lane addition is small, its latency is what the serial loop pays).
+//
+// A running sum that keeps leaving its binade (a component hovering about zero, where the
+// terms cancel) makes every pass short; after such a round the next `backoff` rounds are
+// serial, the backoff going 0, 1, 2, 4, 8 while rounds keep failing that way and back to 0
+// after a round whose passes were all long.  SerialSumState holds that per chain; it starts
+// as {0, 0}.
+struct SerialSumState {
+    int skip;     // serial rounds still to do
+    int backoff;  // serial rounds after the next poor round
+};
 
-__device__ __forceinline__ double warp_serial_sum(double acc, double tk, int m)
+constexpr int SERIAL_GOOD_PASS = 8;
+
+// lane 0 adds T[from..m) in order; every lane returns the result
+__device__ __forceinline__ double serial_tail(double acc, const double* T, int from, int m)
 {
+    if ((threadIdx.x & 31) == 0)
+        for (int k = from; k < m; k++) acc = __dadd_rn(acc, T[k]);
+    return __shfl_sync(0xffffffffu, acc, 0);
+}
+
+__device__ __forceinline__ double warp_serial_sum(double acc, const double* T, int m, SerialSumState& st)
+{
+    if (m <= 0) return acc;
+    if (st.skip > 0) {
+        st.skip--;
+        return serial_tail(acc, T, 0, m);
+    }
     const int lane = threadIdx.x & 31;
+    const double tk = lane < m ? T[lane] : 0.0;
     int pos = 0;
     while (pos < m) {
-        const int ea = (int)((xf::dbits(acc) >> 52) & 0x7ff);
-        if (ea != 0 && ea != 2047) {
-            int64_t r = 0;
-            bool ok = true;
-            const bool mine = lane >= pos && lane < m;
-            if (mine) ok = xf::quantize(tk, ea, &r);
-            if (!ok) r = 0;
-            int64_t P = r;  // inclusive prefix over the lanes
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const long long o = __shfl_up_sync(0xffffffffu, (long long)P, off);
-                if (lane >= off) P += o;
-            }
-            const int64_t A = xf::quanta_of(acc);
-            const int64_t S = A + P;
-            const unsigned bad = __ballot_sync(0xffffffffu, mine && !(ok && xf::inside_binade(A, S)));
-            const int stop = bad ? __ffs(bad) - 1 : m;
-            if (stop > pos) {
-                const long long Sc = __shfl_sync(0xffffffffu, (long long)S, stop - 1);
-                acc = xf::from_quanta(Sc, ea);
-                pos = stop;
-            }
-            if (pos >= m) break;
+        int ea = (int)((xf::dbits(acc) >> 52) & 0x7ff);
+        if (ea == 0 || ea == 2047) {  // a zero, subnormal, infinite or NaN accumulator: one term first
+            acc = serial_tail(acc, T, pos, pos + 1);
+            pos++;
+            continue;
         }
-        double tp[SERIAL_BURST];
+        int64_t r = 0;
+        bool ok = true;
+        const bool mine = lane >= pos && lane < m;
+        if (mine) ok = xf::quantize(tk, ea, &r);
+        if (!ok) r = 0;
+        int64_t P = r;  // inclusive prefix over the lanes
 #pragma unroll
-        for (int k = 0; k < SERIAL_BURST; k++) tp[k] = __shfl_sync(0xffffffffu, tk, min(pos + k, 31));
-#pragma unroll
-        for (int k = 0; k < SERIAL_BURST; k++)
-            if (pos + k < m) acc = __dadd_rn(acc, tp[k]);
-        pos += SERIAL_BURST;
+        for (int off = 1; off < 32; off <<= 1) {
+            const long long o = __shfl_up_sync(0xffffffffu, (long long)P, off);
+            if (lane >= off) P += o;
+        }
+        const int64_t A = xf::quanta_of(acc);
+        const int64_t S = A + P;
+        const unsigned bad = __ballot_sync(0xffffffffu, mine && !(ok && xf::inside_binade(A, S)));
+        const int stop = bad ? __ffs(bad) - 1 : m;
+        if (stop > pos) acc = xf::from_quanta(__shfl_sync(0xffffffffu, (long long)S, stop - 1), ea);
+        if (stop >= m) break;
+        if (stop - pos < SERIAL_GOOD_PASS) {  // a poor pass: the rest of the round serially
+            st.skip = st.backoff;
+            st.backoff = st.backoff ? min(2 * st.backoff, 8) : 1;
+            return serial_tail(acc, T, stop, m);
+        }
+        acc = serial_tail(acc, T, stop, stop + 1);
+        pos = stop + 1;
     }
+    st.backoff = 0;
     return acc;
 }
 

@@ -19,10 +19,16 @@
 // 1027 sources in the planetesimal disk), which thread-per-sink scheduling cannot.
 // The row-serial kernel (thread per sink) serves blocks with few sources per sink
 // (planetesimals x 3 massive bodies).  Sources are staged through shared memory in both.
+#include <string>
+
+#include "../../include/redgb.h"
 #include "common.cuh"
 #include "exact_fp64.h"
+#include "kernels.h"
 
 namespace redgb {
+
+int set_error(int code, const std::string& msg);
 
 struct PairOut {
     double tx, ty, tz;
@@ -85,19 +91,20 @@ __device__ __forceinline__ void pair_term(const GravArgs& g, const Tile& tile, i
 // astrocentric frame of the reference's CPU path -- each sink starts from the star's pull
 // and, for every source it interacts with, adds the direct term and then subtracts the
 // source's indirect term (pp_disk.cu:413-454), in source order.
-// resident CTAs per SM the register budget is cut for (the pair term's integer square root and
-// division hold many values; more resident warps hide their latency)
-#ifndef RG_PAIRPAR_MIN_BLOCKS
-#define RG_PAIRPAR_MIN_BLOCKS 3
-#endif
+// RG_PAIRPAR_RESIDENT (kernels.h): resident CTAs per SM the register budget is cut for (the
+// pair term's integer square root and division hold many values; more resident warps hide
+// their latency)
 
-template <int S, bool ASTRO>
-__global__ void __launch_bounds__(256, RG_PAIRPAR_MIN_BLOCKS) grav_fp64_pairpar(GravArgs g)
+// S sinks x STRIDE threads per CTA, four pair terms per thread and tile (J = 4 STRIDE sources).
+// S sets the number of CTAs, ceil(sinks / S): the tuner picks the S whose grid fills the last
+// wave of resident CTAs best (16 385 sinks at S = 36: 456 CTAs, exactly three per SM of a
+// 152-SM GB300), since every CTA of a block runs the same sources and so takes the same time.
+template <int S, int STRIDE, bool ASTRO>
+__global__ void __launch_bounds__(S * STRIDE, RG_PAIRPAR_RESIDENT) grav_fp64_pairpar(GravArgs g)
 {
-    constexpr int NT = 256;
-    constexpr int J = 1024 / S;
-    constexpr int STRIDE = NT / S;  // source offset between a thread's terms
-    constexpr int JPT = J / STRIDE;  // terms per thread per tile
+    constexpr int NT = S * STRIDE;
+    constexpr int JPT = 4;           // terms per thread per tile
+    constexpr int J = JPT * STRIDE;  // sources per tile
     constexpr int JA = ASTRO ? J : 1;
     __shared__ double tx[J * S], ty[J * S], tz[J * S];
     __shared__ double sx[J], sy[J], sz[J], sm[J], sR[J], srho[J];
@@ -330,6 +337,7 @@ __global__ void __launch_bounds__(128) few_sum_serial(FewSumArgs a)
         }
     };
     double acc = 0.0;
+    SerialSumState sst{0, 0};
     int cur = 0;
     load(0);
     for (int c0 = 0; c0 < n; c0 += SUM_CHUNK) {
@@ -340,7 +348,7 @@ __global__ void __launch_bounds__(128) few_sum_serial(FewSumArgs a)
         const int m = min(SUM_CHUNK, n - c0);
         for (int b = 0; b < m; b += 32) {
             const int mb = min(32, m - b);
-            acc = warp_serial_sum(acc, lane < mb ? B[cur][b + lane] : 0.0, mb);
+            acc = warp_serial_sum(acc, &B[cur][b], mb, sst);
         }
         __syncwarp();
         cur ^= 1;
@@ -386,19 +394,23 @@ int launch_grav_fp64_pairpar(const GravArgs& g, int S, cudaStream_t st)
 {
     if (g.n_tiles <= 0) return 0;
     if (g.astro) {
-        if (S == 16)
-            grav_fp64_pairpar<16, true><<<g.n_tiles, 256, 0, st>>>(g);
-        else if (S == 32)
-            grav_fp64_pairpar<32, true><<<g.n_tiles, 256, 0, st>>>(g);
-        else
-            grav_fp64_pairpar<8, true><<<g.n_tiles, 256, 0, st>>>(g);
+        switch (S) {
+        case 8: grav_fp64_pairpar<8, 32, true><<<g.n_tiles, 256, 0, st>>>(g); break;
+        case 16: grav_fp64_pairpar<16, 16, true><<<g.n_tiles, 256, 0, st>>>(g); break;
+        case 32: grav_fp64_pairpar<32, 8, true><<<g.n_tiles, 256, 0, st>>>(g); break;
+        default: return set_error(RG_ERR_ARG, "pair-parallel sinks per CTA: 8, 16 or 32 in the astrocentric frame");
+        }
     } else {
-        if (S == 16)
-            grav_fp64_pairpar<16, false><<<g.n_tiles, 256, 0, st>>>(g);
-        else if (S == 32)
-            grav_fp64_pairpar<32, false><<<g.n_tiles, 256, 0, st>>>(g);
-        else
-            grav_fp64_pairpar<8, false><<<g.n_tiles, 256, 0, st>>>(g);
+        switch (S) {
+        case 8: grav_fp64_pairpar<8, 32, false><<<g.n_tiles, 256, 0, st>>>(g); break;
+        case 12: grav_fp64_pairpar<12, 21, false><<<g.n_tiles, 252, 0, st>>>(g); break;
+        case 16: grav_fp64_pairpar<16, 16, false><<<g.n_tiles, 256, 0, st>>>(g); break;
+        case 18: grav_fp64_pairpar<18, 14, false><<<g.n_tiles, 252, 0, st>>>(g); break;
+        case 24: grav_fp64_pairpar<24, 10, false><<<g.n_tiles, 240, 0, st>>>(g); break;
+        case 32: grav_fp64_pairpar<32, 8, false><<<g.n_tiles, 256, 0, st>>>(g); break;
+        case 36: grav_fp64_pairpar<36, 7, false><<<g.n_tiles, 252, 0, st>>>(g); break;
+        default: return set_error(RG_ERR_ARG, "pair-parallel sinks per CTA: 8, 12, 16, 18, 24, 32 or 36");
+        }
     }
     RG_CUDA_CHECK(cudaGetLastError());
     return 0;

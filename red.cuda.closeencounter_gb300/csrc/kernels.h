@@ -73,6 +73,8 @@ struct EnergyArgs {
 
 int launch_energy(const EnergyArgs& a, cudaStream_t st);
 
+// resident pair-parallel CTAs per SM (the kernels are built for it: 80 registers, 256 threads)
+constexpr int RG_PAIRPAR_RESIDENT = 3;
 int launch_grav_fp64_pairpar(const GravArgs& g, int S, cudaStream_t st);
 int launch_astro_terms(const double* x, const double* y, const double* z, const double* mass, int n, double m_star,
                        double* out, long long stride, cudaStream_t st);

@@ -36,6 +36,7 @@ def load(auto_build=True):
     L.rg_get_profile.argtypes = [vp, ctypes.POINTER(T.Profile)]
     L.rg_measure_pipe_peak.argtypes = [ci, ctypes.POINTER(ctypes.c_double)]
     L.rg_autotune.argtypes = [vp, ci, ctypes.POINTER(T.Tune)]
+    L.rg_set_launch_shape.argtypes = [vp, ctypes.POINTER(T.Tune)]
     L.rg_test_hold_tile_copies.argtypes = [vp, ci]
     _lib = L
     return L
@@ -81,6 +82,12 @@ class System(api.System):
         t = T.Tune()
         self._call("autotune", self.handle, int(reps), ctypes.byref(t))
         return {f: getattr(t, f) for f, _ in t._fields_}
+
+    def set_launch_shape(self, pairpar_sinks=16, rowseq_max_src=64, mixed_chunks=0):
+        """Pin the launch shape (rg_set_launch_shape), e.g. one an earlier autotune chose."""
+        t = T.Tune()
+        t.pairpar_sinks, t.rowseq_max_src, t.mixed_chunks = int(pairpar_sinks), int(rowseq_max_src), int(mixed_chunks)
+        self._call("set_launch_shape", self.handle, ctypes.byref(t))
 
 
 def measure_pipe_peak(kind):

@@ -14,41 +14,60 @@
 
 using namespace redgb;
 
-// one round of up to 32 terms, as the warp computes it (warp_serial_sum)
-constexpr int SERIAL_BURST = 4;
-static double round_emulated(double acc, const double* t, int m, long long* fast, long long* slow)
+// one round of up to 32 terms, as the warp computes it (warp_serial_sum, with its state)
+struct State {
+    int skip, backoff;
+};
+
+static double round_emulated(double acc, const double* t, int m, State& st, long long* fast, long long* slow)
 {
+    if (m <= 0) return acc;
+    auto tail = [&](int from, int to) {
+        for (int k = from; k < to; k++) acc = acc + t[k];
+        *slow += to - from;
+        return acc;
+    };
+    if (st.skip > 0) {
+        st.skip--;
+        return tail(0, m);
+    }
     int pos = 0;
     while (pos < m) {
         const int ea = (int)((xf::dbits(acc) >> 52) & 0x7ff);
-        if (ea != 0 && ea != 2047) {
-            const int64_t A = xf::quanta_of(acc);
-            int64_t P = 0, Sc = 0;
-            int stop = m;
-            for (int k = pos; k < m; k++) {
-                int64_t r = 0;
-                const bool ok = xf::quantize(t[k], ea, &r);
-                if (!ok) r = 0;
-                P += r;
-                const int64_t S = A + P;
-                if (!(ok && xf::inside_binade(A, S))) {
-                    stop = k;
-                    break;
-                }
-                Sc = S;
-            }
-            if (stop > pos) {
-                *fast += stop - pos;
-                acc = xf::from_quanta(Sc, ea);
-                pos = stop;
-            }
-            if (pos >= m) break;
+        if (ea == 0 || ea == 2047) {
+            tail(pos, pos + 1);
+            pos++;
+            continue;
         }
-        for (int k = 0; k < SERIAL_BURST && pos < m; k++, pos++) {  // the failing term and a few more
-            acc = acc + t[pos];
-            ++*slow;
+        const int64_t A = xf::quanta_of(acc);
+        int64_t P = 0, Sc = 0;
+        int stop = m;
+        for (int k = pos; k < m; k++) {
+            int64_t r = 0;
+            const bool ok = xf::quantize(t[k], ea, &r);
+            if (!ok) r = 0;
+            P += r;
+            const int64_t S = A + P;
+            if (!(ok && xf::inside_binade(A, S))) {
+                stop = k;
+                break;
+            }
+            Sc = S;
         }
+        if (stop > pos) {
+            acc = xf::from_quanta(Sc, ea);
+            *fast += stop - pos;
+        }
+        if (stop >= m) break;
+        if (stop - pos < 8) {  // SERIAL_GOOD_PASS
+            st.skip = st.backoff;
+            st.backoff = st.backoff ? (st.backoff * 2 < 8 ? st.backoff * 2 : 8) : 1;
+            return tail(stop, m);
+        }
+        tail(stop, stop + 1);
+        pos = stop + 1;
     }
+    st.backoff = 0;
     return acc;
 }
 
@@ -69,7 +88,9 @@ int main(int argc, char** argv)
             const int n = sc_row(12345, fam, (uint64_t)row, &acc0, t.data());
             double ref = acc0, got = acc0;
             for (int k = 0; k < n; k++) ref = ref + t[k];
-            for (int b = 0; b < n; b += 32) got = round_emulated(got, t.data() + b, n - b < 32 ? n - b : 32, &fast, &slow);
+            State st{0, 0};
+            for (int b = 0; b < n; b += 32)
+                got = round_emulated(got, t.data() + b, n - b < 32 ? n - b : 32, st, &fast, &slow);
             terms += n;
             if (!same(ref, got)) {
                 if (bad < 5)

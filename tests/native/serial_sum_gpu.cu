@@ -29,10 +29,10 @@ __global__ void __launch_bounds__(32 * WARPS) check(uint64_t seed, int fam, long
             for (int k = 0; k < n; k++) ref = __dadd_rn(ref, t[k]);
         ref = __shfl_sync(0xffffffffu, ref, 0);
         double acc = acc0;
+        redgb::SerialSumState st{0, 0};
         for (int b = 0; b < n; b += 32) {
             const int m = n - b < 32 ? n - b : 32;
-            const double tk = lane < m ? t[b + lane] : 0.0;
-            acc = redgb::warp_serial_sum(acc, tk, m);
+            acc = redgb::warp_serial_sum(acc, t + b, m, st);
         }
         const bool ok = (acc != acc && ref != ref) || __double_as_longlong(acc) == __double_as_longlong(ref);
         if (lane == 0 && !ok) atomicAdd(bad, 1ull);
