@@ -51,9 +51,9 @@ WORKLOADS = {
 }
 FLOP_PER_PAIR = 36  # the reference's own count (pp_disk.cu:170-184,293)
 # DRAM bytes (read + write) of one launch of each gravity kernel of the default workload, from
-# one ncu capture of one launch (`-k <kernel> -c 1`) of
-# `python bench.py --no-ensemble --no-dense-ring --no-cpu-baseline --no-planetesimal-disk --steps 3 --warmup 3`
-NCU_TRAFFIC = {("self_gravitating_16384_rk4", "mixed"): 1332224, ("self_gravitating_16384_rk4", "fp64"): 820480}
+# one ncu capture of one launch (`-k <kernel> -c 1`) of `python bench.py --no-ensemble
+# --no-dense-ring --no-cpu-baseline --no-planetesimal-disk --no-autotune --steps 3 --warmup 3`
+NCU_TRAFFIC = {("self_gravitating_16384_rk4", "mixed"): 1332224, ("self_gravitating_16384_rk4", "fp64"): 809216}
 
 def _hbm_peak():
     """The measured HBM copy bandwidth of the GB300s (MEASURED_PEAKS.json, written
@@ -796,7 +796,8 @@ def ensemble_section(args):
         "proposer": {"train_records": int(len(x)), "train_disks": "seeds 1-64, dither 0.15",
                      "holdout": "whole disks (10%)", "expected_cost": getattr(net, "expected_cost", None),
                      "train_years": args.train_years, "loss": loss, "drift_std": float(np.std(y)),
-                     "residual_std": net.residual_std, "safety": net.safety, "setup_seconds": train_s},
+                     "residual_std": net.residual_std, "holdout_drift_std": net.holdout_drift_std,
+                     "safety": net.safety, "setup_seconds": train_s},
     }
 
 

@@ -139,9 +139,10 @@ __global__ void __launch_bounds__(256) ens_combine_fma_kernel(EnsStageArgs a)
     const StageTile t = a.tiles[blockIdx.x];
     if (!a.active[t.sys]) return;
     const double dt = a.dt[t.sys];
+    constexpr int NW = FORM == FORM_SUM ? NTERM : 5;  // the coefficients the form reads
     double w[MAXT];
 #pragma unroll
-    for (int q = 0; q < MAXT; q++) w[q] = dt * a.c[q];
+    for (int q = 0; q < NW; q++) w[q] = dt * a.c[q];
     const int nb = t.b1 - t.b0;
     for (int row = 0; row < 6; row++) {
         const long long base = (long long)row * a.stride + t.b0;

@@ -190,7 +190,8 @@ def fit(x, y, seed=0, epochs=30, batch=512, lr=2e-3, holdout=0.1, quantile=None,
     each sample) is given, since the samples of one disk are correlated in time.  The
     returned network's `safety` minimises the expected attempts per unit time on the held-out
     residuals y - prediction (best_safety), or with `quantile` is exp(that quantile of
-    them); `residual_std` is their spread."""
+    them); `residual_std` is their spread and `holdout_drift_std` the targets' own spread on the
+    held-out disks (the residual of predicting no drift)."""
     rng = np.random.RandomState(seed)
     if groups is not None and len(np.unique(groups)) > 2:
         disks = np.unique(groups)
@@ -210,11 +211,13 @@ def fit(x, y, seed=0, epochs=30, batch=512, lr=2e-3, holdout=0.1, quantile=None,
     if len(hold) > 0:
         res = y[hold] - p.forward(x[hold])
         p.residual_std = float(np.std(res))
+        p.holdout_drift_std = float(np.std(y[hold]))  # the residual of predicting no drift
         if quantile is not None:
             p.safety = float(min(1.0, np.exp(np.quantile(res, quantile))))
         else:
             p.safety, p.expected_cost = best_safety(res)
     else:
         p.residual_std = float("nan")
+        p.holdout_drift_std = float("nan")
         p.safety = 0.9
     return p, loss
