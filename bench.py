@@ -794,9 +794,10 @@ def ensemble_section(args):
         "event_lists": {name: _compare_events(ev, ev_f, len(disks)) for name, ev in (("learned_vs_fp64", ev_l),
                                                                                      ("mixed_vs_fp64", ev_m))},
         "proposer": {"train_records": int(len(x)), "train_disks": "seeds 1-64, dither 0.15",
-                     "holdout": "whole disks (10%)", "expected_cost": getattr(net, "expected_cost", None),
+                     "holdout": "whole disks (10% for the safety factor, 10% for the epoch kept)", "expected_cost": getattr(net, "expected_cost", None),
                      "train_years": args.train_years, "loss": loss, "drift_std": float(np.std(y)),
                      "residual_std": net.residual_std, "holdout_drift_std": net.holdout_drift_std,
+                     "best_epoch": net.best_epoch,
                      "safety": net.safety, "setup_seconds": train_s},
     }
 

@@ -569,6 +569,19 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
         RG_CUDA_CHECK(cudaStreamWaitEvent(c->st2, c->ev_fork, 0));
     }
     const cudaStream_t row_st = fork ? c->st2 : c->st;
+    // FP64: the few-sink rows (star, giants: their terms, then a long serial sum per row, whose
+    // dependent FP64 additions set the evaluation's latency) on the side stream, beside the other
+    // groups; they write other rows and append events atomically (collect_events sorts them)
+    bool fork_few = false;
+    if (c->gravity_mode == RG_GRAVITY_FP64) {
+        bool few = false, other = false;
+        for (const auto& gr : c->plan[0]) (gr.kind == GROUP_FEW_SERIAL ? few : other) = true;
+        fork_few = few && other;
+    }
+    if (fork_few) {
+        RG_CUDA_CHECK(cudaEventRecord(c->ev_fork, c->st));
+        RG_CUDA_CHECK(cudaStreamWaitEvent(c->st2, c->ev_fork, 0));
+    }
     for (const auto& gr : c->plan[c->gravity_mode == RG_GRAVITY_MIXED ? 1 : 0]) {
         g.tiles = c->d_tiles + gr.off;
         g.n_tiles = gr.n;
@@ -583,7 +596,8 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
             break;
         case GROUP_FEW_SERIAL:
             rc = launch_grav_fp64_few(g, c->d_few_row0 + gr.off, gr.max_src, c->d_terms, c->few_rows, c->few_pitch,
-                                      c->d_row_sink, c->d_row_nsrc, nullptr, gr.row_base, gr.rows, c->st);
+                                      c->d_row_sink, c->d_row_nsrc, nullptr, gr.row_base, gr.rows,
+                                      fork_few ? c->st2 : c->st);
             c->n_kernels += 2;
             break;
         case GROUP_DF_ROWSEQ:
@@ -647,7 +661,7 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
         }
         if (rc) break;
     }
-    if (fork) {  // joined on every path, so that no row kernel outlives the call's stream order
+    if (fork || fork_few) {  // joined on every path, so that no row kernel outlives the call's stream order
         RG_CUDA_CHECK(cudaEventRecord(c->ev_join, c->st2));
         RG_CUDA_CHECK(cudaStreamWaitEvent(c->st, c->ev_join, 0));
     }

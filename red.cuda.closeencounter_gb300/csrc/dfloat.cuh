@@ -76,6 +76,15 @@ __device__ __forceinline__ DF df_add(DF a, DF b)
     return df_fast_sum(s.hi, s.lo);
 }
 
+// a + b for operands of one sign (no cancellation): the "sloppy" addition of Hida, Li and
+// Bailey, whose relative error stays near 2^-46 when the operands cannot cancel
+__device__ __forceinline__ DF df_add_same_sign(DF a, DF b)
+{
+    DF s = df_two_sum(a.hi, b.hi);
+    s.lo += a.lo + b.lo;
+    return df_fast_sum(s.hi, s.lo);
+}
+
 __device__ __forceinline__ DF df_mul(DF a, DF b)
 {
     DF p = df_two_prod(a.hi, b.hi);

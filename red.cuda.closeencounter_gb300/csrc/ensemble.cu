@@ -1274,7 +1274,7 @@ int record_attempt(rg_ens* e, bool in_graph)
     pr = prof_begin(e, 2);
     if (e->d_log || e->mlp || e->dither > 0.0f) {
         // step-start features (and, with a network attached, the proposed trial step): one
-        // kernel, a CTA per disk
+        // kernel, a CTA per stage tile, the network in each disk's last tile
         PropArgs pa{};
         pa.s = e->sys();
         pa.y = e->d_y;

@@ -262,7 +262,7 @@ __device__ __forceinline__ void acc_df(Acc2& acc, DF t)
 __device__ __forceinline__ void df_term_disp(DF dx, DF dy, DF dz, float mh, float ml, DF& tx, DF& ty, DF& tz,
                                              float& r2f)
 {
-    DF r2 = df_add(df_add(df_mul(dx, dx), df_mul(dy, dy)), df_mul(dz, dz));
+    DF r2 = df_add_same_sign(df_add_same_sign(df_mul(dx, dx), df_mul(dy, dy)), df_mul(dz, dz));  // squares: no cancellation
     // a merged body parked at 1e20 AU (pp_disk.cu:1184) overflows r^2 in FP32; its mass is 0
     if (!(r2.hi < 1.0e30f)) r2 = DF{1.0e30f, 0.0f};
     const float y0 = rsqrt_approx(r2.hi);
@@ -304,15 +304,23 @@ __device__ __forceinline__ void df_term_fp64(double xi, double yi, double zi, do
 
 // FP32 screen of the event tests of pair_term (pp_disk.cu:262-280) with a 1e-3 margin;
 // candidates are decided in FP64 by exact_event_tests
+// frad: the tile's collision factor in FP32 (tile_frad_f, formed once per CTA: a per-pair load
+// and conversion would run on GB300's FP64 pipe for every heavy pair)
+__device__ __forceinline__ float tile_frad_f(const GravArgs& g, const Tile& tile)
+{
+    return g.sys_f_rad ? (float)g.sys_f_rad[tile.sys] : g.f_rad_f;
+}
+
 __device__ __forceinline__ void df_screen(const GravArgs& g, const Tile& tile, int i, int j, float r2f, float Ri,
-                                          float Rj, float rhoi, float rhoj, float mi, float mj, float inv3M)
+                                          float Rj, float rhoi, float rhoj, float mi, float mj, float inv3M,
+                                          float frad)
 {
     const int li = i - tile.base, lj = j - tile.base;
     if (!(li > 0 && li > lj)) return;
     const float margin = 1.001f;
     bool cand = false;
     if (g.record) {
-        const float lim = (g.sys_f_rad ? (float)g.sys_f_rad[tile.sys] : g.f_rad_f) * (Ri + Rj) * margin;
+        const float lim = frad * (Ri + Rj) * margin;
         cand = r2f < lim * lim;
     }
     if (g.hill && tile.block != 2 && lj > 0) {
@@ -649,6 +657,7 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
 
     // heavy sources (first chunk only): double-float terms, split over the warps
     if (blockIdx.y == 0) {
+        const float frad = SCREEN ? tile_frad_f(g, tile) : 0.0f;
         for (int j = tile.src_begin + warp; j < heavy_end; j += MX_WARPS) {
             if (0 > g.id[j]) continue;
             const SplitPos pj = a.sp[j];
@@ -671,7 +680,7 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
                 acc_df(az[r], tz);
                 if (SCREEN) {
                     const float4 sf = S.sinkf[s];
-                    df_screen(g, tile, si[r], j, r2f, sf.x, Rj, sf.z, rhoj, sf.y, pj.zm.z, inv3M);
+                    df_screen(g, tile, si[r], j, r2f, sf.x, Rj, sf.z, rhoj, sf.y, pj.zm.z, inv3M, frad);
                 }
             }
         }
@@ -830,6 +839,7 @@ __global__ void __launch_bounds__(DF_ROW_NT, 8) grav_df_rowseq(GravArgs g, const
     const bool active = sink_ok && 0 < g.id[i];
     SplitPos si{};
     float Ri = 0.0f, rhoi = 0.0f, mi = 0.0f, inv3M = 0.0f;
+    const float frad = SCREEN ? tile_frad_f(g, tile) : 0.0f;
     SplitPos p0{};
     if (SCREEN && g.hill) {
         p0 = sp[tile.base];
@@ -844,7 +854,7 @@ __global__ void __launch_bounds__(DF_ROW_NT, 8) grav_df_rowseq(GravArgs g, const
         }
     }
     const float close2 = close_r2(si);
-    DF ax{0.0f, 0.0f}, ay{0.0f, 0.0f}, az{0.0f, 0.0f};
+    Acc2 ax{0.0f, 0.0f}, ay{0.0f, 0.0f}, az{0.0f, 0.0f};  // compensated: a few terms per sink
     for (int j0 = tile.src_begin; j0 < tile.src_end; j0 += DF_ROW_NT) {
         const int nj = min(DF_ROW_NT, tile.src_end - j0);
         if (t < nj) {
@@ -867,18 +877,18 @@ __global__ void __launch_bounds__(DF_ROW_NT, 8) grav_df_rowseq(GravArgs g, const
                 if (r2f < close2)
                     df_term_fp64(g.px[i], g.py[i], g.pz[i], g.px[j], g.py[j], g.pz[j], s_p[q].zm.z, s_p[q].zm.w, tx,
                                  ty, tz, r2f);
-                ax = df_add(ax, tx);
-                ay = df_add(ay, ty);
-                az = df_add(az, tz);
-                if (SCREEN) df_screen(g, tile, i, j, r2f, Ri, s_R[q], rhoi, s_rho[q], mi, s_p[q].zm.z, inv3M);
+                acc_df(ax, tx);
+                acc_df(ay, ty);
+                acc_df(az, tz);
+                if (SCREEN) df_screen(g, tile, i, j, r2f, Ri, s_R[q], rhoi, s_rho[q], mi, s_p[q].zm.z, inv3M, frad);
             }
         }
         __syncthreads();
     }
     if (sink_ok) {
-        g.ax[i] = df_to_double(ax);
-        g.ay[i] = df_to_double(ay);
-        g.az[i] = df_to_double(az);
+        g.ax[i] = f2d_bits(ax.s) + f2d_bits(ax.c);
+        g.ay[i] = f2d_bits(ay.s) + f2d_bits(ay.c);
+        g.az[i] = f2d_bits(az.s) + f2d_bits(az.c);
     }
 }
 
@@ -919,6 +929,7 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
     __shared__ DF s_red[8][3 * SMAX];
     SplitPos p0{};
     float inv3M = 0.0f;
+    const float frad = SCREEN ? tile_frad_f(g, tile) : 0.0f;
     if (SCREEN && g.hill) {
         p0 = a.sp[tile.base];
         inv3M = 1.0f / (3.0f * p0.zm.z);
@@ -934,11 +945,11 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
         s_close2[threadIdx.x] = close_r2(pi);
     }
     __syncthreads();
-    DF acc[SMAX][3];
+    Acc2 acc[SMAX][3];  // compensated sums of the thread's sources (a few per chunk)
 #pragma unroll
     for (int s = 0; s < SMAX; s++)
 #pragma unroll
-        for (int c = 0; c < 3; c++) acc[s][c] = DF{0.0f, 0.0f};
+        for (int c = 0; c < 3; c++) acc[s][c] = Acc2{0.0f, 0.0f};
     const int c1 = min(nsrc, c0 + a.chunk);
     for (int q = c0 + (int)threadIdx.x; q < c1; q += blockDim.x) {
         const int j = tile.src_begin + q;
@@ -960,10 +971,10 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
                     if (r2f < s_close2[s])
                         df_term_fp64(g.px[i], g.py[i], g.pz[i], g.px[j], g.py[j], g.pz[j], pj.zm.z, pj.zm.w, tx, ty,
                                      tz, r2f);
-                    acc[s][0] = df_add(acc[s][0], tx);
-                    acc[s][1] = df_add(acc[s][1], ty);
-                    acc[s][2] = df_add(acc[s][2], tz);
-                    if (SCREEN) df_screen(g, tile, i, j, r2f, s_R[s], Rj, s_rho[s], rhoj, s_m[s], pj.zm.z, inv3M);
+                    acc_df(acc[s][0], tx);
+                    acc_df(acc[s][1], ty);
+                    acc_df(acc[s][2], tz);
+                    if (SCREEN) df_screen(g, tile, i, j, r2f, s_R[s], Rj, s_rho[s], rhoj, s_m[s], pj.zm.z, inv3M, frad);
                 }
             }
         }
@@ -974,7 +985,7 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
         if (s < ns) {  // uniform over the CTA
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                DF v = acc[s][c];
+                DF v = df_two_sum(acc[s][c].s, acc[s][c].c);
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) {
                     const DF o{__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off)};

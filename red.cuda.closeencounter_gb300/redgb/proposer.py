@@ -187,17 +187,24 @@ def fit(x, y, seed=0, epochs=30, batch=512, lr=2e-3, holdout=0.1, quantile=None,
     """A new network standardised on (x, y)'s inputs and trained on the GPU.
 
     A `holdout` fraction is kept out of training -- whole disks when `groups` (the disk of
-    each sample) is given, since the samples of one disk are correlated in time.  The
-    returned network's `safety` minimises the expected attempts per unit time on the held-out
-    residuals y - prediction (best_safety), or with `quantile` is exp(that quantile of
-    them); `residual_std` is their spread and `holdout_drift_std` the targets' own spread on the
-    held-out disks (the residual of predicting no drift)."""
+    each sample) is given, since the samples of one disk are correlated in time -- and, with
+    groups, as many other disks for validation: the weights kept are those of the epoch with
+    the smallest validation residual (the network fits disks it has seen better than new ones
+    after a few epochs).  The returned network's `safety` minimises the expected attempts per
+    unit time on the held-out residuals y - prediction (best_safety), or with `quantile` is
+    exp(that quantile of them); `residual_std` is their spread and `holdout_drift_std` the
+    targets' own spread on the held-out disks (the residual of predicting no drift);
+    `best_epoch` is the epoch kept."""
     rng = np.random.RandomState(seed)
+    val = np.zeros(0, np.int64)
     if groups is not None and len(np.unique(groups)) > 2:
         disks = np.unique(groups)
-        held = rng.choice(disks, size=max(1, int(round(len(disks) * holdout))), replace=False)
-        is_hold = np.isin(groups, held)
-        hold, train = np.flatnonzero(is_hold), np.flatnonzero(~is_hold)
+        k = max(1, int(round(len(disks) * holdout)))
+        pick = rng.choice(disks, size=min(len(disks) - 1, 2 * k), replace=False)
+        held, valid = pick[:k], pick[k:]
+        is_hold, is_val = np.isin(groups, held), np.isin(groups, valid)
+        hold, val = np.flatnonzero(is_hold), np.flatnonzero(is_val)
+        train = np.flatnonzero(~is_hold & ~is_val)
     else:
         perm = rng.permutation(len(x))
         n_hold = int(len(x) * holdout)
@@ -207,7 +214,15 @@ def fit(x, y, seed=0, epochs=30, batch=512, lr=2e-3, holdout=0.1, quantile=None,
     std = x[train].std(axis=0)
     std[std < 1e-6] = 1.0
     p.set_normalisation(mean, std)
-    loss = p.train(x[train], y[train], epochs=epochs, batch=batch, lr=lr, seed=seed)
+    loss, best, best_w, p.best_epoch = float("nan"), np.inf, None, epochs - 1
+    for ep in range(epochs):
+        loss = p.train(x[train], y[train], epochs=1, batch=batch, lr=lr, seed=seed + ep)
+        if len(val) > 0:
+            rms = float(np.sqrt(np.mean((y[val] - p.forward(x[val])) ** 2)))
+            if rms < best:
+                best, best_w, p.best_epoch = rms, p.params(), ep
+    if best_w is not None:
+        p.set_params(best_w)
     if len(hold) > 0:
         res = y[hold] - p.forward(x[hold])
         p.residual_std = float(np.std(res))
