@@ -765,7 +765,7 @@ def ensemble_section(args):
         t_a = s.state()[4]
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        s.advance(warm_day + span_day)
+        s.advance(warm_day + args.sequential_years * T.YEAR)
         torch.cuda.synchronize()
         seq_s += time.perf_counter() - t1
         seq_years += (s.state()[4] - t_a) / T.YEAR
@@ -773,7 +773,8 @@ def ensemble_section(args):
         s.close()
     sequential = {"sim_years_per_s": seq_years / seq_s, "seconds": seq_s, "sim_years": seq_years,
                   "max_dE_over_E": seq_dE, "sample": f"{len(sample)} of {len(disks)} disks (every "
-                  f"{max(1, len(disks) // args.sequential_sample)}th), the rate applies to all of them"}
+                  f"{max(1, len(disks) // args.sequential_sample)}th), {args.sequential_years:g} yr each; the rate "
+                  "applies to all of them"}
     procs = max(1, min(os.cpu_count() or 1, 32))
     cpu = cpu_ensemble([65 + k for k in range(procs)], args.cpu_ensemble_years, hill, procs)
     return {
@@ -824,7 +825,10 @@ def main():
                          "warm-up attempts, in the form --ensemble-form; prints their device times")
     ap.add_argument("--ensemble-form", default="mixed", choices=["mixed", "learned", "fp64"])
     ap.add_argument("--ensemble-disks", type=int, default=256)
-    ap.add_argument("--ensemble-years", type=float, default=10.0)
+    ap.add_argument("--ensemble-years", type=float, default=100.0,
+                    help="simulated years per disk of the batched ensemble forms (the configuration's 100)")
+    ap.add_argument("--sequential-years", type=float, default=10.0,
+                    help="simulated years per disk of the one-disk-at-a-time FP64 sample")
     ap.add_argument("--train-years", type=float, default=450.0,
                     help="years of dithered training runs of the 64 training disks (about 1e6 step records)")
     ap.add_argument("--sequential-sample", type=int, default=8)
