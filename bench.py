@@ -697,13 +697,19 @@ def ensemble_section(args):
         secs, n_att = advance_timed(e, warm_day + span_day)
         _, g1 = e.kernel_count()
         st = [e.stats(k) for k in range(len(disks))]
-        dE = max(abs((e.energy(k)[0] - E0[k]) / E0[k]) for k in range(len(disks)))
+        dEk = [abs((e.energy(k)[0] - E0[k]) / E0[k]) for k in range(len(disks))]
         sim_years = sum(a["t_day"] - b["t_day"] for a, b in zip(st, st0)) / T.YEAR
         tried = sum(a["n_tried_step"] - b["n_tried_step"] for a, b in zip(st, st0))
         failed = sum(a["n_failed_step"] - b["n_failed_step"] for a, b in zip(st, st0))
         ev, sysv = e.events()
+        # a merge is inelastic (the pair's relative kinetic energy is lost) and an ejection or a
+        # hit-star merger removes a body: energy conservation is judged on the disks without one
+        merged = {int(k) for r, k in zip(ev, sysv) if int(r["event_name"]) != T.EVENT_CLOSE_ENCOUNTER}
+        dE_free = [v for k, v in enumerate(dEk) if k not in merged]
         out = {"sim_years_per_s": sim_years / secs, "seconds": secs, "sim_years": sim_years, "attempts": tried,
-               "rejected_frac": failed / max(tried, 1), "max_dE_over_E": dE, "events": int(len(ev)),
+               "rejected_frac": failed / max(tried, 1), "max_dE_over_E": max(dEk),
+               "max_dE_over_E_disks_without_merges": max(dE_free) if dE_free else None,
+               "disks_with_merges": len(merged), "events": int(len(ev)),
                "all_done": all(a["status"] == T.SYS_DONE for a in st),
                "iterations": int(n_att), "ms_per_iteration": 1e3 * secs / max(n_att, 1),
                "graph_launches": int(g1 - g0), "autotune": tune}

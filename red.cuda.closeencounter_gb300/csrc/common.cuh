@@ -88,6 +88,11 @@ struct GravArgs {
     long long astro_stride;
     // ensembles: per system collision factor (THRESHOLD_RADII_ENHANCE_FACTOR); nullptr: f_rad
     const double* sys_f_rad;
+    // the ensemble's mixed form keeps its stage vectors as double-float pairs (float2 per
+    // element, hi + lo): acc_f2 -- the output rows are float2 rows; vel_f2 -- so are the
+    // velocity rows (stages after the step start)
+    int acc_f2;
+    int vel_f2;
 };
 
 // the collision factor of a tile's system

@@ -120,5 +120,36 @@ __device__ __forceinline__ DF split_df(double v)
     return d;
 }
 
+// compensated accumulation: s + c tracks the exact sum of the added terms to ~2^-46
+struct Acc2 {
+    float s, c;
+};
+
+__device__ __forceinline__ void two_sum_add(Acc2& a, float t)
+{
+    const float s = a.s + t;
+    const float bp = s - a.s;
+    const float err = (a.s - (s - bp)) + (t - bp);
+    a.s = s;
+    a.c += err;
+}
+
+// a double-float term into a compensated FP32 accumulator
+__device__ __forceinline__ void acc_df(Acc2& acc, DF t)
+{
+    two_sum_add(acc, t.hi);
+    acc.c += t.lo;
+}
+
+// a stage-vector element stored as a double-float pair (float2: hi, lo)
+__device__ __forceinline__ float2 to_f2(double v)
+{
+    float h, l;
+    split_bits(v, h, l);
+    return make_float2(h, l);
+}
+
+__device__ __forceinline__ double f2_to_double(float2 f) { return f2d_bits(f.x) + f2d_bits(f.y); }
+
 
 }  // namespace redgb

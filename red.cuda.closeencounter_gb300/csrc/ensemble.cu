@@ -108,56 +108,88 @@ __global__ void __launch_bounds__(256) ens_combine_kernel(EnsStageArgs a)
     }
 }
 
-// Mixed-precision mode: the per-disk coefficients dt * c_q are formed once per CTA and the sum
-// is contracted, y + fma(dt c_q, k_q, ...): NTERM + 1 FP64 operations per element, half the
-// bit-exact form's.  (The same sum in double-float on the FP32 pipes, with one FP64 addition
-// onto y, was measured slower on GB300: 2.35 against 1.41 ms of stage kernels per attempt of
-// the 256-disk ensemble, the FP32 / integer work of the splits and double-float products
-// outweighing the FP64 operations it saves.)
-template <int FORM, int NTERM>
-__device__ __forceinline__ double ens_combine_fma(const EnsStageArgs& a, const double* w, long long e)
+// Mixed form with double-float stage vectors (each element of k_q a float2 hi + lo, written
+// by the gravity kernels and by these combinations): y + sum_q (dt c_q) k_q with the products
+// and the sum in double-float on the FP32 pipes and two FP64 additions per element (the sum
+// onto y), where the FP64 form's FMAs kept GB300's FP64 pipe busy; the kernel is then bound
+// by HBM.  Stage rows: positions (rows 0-2) as FP64 for the next evaluation, velocities (the
+// next stage vector's rows 0-2) as double-float; y_{n+1}: FP64.
+__device__ __forceinline__ DF ldf(const double* k, long long e)
 {
-    const double y = a.y[e];
-    double sum;
-    if (FORM == FORM_SUM) {
-        sum = w[0] * a.k[0][e];
-#pragma unroll
-        for (int q = 1; q < NTERM; q++) sum = fma(w[q], a.k[q][e], sum);
-    } else {
-        sum = w[0] * a.k[0][e];
-        sum = fma(w[1], a.k[1][e], sum);
-        sum = fma(w[2], a.k[2][e] + a.k[3][e], sum);
-        sum = fma(w[3], a.k[4][e] + a.k[5][e], sum);
-        sum = fma(w[4], a.k[6][e], sum);
-    }
-    return y + sum;
+    const float2 f = reinterpret_cast<const float2*>(k)[e];
+    return DF{f.x, f.y};
 }
 
 template <int FORM, int NTERM>
-__global__ void __launch_bounds__(256) ens_combine_fma_kernel(EnsStageArgs a)
+__device__ __forceinline__ double ens_combine_df(const EnsStageArgs& a, const DF* w, long long e)
+{
+    DF sum;
+    if (FORM == FORM_SUM) {
+        sum = df_mul(w[0], ldf(a.k[0], e));
+#pragma unroll
+        for (int q = 1; q < NTERM; q++) sum = df_add(sum, df_mul(w[q], ldf(a.k[q], e)));
+    } else {
+        sum = df_mul(w[0], ldf(a.k[0], e));
+        sum = df_add(sum, df_mul(w[1], ldf(a.k[1], e)));
+        sum = df_add(sum, df_mul(w[2], df_add(ldf(a.k[2], e), ldf(a.k[3], e))));
+        sum = df_add(sum, df_mul(w[3], df_add(ldf(a.k[4], e), ldf(a.k[5], e))));
+        sum = df_add(sum, df_mul(w[4], ldf(a.k[6], e)));
+    }
+    return a.y[e] + (f2d_bits(sum.hi) + f2d_bits(sum.lo));
+}
+
+template <int FORM, int NTERM>
+__global__ void __launch_bounds__(256) ens_combine_df_kernel(EnsStageArgs a)
 {
     const StageTile t = a.tiles[blockIdx.x];
     if (!a.active[t.sys]) return;
     const double dt = a.dt[t.sys];
     constexpr int NW = FORM == FORM_SUM ? NTERM : 5;  // the coefficients the form reads
-    double w[MAXT];
+    DF w[MAXT];
 #pragma unroll
-    for (int q = 0; q < NW; q++) w[q] = dt * a.c[q];
+    for (int q = 0; q < NW; q++) w[q] = split_df(dt * a.c[q]);
     const int nb = t.b1 - t.b0;
     for (int row = 0; row < 6; row++) {
         const long long base = (long long)row * a.stride + t.b0;
+        const bool f2 = FORM == FORM_SUM && row >= 3;  // the next stage vector's velocity rows
         double* out = row < 3 ? a.out_lo + base : a.out_hi + base - 3LL * a.stride;
         for (int i = threadIdx.x; i < nb; i += 2 * blockDim.x) {
             const int i2 = i + blockDim.x;
-            const double o1 = ens_combine_fma<FORM, NTERM>(a, w, base + i);
-            if (i2 < nb) {
-                const double o2 = ens_combine_fma<FORM, NTERM>(a, w, base + i2);
-                out[i] = o1;
-                out[i2] = o2;
+            const double o1 = ens_combine_df<FORM, NTERM>(a, w, base + i);
+            const double o2 = i2 < nb ? ens_combine_df<FORM, NTERM>(a, w, base + i2) : 0.0;
+            if (f2) {
+                reinterpret_cast<float2*>(out)[i] = to_f2(o1);
+                if (i2 < nb) reinterpret_cast<float2*>(out)[i2] = to_f2(o2);
             } else {
                 out[i] = o1;
+                if (i2 < nb) out[i2] = o2;
             }
         }
+    }
+}
+
+// rows [r0, r0 + nr) of FP64 src -> double-float rows [d0, d0 + nr) of dst, for disks whose
+// mask is set (the step start's velocities into the first stage vector, mixed form)
+__global__ void ens_copy_to_f2_kernel(const StageTile* tiles, const int* mask, const double* src, int r0, double* dst,
+                                      int d0, int nr, int stride)
+{
+    const StageTile t = tiles[blockIdx.x];
+    if (!mask[t.sys]) return;
+    const int nb = t.b1 - t.b0;
+    for (int f = threadIdx.x; f < nr * nb; f += blockDim.x) {
+        const int r = f / nb, i = t.b0 + f - r * nb;
+        reinterpret_cast<float2*>(dst + (long long)(d0 + r) * stride)[i] = to_f2(src[(long long)(r0 + r) * stride + i]);
+    }
+}
+
+// the stage vectors' storage between FP64 and double-float pairs, in place (n elements)
+__global__ void k_format_kernel(double* k, long long n, int to_f2_pairs)
+{
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
+        if (to_f2_pairs)
+            reinterpret_cast<float2*>(k)[e] = to_f2(k[e]);
+        else
+            k[e] = f2_to_double(reinterpret_cast<const float2*>(k)[e]);
     }
 }
 
@@ -176,6 +208,9 @@ __global__ void ens_copy_kernel(const StageTile* tiles, const int* mask, const d
 }
 
 // e = ((k0 + k10) - k11) - k12, signed maximum starting at 0 (integrator.cu:240-255)
+// F2: the stage vectors are double-float pairs (the mixed form): the same sum in double-float,
+// rounded to FP64 once
+template <bool F2>
 __global__ void __launch_bounds__(256) ens_error_kernel(const StageTile* tiles, const int* active, const double* k0,
                                                         const double* k10, const double* k11, const double* k12,
                                                         int stride, unsigned long long* max_bits)
@@ -187,7 +222,14 @@ __global__ void __launch_bounds__(256) ens_error_kernel(const StageTile* tiles, 
     for (int f = threadIdx.x; f < 6 * nb; f += blockDim.x) {
         const int row = f / nb;
         const long long e = (long long)row * stride + t.b0 + (f - row * nb);
-        const double v = (k0[e] + k10[e] - k11[e] - k12[e]);
+        double v;
+        if (F2) {
+            const DF d = df_add(df_add(df_add(ldf(k0, e), ldf(k10, e)), DF{-ldf(k11, e).hi, -ldf(k11, e).lo}),
+                                DF{-ldf(k12, e).hi, -ldf(k12, e).lo});
+            v = f2d_bits(d.hi) + f2d_bits(d.lo);
+        } else {
+            v = (k0[e] + k10[e] - k11[e] - k12[e]);
+        }
         if (m < v) m = v;
     }
 #pragma unroll
@@ -382,16 +424,28 @@ __device__ __forceinline__ float to_f32(double v)
 // body 0, masses, distance from body 0) in shared memory, ns of them in all (the rest are read
 // from the state rows), M = body 0's mass.  The body's values are loaded before any test, so
 // that the loads of consecutive bodies overlap.
-__device__ __forceinline__ void body_features(const double* y, const double* k0, const double* mass, const int* id,
-                                              long long stride, int b, int ns, const float4* si, const float* si_r,
-                                              float x0, float y0, float z0, float M, int i, float& am, float& h3)
+__device__ __forceinline__ void body_features(const double* y, const double* k0, bool k_f2, const double* mass,
+                                              const int* id, long long stride, int b, int ns, const float4* si,
+                                              const float* si_r, float x0, float y0, float z0, float M, int i,
+                                              float& am, float& h3)
 {
     const int idi = id[i];
+    // the step start's acceleration: FP64, or a double-float pair (the mixed form) whose
+    // leading float is all a feature needs
     const double kx = k0[3LL * stride + i], ky = k0[4LL * stride + i], kz = k0[5LL * stride + i];
     const double px = y[i], py = y[stride + i], pz = y[2LL * stride + i];
     const double pm = mass[i];
     if (idi <= 0) return;
-    const float ax = to_f32(kx), ay = to_f32(ky), az = to_f32(kz);
+    float ax, ay, az;
+    if (k_f2) {
+        ax = __uint_as_float((unsigned)__double_as_longlong(kx));  // the pair's first float
+        ay = __uint_as_float((unsigned)__double_as_longlong(ky));
+        az = __uint_as_float((unsigned)__double_as_longlong(kz));
+    } else {
+        ax = to_f32(kx);
+        ay = to_f32(ky);
+        az = to_f32(kz);
+    }
     am = fmaxf(am, sqrtf(ax * ax + ay * ay + az * az));
     const float xi = to_f32(px) - x0, yi = to_f32(py) - y0, zi = to_f32(pz) - z0;
     const float ri = sqrtf(xi * xi + yi * yi + zi * zi);
@@ -420,6 +474,7 @@ __device__ __forceinline__ void body_features(const double* y, const double* k0,
 
 struct PropArgs {
     EnsSys s;
+    int k_f2;  // the stage vectors are double-float pairs (the mixed form)
     const StageTile* tiles;  // the stage tiles (a disk's tiles are consecutive)
     const int* tiles_of;     // per disk: its stage tiles
     unsigned int* red;       // per disk: max |a| bits, min h3 bits, tiles done (reset by the last)
@@ -481,7 +536,7 @@ __global__ void __launch_bounds__(PROP_THREADS) ens_propose_kernel(PropArgs a)
         __syncthreads();
 #pragma unroll 2
         for (int i = tile.b0 + threadIdx.x; i < tile.b1; i += blockDim.x)
-            body_features(a.y, a.k0, a.mass, a.id, a.stride, b, ns, si, si_r, x0, y0, z0, M, i, am, h3);
+            body_features(a.y, a.k0, a.k_f2 != 0, a.mass, a.id, a.stride, b, ns, si, si_r, x0, y0, z0, M, i, am, h3);
         for (int off = 16; off > 0; off >>= 1) {
             am = fmaxf(am, __shfl_xor_sync(0xffffffffu, am, off));
             h3 = fminf(h3, __shfl_xor_sync(0xffffffffu, h3, off));
@@ -655,6 +710,7 @@ struct rg_ens {
     double* d_y = nullptr;
     double* d_yout = nullptr;
     double* d_k[13] = {};
+    int k_f2_now = 0;  // the first stage vector (kept across a rejected attempt) holds double-float pairs
     double* d_P = nullptr;
     double* d_mass = nullptr;
     double* d_radius = nullptr;
@@ -1036,6 +1092,10 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
     g.hill_f3_f = (float)g.hill_f3;
     g.record = (stage > 0 && g.f_rad > 0.0) ? 1 : 0;
     g.hill = hill ? 1 : 0;
+    // the mixed form's stage vectors are double-float pairs: the accelerations written, and the
+    // velocities read for records after the step start (stage 0 reads the FP64 state's)
+    g.acc_f2 = e->gravity_mode == RG_GRAVITY_MIXED ? 1 : 0;
+    g.vel_f2 = g.acc_f2 && stage > 0 ? 1 : 0;
     g.seq = (uint32_t)stage;
     g.ev = EventBuf{e->d_ev, e->d_ev_count, e->ev_cap};
     g.hv = EventBuf{e->d_hill, e->d_hill_count, e->ev_cap};
@@ -1160,11 +1220,11 @@ int launch_stage(rg_ens* e, int form, int nterm, const int* stages, const double
     a.out_hi = out_hi;
     const int g = (int)e->stiles.size();
     if (g <= 0) return RG_OK;
-    const bool fused = e->gravity_mode == RG_GRAVITY_MIXED;
+    const bool df = e->gravity_mode == RG_GRAVITY_MIXED;  // double-float stage vectors
 #define RG_ENS(F, T)                                                     \
     do {                                                                 \
-        if (fused)                                                       \
-            ens_combine_fma_kernel<F, T><<<g, 256, 0, e->st>>>(a);       \
+        if (df)                                                          \
+            ens_combine_df_kernel<F, T><<<g, 256, 0, e->st>>>(a);        \
         else                                                             \
             ens_combine_kernel<F, T><<<g, 256, 0, e->st>>>(a);           \
     } while (0)
@@ -1263,7 +1323,10 @@ int record_attempt(rg_ens* e, bool in_graph)
     const int nb = (e->n_sys + 127) / 128;
     // stage 0 for the disks that start a new step: k0 = (v, a(y))
     long pr = prof_begin(e, 2);
-    ens_copy_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active_f0, e->d_y, 3, e->d_k[0], 0, 3, e->cap);
+    if (e->gravity_mode == RG_GRAVITY_MIXED)  // the stage vectors are double-float pairs
+        ens_copy_to_f2_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active_f0, e->d_y, 3, e->d_k[0], 0, 3, e->cap);
+    else
+        ens_copy_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active_f0, e->d_y, 3, e->d_k[0], 0, 3, e->cap);
     prof_end(e, pr);
     RG_CUDA_CHECK(cudaGetLastError());
     e->n_kernels++;
@@ -1279,6 +1342,7 @@ int record_attempt(rg_ens* e, bool in_graph)
         pa.s = e->sys();
         pa.y = e->d_y;
         pa.k0 = e->d_k[0];
+        pa.k_f2 = e->gravity_mode == RG_GRAVITY_MIXED ? 1 : 0;
         pa.mass = e->d_mass;
         pa.id = e->d_id;
         pa.base = e->d_base;
@@ -1320,8 +1384,12 @@ int record_attempt(rg_ens* e, bool in_graph)
     pr = prof_begin(e, 1);
     rc = launch_stage(e, FORM_RK8_NP1, 7, snp, bnp, e->d_yout, e->d_yout + 3 * cap);
     if (rc) return rc;
-    ens_error_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active, e->d_k[0], e->d_k[10], e->d_k[11], e->d_k[12],
-                                           e->cap, e->d_maxbits);
+    if (e->gravity_mode == RG_GRAVITY_MIXED)
+        ens_error_kernel<true><<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active, e->d_k[0], e->d_k[10], e->d_k[11],
+                                                      e->d_k[12], e->cap, e->d_maxbits);
+    else
+        ens_error_kernel<false><<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active, e->d_k[0], e->d_k[10], e->d_k[11],
+                                                       e->d_k[12], e->cap, e->d_maxbits);
     prof_end(e, pr);
     RG_CUDA_CHECK(cudaGetLastError());
     pr = prof_begin(e, 2);
@@ -1758,9 +1826,27 @@ int collect(rg_ens* e)
     return RG_OK;
 }
 
+// The stage vectors' storage follows the gravity mode (double-float pairs in the mixed form);
+// the first one outlives an attempt (a rejected attempt retries from it), so after a change of
+// mode it is converted in place before the next launch.
+int ensure_k_format(rg_ens* e)
+{
+    const int want = e->gravity_mode == RG_GRAVITY_MIXED ? 1 : 0;
+    if (e->k_f2_now == want) return RG_OK;
+    const long long n = 6LL * e->cap;
+    if (n > 0) {
+        const long long blocks = std::min<long long>((n + 255) / 256, (long long)NUM_SMS_HINT * 16);
+        k_format_kernel<<<(unsigned)blocks, 256, 0, e->st>>>(e->d_k[0], n, want);
+        RG_CUDA_CHECK(cudaGetLastError());
+    }
+    e->k_f2_now = want;
+    return RG_OK;
+}
+
 int advance_impl(rg_ens* e, double t_stop_day, int64_t max_attempts, int64_t* n_attempts)
 {
     if (!e->has_int) return set_error(RG_ERR_STATE, "no integrator set (rg_ens_set_integrator)");
+    if (int krc = ensure_k_format(e)) return krc;
     if (n_attempts) *n_attempts = 0;
     const double stop = t_stop_day * GAUSS;
     std::vector<int> status;
@@ -2120,6 +2206,7 @@ static int time_ens_evaluations(rg_ens* e, int reps, double* ms)
 // bit-exact), mixed mode sources per few-sink CTA x the row-kernel limit
 static int ens_autotune_impl(rg_ens* e, int reps, rg_tune_t* out)
 {
+    if (int krc = ensure_k_format(e)) return krc;
     struct Shape {
         int S, rowseq, chunk;
     };

@@ -148,19 +148,6 @@ __device__ __forceinline__ float light_w(float mj, float r2)
     return (mj * (y0 * s)) * t;
 }
 
-// compensated accumulation: s + c tracks the exact sum of the added terms to ~2^-46
-struct Acc2 {
-    float s, c;
-};
-
-__device__ __forceinline__ void two_sum_add(Acc2& a, float t)
-{
-    const float s = a.s + t;
-    const float bp = s - a.s;
-    const float err = (a.s - (s - bp)) + (t - bp);
-    a.s = s;
-    a.c += err;
-}
 
 __device__ __forceinline__ Acc2 two_sum_merge(Acc2 a, Acc2 b)
 {
@@ -188,6 +175,21 @@ constexpr int MX_S = 32 * MX_R;  // sinks per CTA
 static_assert(MX_S == MIXED_SINKS_PER_TILE, "tile size");
 static_assert(sizeof(SplitPos) == SPLIT_POS_BYTES, "split size");
 constexpr int MX_T = 256;        // sources per shared-memory tile
+
+// an output row element and a velocity row element in the stage vectors' format (GravArgs::
+// acc_f2, vel_f2: double-float pairs in the ensemble's mixed form, FP64 otherwise)
+__device__ __forceinline__ void store_acc(const GravArgs& g, double* row, int i, double v)
+{
+    if (g.acc_f2)
+        reinterpret_cast<float2*>(row)[i] = to_f2(v);
+    else
+        row[i] = v;
+}
+
+__device__ __forceinline__ double load_vel(const GravArgs& g, const double* row, int i)
+{
+    return g.vel_f2 ? f2_to_double(reinterpret_cast<const float2*>(row)[i]) : row[i];
+}
 
 __device__ __forceinline__ void exact_event_tests(const GravArgs& g, const Tile& tile, int i, int j, double xi,
                                                   double yi, double zi, double Ri, double mi, double rhoi)
@@ -226,10 +228,10 @@ __device__ __forceinline__ void exact_event_tests(const GravArgs& g, const Tile&
             const int b0 = tile.base;
             e->ri[0] = xi; e->ri[1] = yi; e->ri[2] = zi;
             e->rj[0] = xj; e->rj[1] = yj; e->rj[2] = zj;
-            e->vi[0] = g.vx[i]; e->vi[1] = g.vy[i]; e->vi[2] = g.vz[i];
-            e->vj[0] = g.vx[j]; e->vj[1] = g.vy[j]; e->vj[2] = g.vz[j];
+            e->vi[0] = load_vel(g, g.vx, i); e->vi[1] = load_vel(g, g.vy, i); e->vi[2] = load_vel(g, g.vz, i);
+            e->vj[0] = load_vel(g, g.vx, j); e->vj[1] = load_vel(g, g.vy, j); e->vj[2] = load_vel(g, g.vz, j);
             e->r0[0] = g.px[b0]; e->r0[1] = g.py[b0]; e->r0[2] = g.pz[b0];
-            e->v0[0] = g.vx[b0]; e->v0[1] = g.vy[b0]; e->v0[2] = g.vz[b0];
+            e->v0[0] = load_vel(g, g.vx, b0); e->v0[1] = load_vel(g, g.vy, b0); e->v0[2] = load_vel(g, g.vz, b0);
         }
     }
 }
@@ -250,12 +252,6 @@ __device__ __forceinline__ void exact_event_tests(const GravArgs& g, const Tile&
 // double-float until one conversion to FP64 per sink and component.  Event decisions are
 // screened in FP32 with the same 1e-3 margin as the mixed kernel and re-taken in FP64.
 
-// a double-float term into a compensated FP32 accumulator
-__device__ __forceinline__ void acc_df(Acc2& acc, DF t)
-{
-    two_sum_add(acc, t.hi);
-    acc.c += t.lo;
-}
 
 // the term m_j (r_j - r_i) / |r_j - r_i|^3 of one pair; r2f = |r_j - r_i|^2 in FP32
 // the term from a double-float displacement r_j - r_i and the source's split mass
@@ -802,13 +798,14 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
         if (a.partial)
             a.partial[((long long)blockIdx.y * 3 + comp) * a.n_part + i] = v;
         else
-            (comp == 0 ? g.ax : (comp == 1 ? g.ay : g.az))[i] = v;
+            store_acc(g, comp == 0 ? g.ax : (comp == 1 ? g.ay : g.az), i, v);
     }
 }
 
 // a_i = sum over source chunks of the partials, in chunk order
 __global__ void mixed_reduce_kernel(const double* __restrict__ partial, int n_chunks, int n_part, const Tile* tiles,
-                                    int n_tiles, const int* sys_active, double* ax, double* ay, double* az)
+                                    int n_tiles, const int* sys_active, double* ax, double* ay, double* az,
+                                    int acc_f2)
 {
     const Tile tile = tiles[blockIdx.x];
     if (sys_active && !sys_active[tile.sys]) return;
@@ -817,7 +814,11 @@ __global__ void mixed_reduce_kernel(const double* __restrict__ partial, int n_ch
     for (int comp = 0; comp < 3; comp++) {
         double v = 0.0;
         for (int c = 0; c < n_chunks; c++) v += partial[((long long)c * 3 + comp) * n_part + i];
-        (comp == 0 ? ax : (comp == 1 ? ay : az))[i] = v;
+        double* row = comp == 0 ? ax : (comp == 1 ? ay : az);
+        if (acc_f2)
+            reinterpret_cast<float2*>(row)[i] = to_f2(v);
+        else
+            row[i] = v;
     }
 }
 
@@ -886,9 +887,16 @@ __global__ void __launch_bounds__(DF_ROW_NT, 8) grav_df_rowseq(GravArgs g, const
         __syncthreads();
     }
     if (sink_ok) {
-        g.ax[i] = f2d_bits(ax.s) + f2d_bits(ax.c);
-        g.ay[i] = f2d_bits(ay.s) + f2d_bits(ay.c);
-        g.az[i] = f2d_bits(az.s) + f2d_bits(az.c);
+        if (g.acc_f2) {  // the compensated sums as double-float pairs, no FP64 work
+            const DF x = df_two_sum(ax.s, ax.c), y = df_two_sum(ay.s, ay.c), z = df_two_sum(az.s, az.c);
+            reinterpret_cast<float2*>(g.ax)[i] = make_float2(x.hi, x.lo);
+            reinterpret_cast<float2*>(g.ay)[i] = make_float2(y.hi, y.lo);
+            reinterpret_cast<float2*>(g.az)[i] = make_float2(z.hi, z.lo);
+        } else {
+            g.ax[i] = f2d_bits(ax.s) + f2d_bits(ax.c);
+            g.ay[i] = f2d_bits(ay.s) + f2d_bits(ay.c);
+            g.az[i] = f2d_bits(az.s) + f2d_bits(az.c);
+        }
     }
 }
 
@@ -1006,6 +1014,7 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
 }
 
 struct DfFinalArgs {
+    int acc_f2;
     const double* partial;
     int rows, row0, nrows;
     long long pitch;
@@ -1028,7 +1037,11 @@ __global__ void df_few_final(DfFinalArgs a)
     const double* P = a.partial + ((long long)comp * a.rows + row) * a.pitch;
     double s = 0.0;
     for (int c = 0; c < nch; c++) s += P[c];
-    (comp == 0 ? a.ax : (comp == 1 ? a.ay : a.az))[a.row_sink[row]] = s;
+    double* out = comp == 0 ? a.ax : (comp == 1 ? a.ay : a.az);
+    if (a.acc_f2)
+        reinterpret_cast<float2*>(out)[a.row_sink[row]] = to_f2(s);
+    else
+        out[a.row_sink[row]] = s;
 }
 
 int launch_grav_df_rowseq(const GravArgs& g, const void* split, cudaStream_t st)
@@ -1072,7 +1085,7 @@ int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row
             grav_df_few<false, FEW_SINKS_MAX><<<grid, 256, 0, st>>>(a);
     }
     RG_CUDA_CHECK(cudaGetLastError());
-    DfFinalArgs f{partial, rows, group_row0, group_rows, pitch, row_sink, row_nsrc, row_sys, g.sys_active,
+    DfFinalArgs f{g.acc_f2, partial, rows, group_row0, group_rows, pitch, row_sink, row_nsrc, row_sys, g.sys_active,
                   g.ax, g.ay, g.az, chunk};
     df_few_final<<<(3 * group_rows + 127) / 128, 128, 0, st>>>(f);
     RG_CUDA_CHECK(cudaGetLastError());
@@ -1124,7 +1137,7 @@ int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* hea
     RG_CUDA_CHECK(cudaGetLastError());
     if (n_chunks > 1) {
         mixed_reduce_kernel<<<g.n_tiles, MX_S, 0, st>>>(partial, n_chunks, n_part, g.tiles, g.n_tiles, g.sys_active,
-                                                        g.ax, g.ay, g.az);
+                                                        g.ax, g.ay, g.az, g.acc_f2);
         RG_CUDA_CHECK(cudaGetLastError());
     }
     return 0;

@@ -248,3 +248,26 @@ def test_graph_replay_equals_direct_launches(gpulib, mode):
         assert (a["n_tried_step"], a["n_passed_step"], a["t_day"]) == (b["n_tried_step"], b["n_passed_step"], b["t_day"])
     for (ea, la), (eb, lb) in zip(en_g, en_d):
         assert ea == eb and np.array_equal(la, lb)
+
+
+def test_mode_switch_keeps_the_first_stage_vector(gpulib):
+    """The mixed form keeps its stage vectors as double-float pairs and the FP64 form as FP64;
+    the first stage vector outlives a rejected attempt, so a change of gravity mode converts it
+    in place.  Dithered trial steps make rejections, and the mode changes between advances of
+    a few attempts each: the run stays finite and conserves energy as an unswitched one does."""
+    from redgb.proposer import set_dither
+    disks = [bodies.config_disk("ensemble_member", seed=s, n=600) for s in (1, 2)]
+    thr = bodies.thresholds(collision_factor=0.0)
+    ens = Ensemble(disks, thr)
+    ens.set_integrator(0.001, 1e-10)
+    set_dither(ens, 0.3, seed=11)
+    E0 = [ens.energy(s)[0] for s in range(2)]
+    for k, mode in enumerate([T.GRAVITY_MIXED, T.GRAVITY_FP64] * 6):
+        ens.set_options(gravity_mode=mode, hill_factor=3.0)
+        ens.advance(1e9, max_attempts=7 + k)
+    failed = sum(ens.stats(s)["n_failed_step"] for s in range(2))
+    assert failed > 0  # some switches came after a rejected attempt
+    for s in range(2):
+        E1 = ens.energy(s)[0]
+        assert np.isfinite(E1) and abs((E1 - E0[s]) / E0[s]) < 1e-10
+        assert ens.stats(s)["status"] == T.SYS_RUNNING
