@@ -12,8 +12,9 @@ namespace redgb {
 // The split is done on the bit patterns, with integer operations only (a conversion
 // FP64 -> FP32 runs on GB300's scarce FP64 pipe): hi = v rounded to 24 significant bits
 // (round half up on the dropped 29 bits; a carry into the exponent is the correct next
-// value), lo = the signed remainder rounded to FP32, so |v - (hi + lo)| <= 2^-48 |v| and hi
-// carries no bias.  |v| < 2^-74 gives lo = 0 and |v| < 2^-126 gives hi = lo = 0.
+// value, up to infinity), lo = the signed remainder rounded to FP32, so |v - (hi + lo)| <=
+// 2^-48 |v| and hi carries no bias.  |v| < 2^-74 gives lo = 0 and |v| < 2^-126 gives
+// hi = lo = 0; |v| >= 2^128 gives an infinite hi.
 __device__ __forceinline__ void split_bits(double v, float& hi, float& lo)
 {
     const unsigned long long b = (unsigned long long)__double_as_longlong(v);
@@ -24,12 +25,13 @@ __device__ __forceinline__ void split_bits(double v, float& hi, float& lo)
         hi = lo = 0.0f;
         return;
     }
-    if (ef >= 254) {  // at or beyond FP32's largest binade, or inf / NaN
-        hi = (float)v;
+    const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+    if (ef >= 255) {  // beyond FP32's range, or inf / NaN: built from bits (a hardware
+                      // conversion here would be evaluated for every call, on the FP64 pipe)
+        hi = __uint_as_float(sign | 0x7f800000u | (e == 2047 && mant != 0 ? 0x400000u : 0u));
         lo = 0.0f;
         return;
     }
-    const unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
     unsigned hb = sign | ((unsigned)ef << 23) | (unsigned)(mant >> 29);
     int r = (int)(mant & 0x1FFFFFFFu);  // the dropped bits, in units of 2^(e - 1075)
     if (r >= (1 << 28)) {
@@ -99,16 +101,17 @@ __device__ __forceinline__ DF df_diff(float ah, float al, float bh, float bl)
     return df_two_sum(s.hi, (al - bl) + s.lo);
 }
 
-// FP32 -> FP64 on the bit pattern (exact; no FP64-pipe conversion); FP32 denormals -> 0
+// FP32 -> FP64 on the bit pattern (exact; no FP64-pipe conversion); FP32 denormals -> 0.
+// Infinities and NaNs are built from their bits too: a hardware conversion in that branch is
+// evaluated for every call (a select, not a branch) and runs on GB300's FP64 pipe.
 __device__ __forceinline__ double f2d_bits(float f)
 {
     const unsigned u = __float_as_uint(f);
     const unsigned ef = (u >> 23) & 0xffu;
-    if (ef == 0) return 0.0;
-    if (ef == 255) return (double)f;
-    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) |
-                                 ((unsigned long long)(ef + 896u) << 52) | ((unsigned long long)(u & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)b);
+    const unsigned long long e = ef == 255u ? 0x7ffull : (unsigned long long)(ef + 896u);
+    const unsigned long long b = ((unsigned long long)(u & 0x80000000u) << 32) | (e << 52) |
+                                 ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double(ef == 0u ? 0ll : (long long)b);
 }
 
 __device__ __forceinline__ double df_to_double(DF a) { return f2d_bits(a.hi) + f2d_bits(a.lo); }

@@ -219,19 +219,20 @@ __global__ void __launch_bounds__(256) ens_error_kernel(const StageTile* tiles, 
     if (!active[t.sys]) return;
     const int nb = t.e1 - t.b0;
     double m = 0.0;
+    DF mdf{0.0f, 0.0f};  // F2: the running maximum as a normalised double-float (FP32 compares)
     for (int f = threadIdx.x; f < 6 * nb; f += blockDim.x) {
         const int row = f / nb;
         const long long e = (long long)row * stride + t.b0 + (f - row * nb);
-        double v;
         if (F2) {
-            const DF d = df_add(df_add(df_add(ldf(k0, e), ldf(k10, e)), DF{-ldf(k11, e).hi, -ldf(k11, e).lo}),
-                                DF{-ldf(k12, e).hi, -ldf(k12, e).lo});
-            v = f2d_bits(d.hi) + f2d_bits(d.lo);
+            const DF k11e = ldf(k11, e), k12e = ldf(k12, e);
+            const DF d = df_add(df_add(df_add(ldf(k0, e), ldf(k10, e)), DF{-k11e.hi, -k11e.lo}), DF{-k12e.hi, -k12e.lo});
+            if (mdf.hi < d.hi || (mdf.hi == d.hi && mdf.lo < d.lo)) mdf = d;
         } else {
-            v = (k0[e] + k10[e] - k11[e] - k12[e]);
+            const double v = (k0[e] + k10[e] - k11[e] - k12[e]);
+            if (m < v) m = v;
         }
-        if (m < v) m = v;
     }
+    if (F2) m = f2d_bits(mdf.hi) + f2d_bits(mdf.lo);  // rounding is monotone: the maximum's rounding
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         const double o = __shfl_xor_sync(0xffffffffu, m, off);

@@ -793,7 +793,7 @@ __global__ void __launch_bounds__(256, 2) grav_mixed_kernel(MixedArgs a)
         const int i = tile.sink_begin + s;
         if (i >= tile.sink_end) continue;
         double v = 0.0;
-        for (int w = 0; w < MX_WARPS; w++) v += (double)S.part[w][comp][s].s + (double)S.part[w][comp][s].c;
+        for (int w = 0; w < MX_WARPS; w++) v += f2d_bits(S.part[w][comp][s].s) + f2d_bits(S.part[w][comp][s].c);
         if (!(0 < g.id[i])) v = 0.0;  // inactive sinks feel nothing (pp_disk.cu:235-236)
         if (a.partial)
             a.partial[((long long)blockIdx.y * 3 + comp) * a.n_part + i] = v;
