@@ -116,26 +116,26 @@ __global__ void __launch_bounds__(256) ens_combine_kernel(EnsStageArgs a)
 // next stage vector's rows 0-2) as double-float; y_{n+1}: FP64.
 __device__ __forceinline__ DF ldf(const double* k, long long e)
 {
-    const float2 f = reinterpret_cast<const float2*>(k)[e];
+    const float2 f = __ldg(reinterpret_cast<const float2*>(k) + e);  // read-only for the kernel
     return DF{f.x, f.y};
 }
 
 template <int FORM, int NTERM>
-__device__ __forceinline__ double ens_combine_df(const EnsStageArgs& a, const DF* w, long long e)
+__device__ __forceinline__ double ens_combine_df_sum(const DF* w, const DF* k, double y)
 {
     DF sum;
     if (FORM == FORM_SUM) {
-        sum = df_mul(w[0], ldf(a.k[0], e));
+        sum = df_mul(w[0], k[0]);
 #pragma unroll
-        for (int q = 1; q < NTERM; q++) sum = df_add(sum, df_mul(w[q], ldf(a.k[q], e)));
+        for (int q = 1; q < NTERM; q++) sum = df_add(sum, df_mul(w[q], k[q]));
     } else {
-        sum = df_mul(w[0], ldf(a.k[0], e));
-        sum = df_add(sum, df_mul(w[1], ldf(a.k[1], e)));
-        sum = df_add(sum, df_mul(w[2], df_add(ldf(a.k[2], e), ldf(a.k[3], e))));
-        sum = df_add(sum, df_mul(w[3], df_add(ldf(a.k[4], e), ldf(a.k[5], e))));
-        sum = df_add(sum, df_mul(w[4], ldf(a.k[6], e)));
+        sum = df_mul(w[0], k[0]);
+        sum = df_add(sum, df_mul(w[1], k[1]));
+        sum = df_add(sum, df_mul(w[2], df_add(k[2], k[3])));
+        sum = df_add(sum, df_mul(w[3], df_add(k[4], k[5])));
+        sum = df_add(sum, df_mul(w[4], k[6]));
     }
-    return a.y[e] + (f2d_bits(sum.hi) + f2d_bits(sum.lo));
+    return y + (f2d_bits(sum.hi) + f2d_bits(sum.lo));
 }
 
 template <int FORM, int NTERM>
@@ -145,6 +145,10 @@ __global__ void __launch_bounds__(256) ens_combine_df_kernel(EnsStageArgs a)
     if (!a.active[t.sys]) return;
     const double dt = a.dt[t.sys];
     constexpr int NW = FORM == FORM_SUM ? NTERM : 5;  // the coefficients the form reads
+    constexpr int NL = FORM == FORM_SUM ? NTERM : 7;  // the stage vectors it reads
+    // elements per thread and iteration, all their loads issued before any arithmetic (the
+    // kernel is bound by memory latency otherwise): about 40 loaded registers
+    constexpr int U = NL <= 4 ? 4 : (NL <= 8 ? 2 : 1);
     DF w[MAXT];
 #pragma unroll
     for (int q = 0; q < NW; q++) w[q] = split_df(dt * a.c[q]);
@@ -153,16 +157,26 @@ __global__ void __launch_bounds__(256) ens_combine_df_kernel(EnsStageArgs a)
         const long long base = (long long)row * a.stride + t.b0;
         const bool f2 = FORM == FORM_SUM && row >= 3;  // the next stage vector's velocity rows
         double* out = row < 3 ? a.out_lo + base : a.out_hi + base - 3LL * a.stride;
-        for (int i = threadIdx.x; i < nb; i += 2 * blockDim.x) {
-            const int i2 = i + blockDim.x;
-            const double o1 = ens_combine_df<FORM, NTERM>(a, w, base + i);
-            const double o2 = i2 < nb ? ens_combine_df<FORM, NTERM>(a, w, base + i2) : 0.0;
-            if (f2) {
-                reinterpret_cast<float2*>(out)[i] = to_f2(o1);
-                if (i2 < nb) reinterpret_cast<float2*>(out)[i2] = to_f2(o2);
-            } else {
-                out[i] = o1;
-                if (i2 < nb) out[i2] = o2;
+        for (int i = threadIdx.x; i < nb; i += U * blockDim.x) {
+            DF kv[U][NL];
+            double yv[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int iu = min(i + u * (int)blockDim.x, nb - 1);  // in range; excess lanes repeat the last
+                yv[u] = __ldg(a.y + base + iu);
+#pragma unroll
+                for (int q = 0; q < NL; q++) kv[u][q] = ldf(a.k[q], base + iu);
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int iu = i + u * blockDim.x;
+                if (iu < nb) {
+                    const double o = ens_combine_df_sum<FORM, NTERM>(w, kv[u], yv[u]);
+                    if (f2)
+                        reinterpret_cast<float2*>(out)[iu] = to_f2(o);
+                    else
+                        out[iu] = o;
+                }
             }
         }
     }
