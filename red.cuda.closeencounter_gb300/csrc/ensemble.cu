@@ -147,8 +147,8 @@ __global__ void __launch_bounds__(256) ens_combine_df_kernel(EnsStageArgs a)
     constexpr int NW = FORM == FORM_SUM ? NTERM : 5;  // the coefficients the form reads
     constexpr int NL = FORM == FORM_SUM ? NTERM : 7;  // the stage vectors it reads
     // elements per thread and iteration, all their loads issued before any arithmetic (the
-    // kernel is bound by memory latency otherwise): about 40 loaded registers
-    constexpr int U = NL <= 4 ? 4 : (NL <= 8 ? 2 : 1);
+    // kernel is bound by memory latency otherwise): 20-40 loaded registers
+    constexpr int U = NL <= 4 ? 4 : 2;
     DF w[MAXT];
 #pragma unroll
     for (int q = 0; q < NW; q++) w[q] = split_df(dt * a.c[q]);
@@ -214,10 +214,22 @@ __global__ void ens_copy_kernel(const StageTile* tiles, const int* mask, const d
     const StageTile t = tiles[blockIdx.x];
     if (!mask[t.sys]) return;
     const int nb = t.b1 - t.b0;
-    for (int f = threadIdx.x; f < nr * nb; f += blockDim.x) {
-        const int row = f / nb;
-        const long long o = (long long)t.b0 + (f - row * nb);
-        dst[(long long)(d0 + row) * stride + o] = src[(long long)(r0 + row) * stride + o];
+    // four elements per thread and iteration, loads first (the copy is bound by memory latency)
+    constexpr int U = 4;
+    for (int f0 = threadIdx.x; f0 < nr * nb; f0 += U * blockDim.x) {
+        double v[U];
+        long long o[U];
+        int row[U];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int f = min(f0 + u * (int)blockDim.x, nr * nb - 1);
+            row[u] = f / nb;
+            o[u] = (long long)t.b0 + (f - row[u] * nb);
+            v[u] = __ldg(src + (long long)(r0 + row[u]) * stride + o[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++)
+            if (f0 + u * (int)blockDim.x < nr * nb) dst[(long long)(d0 + row[u]) * stride + o[u]] = v[u];
     }
 }
 
@@ -234,14 +246,32 @@ __global__ void __launch_bounds__(256) ens_error_kernel(const StageTile* tiles, 
     const int nb = t.e1 - t.b0;
     double m = 0.0;
     DF mdf{0.0f, 0.0f};  // F2: the running maximum as a normalised double-float (FP32 compares)
-    for (int f = threadIdx.x; f < 6 * nb; f += blockDim.x) {
-        const int row = f / nb;
-        const long long e = (long long)row * stride + t.b0 + (f - row * nb);
-        if (F2) {
-            const DF k11e = ldf(k11, e), k12e = ldf(k12, e);
-            const DF d = df_add(df_add(df_add(ldf(k0, e), ldf(k10, e)), DF{-k11e.hi, -k11e.lo}), DF{-k12e.hi, -k12e.lo});
-            if (mdf.hi < d.hi || (mdf.hi == d.hi && mdf.lo < d.lo)) mdf = d;
-        } else {
+    if (F2) {
+        // four elements per thread and iteration, their loads first (bound by memory latency)
+        constexpr int U = 4;
+        for (int f0 = threadIdx.x; f0 < 6 * nb; f0 += U * blockDim.x) {
+            DF kv[U][4];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const int f = min(f0 + u * (int)blockDim.x, 6 * nb - 1);  // excess lanes repeat the last
+                const int row = f / nb;
+                const long long e = (long long)row * stride + t.b0 + (f - row * nb);
+                kv[u][0] = ldf(k0, e);
+                kv[u][1] = ldf(k10, e);
+                kv[u][2] = ldf(k11, e);
+                kv[u][3] = ldf(k12, e);
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const DF d = df_add(df_add(df_add(kv[u][0], kv[u][1]), DF{-kv[u][2].hi, -kv[u][2].lo}),
+                                    DF{-kv[u][3].hi, -kv[u][3].lo});
+                if (mdf.hi < d.hi || (mdf.hi == d.hi && mdf.lo < d.lo)) mdf = d;
+            }
+        }
+    } else {
+        for (int f = threadIdx.x; f < 6 * nb; f += blockDim.x) {
+            const int row = f / nb;
+            const long long e = (long long)row * stride + t.b0 + (f - row * nb);
             const double v = (k0[e] + k10[e] - k11[e] - k12[e]);
             if (m < v) m = v;
         }
@@ -1138,9 +1168,14 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
     const auto& plan = e->plan[e->gravity_mode == RG_GRAVITY_MIXED ? 1 : 0];
     bool split_done = false;
     if (e->gravity_mode == RG_GRAVITY_MIXED && !plan.empty()) {
-        rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->d_base_of, e->d_screen_slot, e->d_radius,
-                                    e->cap, (SplitPos*)e->d_split, e->d_rf, g.smax ? e->d_smax : nullptr, g.hill != 0,
-                                    e->st);
+        // a later stage of the attempt needs only the coordinates split again: the step start's
+        // split wrote the masses and radii, which change only at events (after the attempt)
+        if (stage > 0 && !g.smax)
+            rc = launch_split_coords(g.px, g.py, g.pz, e->cap, (SplitPos*)e->d_split, e->st);
+        else
+            rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->d_base_of, e->d_screen_slot,
+                                        e->d_radius, e->cap, (SplitPos*)e->d_split, e->d_rf,
+                                        g.smax ? e->d_smax : nullptr, g.hill != 0, e->st);
         split_done = true;
         e->n_kernels++;
         if (rc) return rc;

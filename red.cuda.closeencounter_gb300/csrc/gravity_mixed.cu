@@ -1092,6 +1092,30 @@ int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row
     return 0;
 }
 
+// the coordinates alone of a later stage (the masses, radii and ids change only at events, and
+// the step start's split has written them): 24 B read and written per body instead of 80
+__global__ void split_coords_kernel(const double* __restrict__ x, const double* __restrict__ y,
+                                    const double* __restrict__ z, int n, SplitPos* __restrict__ out)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 xy;
+    float2 zz;
+    split_coord(x[i], xy.x, xy.y);
+    split_coord(y[i], xy.z, xy.w);
+    split_coord(z[i], zz.x, zz.y);
+    out[i].xy = xy;
+    *reinterpret_cast<float2*>(&out[i].zm) = zz;
+}
+
+int launch_split_coords(const double* x, const double* y, const double* z, int n, SplitPos* out, cudaStream_t st)
+{
+    if (n <= 0) return 0;
+    split_coords_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, n, out);
+    RG_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
 int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id,
                            const int* base_of, const int* screen_slot, const double* radius, int n,
                            SplitPos* out, float* rf, unsigned int* smax, bool hill, cudaStream_t st)

@@ -88,6 +88,7 @@ struct SplitPos;
 constexpr int MIXED_SINKS_PER_TILE = 128;
 constexpr int MIXED_SOURCE_TILE = 256;  // source-chunk lengths are multiples of this
 constexpr size_t SPLIT_POS_BYTES = 32;  // per body
+int launch_split_coords(const double* x, const double* y, const double* z, int n, SplitPos* out, cudaStream_t st);
 int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id,
                            const int* base_of, const int* screen_slot, const double* radius, int n,
                            SplitPos* out, float* rf, unsigned int* smax, bool hill, cudaStream_t st);
