@@ -993,13 +993,15 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
         if (s < ns) {  // uniform over the CTA
 #pragma unroll
             for (int c = 0; c < 3; c++) {
-                DF v = df_two_sum(acc[s][c].s, acc[s][c].c);
+                // the warp's compensated sums merged pairwise (a two-sum of the leading parts
+                // and one addition of the corrections: a third of a double-float addition)
+                Acc2 v = acc[s][c];
 #pragma unroll
                 for (int off = 16; off > 0; off >>= 1) {
-                    const DF o{__shfl_xor_sync(0xffffffffu, v.hi, off), __shfl_xor_sync(0xffffffffu, v.lo, off)};
-                    v = df_add(v, o);
+                    const Acc2 o{__shfl_xor_sync(0xffffffffu, v.s, off), __shfl_xor_sync(0xffffffffu, v.c, off)};
+                    v = two_sum_merge(v, o);
                 }
-                if (lane == 0) s_red[warp][3 * s + c] = v;
+                if (lane == 0) s_red[warp][3 * s + c] = df_two_sum(v.s, v.c);
             }
         }
     }
