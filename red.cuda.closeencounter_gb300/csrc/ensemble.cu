@@ -63,6 +63,9 @@ struct EnsStageArgs {
     int stride;
     double* out_lo;       // rows 0..2
     double* out_hi;       // rows 3..5
+    // y_{n+1} in the mixed form: also the error norm's signed maximum (k[7] = k11, k[8] = k12;
+    // the error reads k0 = k[0] and k10 = k[6]), per disk into max_bits; nullptr: none
+    unsigned long long* max_bits;
 };
 
 // FORM_SUM (stage rows) or FORM_RK8_NP1 (y_{n+1}), one CTA per stage tile, in the
@@ -145,7 +148,8 @@ __global__ void __launch_bounds__(256) ens_combine_df_kernel(EnsStageArgs a)
     if (!a.active[t.sys]) return;
     const double dt = a.dt[t.sys];
     constexpr int NW = FORM == FORM_SUM ? NTERM : 5;  // the coefficients the form reads
-    constexpr int NL = FORM == FORM_SUM ? NTERM : 7;  // the stage vectors it reads
+    constexpr bool NP1 = FORM == FORM_RK8_NP1;
+    constexpr int NL = FORM == FORM_SUM ? NTERM : 9;  // the stage vectors it reads (y_{n+1}: + error)
     // elements per thread and iteration, all their loads issued before any arithmetic (the
     // kernel is bound by memory latency otherwise): 20-40 loaded registers
     constexpr int U = NL <= 4 ? 4 : 2;
@@ -153,6 +157,8 @@ __global__ void __launch_bounds__(256) ens_combine_df_kernel(EnsStageArgs a)
 #pragma unroll
     for (int q = 0; q < NW; q++) w[q] = split_df(dt * a.c[q]);
     const int nb = t.b1 - t.b0;
+    const int ne = t.e1 - t.b0;  // y_{n+1}: the elements the error norm covers
+    DF mdf{0.0f, 0.0f};          // the error's running maximum (normalised double-float)
     for (int row = 0; row < 6; row++) {
         const long long base = (long long)row * a.stride + t.b0;
         const bool f2 = FORM == FORM_SUM && row >= 3;  // the next stage vector's velocity rows
@@ -176,8 +182,34 @@ __global__ void __launch_bounds__(256) ens_combine_df_kernel(EnsStageArgs a)
                         reinterpret_cast<float2*>(out)[iu] = to_f2(o);
                     else
                         out[iu] = o;
+                    if (NP1 && iu < ne) {  // e = ((k0 + k10) - k11) - k12 (integrator.cu:240-255)
+                        const DF d = df_add(df_add(df_add(kv[u][0], kv[u][6]), DF{-kv[u][7].hi, -kv[u][7].lo}),
+                                            DF{-kv[u][8].hi, -kv[u][8].lo});
+                        if (mdf.hi < d.hi || (mdf.hi == d.hi && mdf.lo < d.lo)) mdf = d;
+                    }
                 }
             }
+        }
+    }
+    if (NP1) {  // the CTA's signed maximum (starting at 0) into the disk's word
+        double m = f2d_bits(mdf.hi) + f2d_bits(mdf.lo);  // rounding is monotone
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+            const double o = __shfl_xor_sync(0xffffffffu, m, off);
+            if (m < o) m = o;
+        }
+        __shared__ double wmax[8];
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        if (lane == 0) wmax[warp] = m;
+        __syncthreads();
+        if (warp == 0) {
+            m = lane < (int)(blockDim.x >> 5) ? wmax[lane] : 0.0;
+#pragma unroll
+            for (int off = 4; off > 0; off >>= 1) {
+                const double o = __shfl_xor_sync(0xffffffffu, m, off);
+                if (m < o) m = o;
+            }
+            if (lane == 0 && m > 0.0) atomicMax(&a.max_bits[t.sys], (unsigned long long)__double_as_longlong(m));
         }
     }
 }
@@ -234,9 +266,6 @@ __global__ void ens_copy_kernel(const StageTile* tiles, const int* mask, const d
 }
 
 // e = ((k0 + k10) - k11) - k12, signed maximum starting at 0 (integrator.cu:240-255)
-// F2: the stage vectors are double-float pairs (the mixed form): the same sum in double-float,
-// rounded to FP64 once
-template <bool F2>
 __global__ void __launch_bounds__(256) ens_error_kernel(const StageTile* tiles, const int* active, const double* k0,
                                                         const double* k10, const double* k11, const double* k12,
                                                         int stride, unsigned long long* max_bits)
@@ -245,38 +274,12 @@ __global__ void __launch_bounds__(256) ens_error_kernel(const StageTile* tiles, 
     if (!active[t.sys]) return;
     const int nb = t.e1 - t.b0;
     double m = 0.0;
-    DF mdf{0.0f, 0.0f};  // F2: the running maximum as a normalised double-float (FP32 compares)
-    if (F2) {
-        // four elements per thread and iteration, their loads first (bound by memory latency)
-        constexpr int U = 4;
-        for (int f0 = threadIdx.x; f0 < 6 * nb; f0 += U * blockDim.x) {
-            DF kv[U][4];
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-                const int f = min(f0 + u * (int)blockDim.x, 6 * nb - 1);  // excess lanes repeat the last
-                const int row = f / nb;
-                const long long e = (long long)row * stride + t.b0 + (f - row * nb);
-                kv[u][0] = ldf(k0, e);
-                kv[u][1] = ldf(k10, e);
-                kv[u][2] = ldf(k11, e);
-                kv[u][3] = ldf(k12, e);
-            }
-#pragma unroll
-            for (int u = 0; u < U; u++) {
-                const DF d = df_add(df_add(df_add(kv[u][0], kv[u][1]), DF{-kv[u][2].hi, -kv[u][2].lo}),
-                                    DF{-kv[u][3].hi, -kv[u][3].lo});
-                if (mdf.hi < d.hi || (mdf.hi == d.hi && mdf.lo < d.lo)) mdf = d;
-            }
-        }
-    } else {
-        for (int f = threadIdx.x; f < 6 * nb; f += blockDim.x) {
-            const int row = f / nb;
-            const long long e = (long long)row * stride + t.b0 + (f - row * nb);
-            const double v = (k0[e] + k10[e] - k11[e] - k12[e]);
-            if (m < v) m = v;
-        }
+    for (int f = threadIdx.x; f < 6 * nb; f += blockDim.x) {
+        const int row = f / nb;
+        const long long e = (long long)row * stride + t.b0 + (f - row * nb);
+        const double v = (k0[e] + k10[e] - k11[e] - k12[e]);
+        if (m < v) m = v;
     }
-    if (F2) m = f2d_bits(mdf.hi) + f2d_bits(mdf.lo);  // rounding is monotone: the maximum's rounding
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
         const double o = __shfl_xor_sync(0xffffffffu, m, off);
@@ -1268,6 +1271,12 @@ int launch_stage(rg_ens* e, int form, int nterm, const int* stages, const double
     a.stride = e->cap;
     a.out_lo = out_lo;
     a.out_hi = out_hi;
+    a.max_bits = nullptr;
+    if (form == FORM_RK8_NP1 && e->gravity_mode == RG_GRAVITY_MIXED) {  // the error norm folded in
+        a.k[7] = e->d_k[11];
+        a.k[8] = e->d_k[12];
+        a.max_bits = e->d_maxbits;
+    }
     const int g = (int)e->stiles.size();
     if (g <= 0) return RG_OK;
     const bool df = e->gravity_mode == RG_GRAVITY_MIXED;  // double-float stage vectors
@@ -1434,12 +1443,9 @@ int record_attempt(rg_ens* e, bool in_graph)
     pr = prof_begin(e, 1);
     rc = launch_stage(e, FORM_RK8_NP1, 7, snp, bnp, e->d_yout, e->d_yout + 3 * cap);
     if (rc) return rc;
-    if (e->gravity_mode == RG_GRAVITY_MIXED)
-        ens_error_kernel<true><<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active, e->d_k[0], e->d_k[10], e->d_k[11],
-                                                      e->d_k[12], e->cap, e->d_maxbits);
-    else
-        ens_error_kernel<false><<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active, e->d_k[0], e->d_k[10], e->d_k[11],
-                                                       e->d_k[12], e->cap, e->d_maxbits);
+    if (e->gravity_mode != RG_GRAVITY_MIXED)  // the mixed form's y_{n+1} kernel takes the error norm too
+        ens_error_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_active, e->d_k[0], e->d_k[10], e->d_k[11],
+                                                e->d_k[12], e->cap, e->d_maxbits);
     prof_end(e, pr);
     RG_CUDA_CHECK(cudaGetLastError());
     pr = prof_begin(e, 2);
@@ -1457,7 +1463,7 @@ int record_attempt(rg_ens* e, bool in_graph)
     if (!rc) rc = launch_ens_loop(loop_args(e, in_graph), e->st);
     prof_end(e, pr);
     if (rc) return rc;
-    e->n_kernels += 7;
+    e->n_kernels += e->gravity_mode == RG_GRAVITY_MIXED ? 6 : 7;  // (error norm,) controller ... loop
     return RG_OK;
 }
 
