@@ -21,7 +21,8 @@ namespace redgb {
 struct Tile {
     int sink_begin, sink_end;
     int src_begin, src_end;
-    int sys, base, block, pad;
+    int sys, base, block;
+    int part;  // a symmetric heavy-light tile (grav_df_sym): its part of the heavy rows, from 1; else 0
 };
 
 // A collision / close-encounter / Hill-sphere candidate found by a gravity kernel.

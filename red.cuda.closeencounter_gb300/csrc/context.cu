@@ -20,6 +20,7 @@
 #include "common.cuh"
 #include "host_tools.h"
 #include "kernels.h"
+#include "plan_tools.h"
 #include "rk_tables.h"
 
 namespace redgb {
@@ -81,6 +82,10 @@ struct rg_ctx {
     unsigned int* d_ev_count = nullptr;    // d_counters + 0
     unsigned int* d_hill_count = nullptr;  // d_counters + 1
     unsigned int* d_kerr = nullptr;        // d_counters + 2
+    unsigned int* d_sym_ticket = nullptr;  // d_counters + 3: the symmetric kernel's last-segment ticket
+    std::vector<int> sym_cta;              // the symmetric kernel's CTAs: first segments (+ end)
+    int* d_sym_cta = nullptr;
+    int sym_cta_cap = 0;
     unsigned int ev_cap = 0;
     EjectRec* d_ej = nullptr;
     unsigned int* d_ej_count = nullptr;
@@ -143,6 +148,7 @@ struct rg_ctx {
     std::vector<int> screen_slot;  // per body: 0 light, -1 heavy (the mixed kernels' screen cutoffs)
     std::vector<int> few_row0, few_nsrc;  // per tile (few-sink groups)
     std::vector<int> row_sink, row_nsrc;  // per terms-buffer row
+    std::vector<int> row_nparts;          // per terms-buffer row: parts of a symmetric heavy row (else 0)
     int few_rows = 0;
     long long few_pitch = 0;
     double* d_terms = nullptr;
@@ -152,6 +158,7 @@ struct rg_ctx {
     int n_sm = 152;
     int* d_row_sink = nullptr;
     int* d_row_nsrc = nullptr;
+    int* d_row_nparts = nullptr;
     int rows_cap = 0;
     int* d_few_row0 = nullptr;  // per tile
     int64_t pairs_per_eval = 0;
@@ -216,6 +223,8 @@ void free_all(rg_ctx* c)
     cudaFree(c->d_partial);
     cudaFree(c->d_row_sink);
     cudaFree(c->d_row_nsrc);
+    cudaFree(c->d_row_nparts);
+    cudaFree(c->d_sym_cta);
     cudaFree(c->d_few_row0);
     cudaFree(c->d_ev);
     cudaFree(c->d_hill);
@@ -345,7 +354,11 @@ enum {
     GROUP_MIXED = 3,
     GROUP_DF_ROWSEQ = 4,  // mixed mode: the row kernel in double-float arithmetic
     GROUP_DF_FEW = 5,     // mixed mode: few heavy sinks in double-float arithmetic
+    GROUP_DF_SYM = 6,     // mixed mode: heavy-light pairs once for both rows (grav_df_sym)
 };
+// light bodies per symmetric tile of one disk, about: one per thread of a 256-thread CTA up to
+// a wave of resident CTAs, so that a disk of a thousand bodies spreads over several SMs (the
+// evaluation's latency is one tile's)
 constexpr int FEW_BLOCK_SINKS = 32;  // blocks with at most this many sinks use the few-sink path
 
 // CTA tiles of the interaction matrix (number_of_bodies::get_bound_SI/NSI/NI,
@@ -358,6 +371,7 @@ void build_tiles(rg_ctx* c)
     c->few_nsrc.clear();
     c->row_sink.clear();
     c->row_nsrc.clear();
+    c->row_nparts.clear();
     c->few_rows = 0;
     c->few_pitch = 0;
     const int nsi = c->n_si(), nm = c->n_massive(), nt = c->n_total();
@@ -377,6 +391,14 @@ void build_tiles(rg_ctx* c)
         c->pairs_per_eval = nsi > 1 ? (int64_t)(nsi - 1) * (nm - 2) : 0;
     }
 
+    // mixed plan: with a few heavy SI bodies (a few-sink block over every massive body) and an
+    // NSI block on the row kernel over them, the pairs between the blocks are evaluated once
+    // for both rows (grav_df_sym, the heavy-heavy pairs with them): the light bodies in
+    // balanced tiles, each one part of the heavy rows
+    const bool sym = !src0 && nsi >= 1 && nsi <= DF_SYM_MAX_HEAVY && nm > nsi && nsi <= c->rowseq_max_src &&
+                     nm > c->rowseq_max_src && nsi <= FEW_BLOCK_SINKS;
+    const int sym_ctas = sym ? std::min((nm - nsi + DF_SYM_PASS - 1) / DF_SYM_PASS, DF_SYM_RESIDENT * c->n_sm) : 0;
+    c->sym_cta.clear();
     auto add_group = [&](int mode, int kind, int s0, int s1, int src1, int block, int step) {
         if (s1 <= s0) return;
         rg_ctx::Group gr{kind, c->tiles.size(), 0, c->few_rows, 0, src1, std::min(step, s1 - s0)};
@@ -389,6 +411,7 @@ void build_tiles(rg_ctx* c)
                 for (int i = s; i < std::min(s + step, s1); i++) {
                     c->row_sink.push_back(i);
                     c->row_nsrc.push_back(src1);
+                    c->row_nparts.push_back(0);
                     c->few_rows++;
                     gr.rows++;
                 }
@@ -415,14 +438,39 @@ void build_tiles(rg_ctx* c)
             // serial pair terms are latency-bound, so more SMs beat fuller CTAs)
             const int rs_step = ns >= 2 * 128 * c->n_sm ? 128 : (ns >= 2 * 64 * c->n_sm ? 64 : 32);
             add_group(0, GROUP_ROWSEQ, b.s0, b.s1, b.src1, b.block, rs_step);
-            c->plan[1].push_back(c->plan[0].back());
-            c->plan[1].back().kind = GROUP_DF_ROWSEQ;
+            if (sym && b.block == 1) {  // the heavy rows [0, nsi), then one segment per CTA (Tile::part from 1)
+                const size_t t0 = c->tiles.size();
+                std::vector<int> parts;
+                build_sym_segments({Tile{b.s0, b.s1, 0, nsi, 0, 0, b.block, 0}}, sym_ctas, DF_SYM_PASS,
+                                   DF_SYM_SEGMENT_COST, c->tiles, c->sym_cta, parts);
+                const int nseg = (int)(c->tiles.size() - t0);
+                rg_ctx::Group gr{GROUP_DF_SYM, t0, nseg, c->few_rows, nsi, nsi, 0};
+                const int row0 = c->few_rows;
+                for (int h = 0; h < nsi; h++) {
+                    c->row_sink.push_back(h);
+                    c->row_nsrc.push_back(nm);
+                    c->row_nparts.push_back(parts[0]);
+                    c->few_rows++;
+                }
+                c->few_pitch = std::max<long long>(c->few_pitch, parts[0]);
+                for (int k = 0; k < nseg; k++) {
+                    c->heavy_mx.push_back(0);
+                    c->few_row0.push_back(row0);
+                    c->few_nsrc.push_back(0);
+                }
+                c->plan[1].push_back(gr);
+            } else {
+                c->plan[1].push_back(c->plan[0].back());
+                c->plan[1].back().kind = GROUP_DF_ROWSEQ;
+            }
             continue;
         }
         if (ns <= FEW_BLOCK_SINKS) {  // few sinks, many sources: exact serial row sums (same rows)
             add_group(0, GROUP_FEW_SERIAL, b.s0, b.s1, b.src1, b.block, FEW_SINKS_MAX);
-            c->plan[1].push_back(c->plan[0].back());
-            c->plan[1].back().kind = GROUP_DF_FEW;
+            if (!(sym && b.block == 0)) {  // a symmetric plan's heavy rows come with its tiles
+                c->plan[1].push_back(c->plan[0].back());
+                c->plan[1].back().kind = GROUP_DF_FEW;
+            }
             continue;
         }
         add_group(0, GROUP_PAIRPAR, b.s0, b.s1, b.src1, b.block, c->pairpar_S);
@@ -463,12 +511,24 @@ int sync_tiles(rg_ctx* c)
     if (c->few_rows > c->rows_cap) {
         cudaFree(c->d_row_sink);
         cudaFree(c->d_row_nsrc);
-        c->d_row_sink = c->d_row_nsrc = nullptr;
+        cudaFree(c->d_row_nparts);
+        c->d_row_sink = c->d_row_nsrc = c->d_row_nparts = nullptr;
         int rc = dalloc(&c->d_row_sink, (size_t)c->few_rows);
         if (!rc) rc = dalloc(&c->d_row_nsrc, (size_t)c->few_rows);
+        if (!rc) rc = dalloc(&c->d_row_nparts, (size_t)c->few_rows);
         if (rc) return rc;
         c->rows_cap = c->few_rows;
     }
+    if ((int)c->sym_cta.size() > c->sym_cta_cap) {
+        cudaFree(c->d_sym_cta);
+        c->d_sym_cta = nullptr;
+        int rc = dalloc(&c->d_sym_cta, c->sym_cta.size());
+        if (rc) return rc;
+        c->sym_cta_cap = (int)c->sym_cta.size();
+    }
+    if (!c->sym_cta.empty())
+        RG_CUDA_CHECK(cudaMemcpyAsync(c->d_sym_cta, c->sym_cta.data(), c->sym_cta.size() * sizeof(int),
+                                      cudaMemcpyHostToDevice, c->st));
     if (n > 0) {
         RG_CUDA_CHECK(cudaMemcpyAsync(c->d_tiles, c->tiles.data(), n * sizeof(Tile), cudaMemcpyHostToDevice, c->st));
         RG_CUDA_CHECK(cudaMemcpyAsync(c->d_heavy, c->heavy_mx.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->st));
@@ -481,6 +541,8 @@ int sync_tiles(rg_ctx* c)
         RG_CUDA_CHECK(cudaMemcpyAsync(c->d_row_sink, c->row_sink.data(), c->few_rows * sizeof(int),
                                       cudaMemcpyHostToDevice, c->st));
         RG_CUDA_CHECK(cudaMemcpyAsync(c->d_row_nsrc, c->row_nsrc.data(), c->few_rows * sizeof(int),
+                                      cudaMemcpyHostToDevice, c->st));
+        RG_CUDA_CHECK(cudaMemcpyAsync(c->d_row_nparts, c->row_nparts.data(), c->few_rows * sizeof(int),
                                       cudaMemcpyHostToDevice, c->st));
     }
     RG_CUDA_CHECK(cudaStreamSynchronize(c->st));
@@ -557,7 +619,8 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
     // side stream beside it: they write other rows and append events atomically
     bool fork = false;
     if (c->gravity_mode == RG_GRAVITY_MIXED && mixed_tiles)
-        for (const auto& gr : c->plan[1]) fork = fork || gr.kind == GROUP_DF_ROWSEQ || gr.kind == GROUP_DF_FEW;
+        for (const auto& gr : c->plan[1])
+            fork = fork || gr.kind == GROUP_DF_ROWSEQ || gr.kind == GROUP_DF_FEW || gr.kind == GROUP_DF_SYM;
     if (fork) {
         rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, nullptr, c->d_screen_slot, c->d_radius,
                                     c->n_total(), (SplitPos*)c->d_split, c->d_rf, g.smax ? c->d_smax : nullptr,
@@ -620,6 +683,20 @@ int gravity(rg_ctx* c, const double* pos, const double* vel, double* acc, int st
                                         row_st);
                 c->n_kernels += 2;
             }
+            break;
+        case GROUP_DF_SYM:
+            if (!split_done) {
+                rc = launch_split_positions(g.px, g.py, g.pz, c->d_mass, c->d_id, nullptr, c->d_screen_slot,
+                                            c->d_radius, c->n_total(), (SplitPos*)c->d_split, c->d_rf,
+                                            g.smax ? c->d_smax : nullptr, g.hill != 0, c->st);
+                split_done = true;
+                c->n_kernels++;
+            }
+            if (!rc)
+                rc = launch_grav_df_sym(g, c->d_sym_cta, (int)c->sym_cta.size() - 1, c->d_split,
+                                        c->d_few_row0 + gr.off, gr.max_src, c->d_terms, c->few_rows, c->few_pitch,
+                                        c->d_row_sink, c->d_row_nparts, c->d_sym_ticket, row_st);
+            c->n_kernels++;
             break;
         case GROUP_MIXED:
             if (!split_done) {
@@ -1542,6 +1619,7 @@ static int create_impl(const rg_counts_t* n, const rg_vec_t* r, const rg_vec_t* 
         c->d_ev_count = c->d_counters;
         c->d_hill_count = c->d_counters + 1;
         c->d_kerr = c->d_counters + 2;
+        c->d_sym_ticket = c->d_counters + 3;
     }
     if (!rc && cudaMemsetAsync(c->d_counters, 0, 4 * sizeof(unsigned int), c->st) != cudaSuccess)
         chk(set_error(RG_ERR_CUDA, "cudaMemsetAsync"));

@@ -154,5 +154,19 @@ __device__ __forceinline__ float2 to_f2(double v)
 
 __device__ __forceinline__ double f2_to_double(float2 f) { return f2d_bits(f.x) + f2d_bits(f.y); }
 
+// a coordinate split for the mixed gravity kernels' 32-byte body records (x, y, z, m as
+// float2 pairs #0..#3).  Coordinates beyond 1e15 AU are clamped there (a merged body is
+// parked at 1e20 AU, pp_disk.cu:1184, and a hit-star merger stays active with m = 0 until
+// the next ejection check): |r|^2 then stays finite in FP32, so the pair loops need no clamp,
+// and such a body's zero mass gives a zero term.
+__device__ __forceinline__ void split_coord(double v, float& hi, float& lo)
+{
+    split_bits(v, hi, lo);
+    if (fabsf(hi) > 1.0e15f) {
+        hi = copysignf(1.0e15f, hi);
+        lo = 0.0f;
+    }
+}
+
 
 }  // namespace redgb

@@ -38,6 +38,7 @@
 #include "ens_events.h"
 #include "host_tools.h"
 #include "kernels.h"
+#include "plan_tools.h"
 #include "rk_tables.h"
 #include "mlp.h"
 #include <cuda_bf16.h>
@@ -182,6 +183,7 @@ __global__ void __launch_bounds__(256) ens_combine_df_kernel(EnsStageArgs a)
                         reinterpret_cast<float2*>(out)[iu] = to_f2(o);
                     else
                         out[iu] = o;
+
                     if (NP1 && iu < ne) {  // e = ((k0 + k10) - k11) - k12 (integrator.cu:240-255)
                         const DF d = df_add(df_add(df_add(kv[u][0], kv[u][6]), DF{-kv[u][7].hi, -kv[u][7].lo}),
                                             DF{-kv[u][8].hi, -kv[u][8].lo});
@@ -797,13 +799,17 @@ struct rg_ens {
     };
     std::vector<Group> plan[2];
     std::vector<Tile> tiles;
-    std::vector<int> heavy, few_row0, row_sink, row_nsrc, row_sys;
+    std::vector<int> heavy, few_row0, row_sink, row_nsrc, row_sys, row_nparts;
     int few_rows = 0;
+    int sym_chunk = 0;  // light bodies per symmetric heavy-light tile, about (mixed plan)
     long long few_pitch = 0;
     Tile* d_tiles = nullptr;
     int* d_heavy = nullptr;
     int* d_few_row0 = nullptr;
-    int *d_row_sink = nullptr, *d_row_nsrc = nullptr, *d_row_sys = nullptr;
+    int *d_row_sink = nullptr, *d_row_nsrc = nullptr, *d_row_sys = nullptr, *d_row_nparts = nullptr;
+    unsigned int* d_sym_ticket = nullptr;  // per disk: the symmetric kernel's last-segment tickets
+    std::vector<int> sym_cta;              // the symmetric kernel's CTAs: first segments (+ end)
+    int* d_sym_cta = nullptr;
     double* d_terms = nullptr;
     int64_t pairs_per_eval = 0;
     // events: raw records of one attempt, handled on the device (ens_events.cu)
@@ -889,8 +895,8 @@ constexpr int ENS_FEW_BLOCK = 32;
 constexpr int HILL_SET_CAP = 256;  // pairs inside their Hill spheres per disk
 constexpr int HIT_CAP = 64;        // hit-star records per disk and check
 constexpr long long ATTEMPT_CHUNK = 4096;  // attempts per graph launch at most
-// the FP64 plan uses the first three kinds; the mixed-precision plan uses MIXED, DF_ROWSEQ
-// and DF_FEW (double-float heavy pairs)
+// the FP64 plan uses the first three kinds; the mixed-precision plan uses MIXED, DF_ROWSEQ,
+// DF_FEW and DF_SYM (double-float heavy pairs)
 enum {
     GROUP_PAIRPAR = 0,
     GROUP_ROWSEQ = 1,
@@ -898,8 +904,10 @@ enum {
     GROUP_MIXED = 3,
     GROUP_DF_ROWSEQ = 4,
     GROUP_DF_FEW = 5,
-    GROUP_KINDS = 6
+    GROUP_DF_SYM = 6,  // heavy-light pairs once for both rows, with its systems' heavy rows
+    GROUP_KINDS = 7
 };
+constexpr int ENS_SYM_CHUNK = 2048;  // light bodies per symmetric tile about, unless tuned
 
 template <class T>
 int dalloc(T** p, size_t count)
@@ -921,8 +929,8 @@ void free_all(rg_ens* e)
                     e->d_partial, e->d_thr, e->d_status, e->d_active, e->d_active_f0, e->d_acc, e->d_ej,
                     e->d_sys_events, e->d_maxbits, e->d_t, e->d_tprev, e->d_tstop, e->d_dt_try, e->d_dt_did,
                     e->d_ntried, e->d_npassed, e->d_nfailed, e->d_attempt, e->d_acc_attempt, e->d_nf0, e->d_stiles,
-                    e->d_tiles, e->d_heavy, e->d_few_row0, e->d_row_sink, e->d_row_nsrc, e->d_row_sys, e->d_terms,
-                    e->d_ev, e->d_ev_count, e->d_hill, e->d_hill_count, e->d_part, e->d_base_of, e->d_log,
+                    e->d_tiles, e->d_heavy, e->d_few_row0, e->d_row_sink, e->d_row_nsrc, e->d_row_sys, e->d_row_nparts,
+                    e->d_sym_ticket, e->d_sym_cta, e->d_terms, e->d_ev, e->d_ev_count, e->d_hill, e->d_hill_count, e->d_part, e->d_base_of, e->d_log,
                     e->d_log_count, e->d_feat, e->d_dt_last, e->d_ideal_last, e->d_hist, e->d_proposed, e->d_step_prop_rej,
                     e->d_prop_rej_steps, e->d_cool, e->d_nprop, e->d_nprop_acc, e->d_nfallback,
                     e->d_kerr, e->d_rf, e->d_smax, e->d_screen_slot, e->d_prm,
@@ -986,6 +994,7 @@ void build_gravity_plan(rg_ens* e)
     e->row_sink.clear();
     e->row_nsrc.clear();
     e->row_sys.clear();
+    e->row_nparts.clear();
     e->few_rows = 0;
     e->few_pitch = 0;
     e->pairs_per_eval = 0;
@@ -998,6 +1007,36 @@ void build_gravity_plan(rg_ens* e)
     std::vector<Tile> by[2][GROUP_KINDS];
     std::vector<int> hv[2][GROUP_KINDS];
     e->screen_slot.assign(e->cap, -1);
+    // mixed plan: a system whose SI block is a few heavy bodies (a few-sink block over every
+    // massive body) and whose NSI block takes the row kernel over them evaluates the pairs
+    // between the two blocks once, for both rows (grav_df_sym, the heavy-heavy pairs with
+    // them).  The light bodies of all such systems, end to end, are cut into equal ranges of
+    // about sym_chunk, one per CTA, their count whole waves of resident CTAs; a range's pieces
+    // in different systems are its segments, each one part of its system's heavy rows.
+    e->sym_chunk = e->few_chunk > 0 ? e->few_chunk : ENS_SYM_CHUNK;
+    std::vector<char> sym(e->n_sys, 0);
+    std::vector<Tile> sym_systems;
+    std::vector<int> sym_parts(e->n_sys, 0), sym_row0(e->n_sys, 0);
+    double sym_light = 0.0;
+    for (int s = 0; s < e->n_sys; s++) {
+        const int nsi = e->n_si(s), nm = e->n_massive(s), b = e->base[s];
+        sym[s] = nsi >= 1 && nsi <= DF_SYM_MAX_HEAVY && nm > nsi && nsi <= e->rowseq_max_src &&
+                 nm > e->rowseq_max_src && nsi <= ENS_FEW_BLOCK;
+        if (!sym[s]) continue;
+        sym_light += nm - nsi;
+        sym_systems.push_back(Tile{b + nsi, b + nm, b, b + nsi, s, b, 1, 0});
+    }
+    e->sym_cta.clear();
+    if (!sym_systems.empty()) {
+        const int slots = DF_SYM_RESIDENT * e->n_sm;
+        const int waves = std::max(1, (int)std::lround(sym_light / ((double)slots * e->sym_chunk)));
+        const int n_cta = (int)std::min<double>(waves * slots, std::ceil(sym_light / DF_SYM_PASS));
+        std::vector<int> parts;
+        build_sym_segments(sym_systems, n_cta, DF_SYM_PASS, DF_SYM_SEGMENT_COST, by[1][GROUP_DF_SYM], e->sym_cta,
+                           parts);
+        hv[1][GROUP_DF_SYM].assign(by[1][GROUP_DF_SYM].size(), 0);
+        for (size_t k = 0; k < sym_systems.size(); k++) sym_parts[sym_systems[k].sys] = parts[k];
+    }
     for (int s = 0; s < e->n_sys; s++) {
         const int b = e->base[s];
         const int nsi = e->n_si(s), nm = e->n_massive(s), nt = e->ntot[s];
@@ -1017,10 +1056,12 @@ void build_gravity_plan(rg_ens* e)
             if (k.s1 <= k.s0) continue;
             if (k.src1 <= e->rowseq_max_src) {
                 add(0, GROUP_ROWSEQ, k.s0, k.s1, k.src1, k.block, 128);
-                add(1, GROUP_DF_ROWSEQ, k.s0, k.s1, k.src1, k.block, 128);
+                if (!(sym[s] && k.block == 1))  // a symmetric system's light rows: the segments above
+                    add(1, GROUP_DF_ROWSEQ, k.s0, k.s1, k.src1, k.block, 128);
             } else if (k.s1 - k.s0 <= ENS_FEW_BLOCK) {
                 add(0, GROUP_FEW_SERIAL, k.s0, k.s1, k.src1, k.block, FEW_SINKS_MAX);
-                add(1, GROUP_DF_FEW, k.s0, k.s1, k.src1, k.block, FEW_SINKS_MAX);
+                if (!(sym[s] && k.block == 0))  // a symmetric system's heavy rows come with its tiles
+                    add(1, GROUP_DF_FEW, k.s0, k.s1, k.src1, k.block, FEW_SINKS_MAX);
             } else {
                 add(0, GROUP_PAIRPAR, k.s0, k.s1, k.src1, k.block, e->pairpar_S);  // S sinks per CTA and tile
                 const int light0 = k.block == 0 ? std::max(k.s0, std::min(n_heavy, k.s1)) : k.s0;
@@ -1045,12 +1086,29 @@ void build_gravity_plan(rg_ens* e)
                         e->row_sink.push_back(i);
                         e->row_nsrc.push_back(nsrc);
                         e->row_sys.push_back(T[k].sys);
+                        e->row_nparts.push_back(0);
                         e->few_rows++;
                         gr.rows++;
                     }
                     gr.max_src = std::max(gr.max_src, nsrc);
                     gr.max_sinks = std::max(gr.max_sinks, T[k].sink_end - T[k].sink_begin);
                     e->few_pitch = std::max<long long>(e->few_pitch, nsrc);
+                } else if (kind == GROUP_DF_SYM) {
+                    const int sy = T[k].sys, nh = T[k].src_end - T[k].src_begin;
+                    if (T[k].part == 1) {  // the system's heavy rows: the heavy-heavy part + one per segment
+                        sym_row0[sy] = e->few_rows;
+                        for (int h = 0; h < nh; h++) {
+                            e->row_sink.push_back(T[k].src_begin + h);
+                            e->row_nsrc.push_back(e->n_massive(sy));
+                            e->row_sys.push_back(sy);
+                            e->row_nparts.push_back(sym_parts[sy]);
+                            e->few_rows++;
+                            gr.rows++;
+                        }
+                        e->few_pitch = std::max<long long>(e->few_pitch, sym_parts[sy]);
+                    }
+                    e->few_row0.push_back(sym_row0[sy]);
+                    gr.max_src = std::max(gr.max_src, nh);
                 } else {
                     e->few_row0.push_back(0);
                 }
@@ -1073,13 +1131,16 @@ int upload_plans(rg_ens* e)
     cudaFree(e->d_few_row0);
     cudaFree(e->d_row_sink);
     cudaFree(e->d_row_nsrc);
+    cudaFree(e->d_row_nparts);
+    cudaFree(e->d_sym_cta);
     cudaFree(e->d_row_sys);
     cudaFree(e->d_terms);
     cudaFree(e->d_tiles_of);
     e->d_stiles = nullptr;
     e->d_tiles_of = nullptr;
     e->d_tiles = nullptr;
-    e->d_heavy = e->d_few_row0 = e->d_row_sink = e->d_row_nsrc = e->d_row_sys = nullptr;
+    e->d_heavy = e->d_few_row0 = e->d_row_sink = e->d_row_nsrc = e->d_row_sys = e->d_row_nparts = nullptr;
+    e->d_sym_cta = nullptr;
     e->d_terms = nullptr;
     chk(dalloc(&e->d_stiles, e->stiles.size()));
     chk(dalloc(&e->d_tiles_of, e->tiles_of.size()));
@@ -1088,6 +1149,8 @@ int upload_plans(rg_ens* e)
     chk(dalloc(&e->d_few_row0, nt));
     chk(dalloc(&e->d_row_sink, (size_t)e->few_rows));
     chk(dalloc(&e->d_row_nsrc, (size_t)e->few_rows));
+    chk(dalloc(&e->d_row_nparts, (size_t)e->few_rows));
+    chk(dalloc(&e->d_sym_cta, e->sym_cta.size()));
     chk(dalloc(&e->d_row_sys, (size_t)e->few_rows));
     chk(dalloc(&e->d_terms, (size_t)3 * e->few_rows * (size_t)std::max<long long>(e->few_pitch, 1)));
     if (rc) return rc;
@@ -1105,6 +1168,8 @@ int upload_plans(rg_ens* e)
     up(e->d_few_row0, e->few_row0.data(), nt * sizeof(int));
     up(e->d_row_sink, e->row_sink.data(), e->row_sink.size() * sizeof(int));
     up(e->d_row_nsrc, e->row_nsrc.data(), e->row_nsrc.size() * sizeof(int));
+    up(e->d_row_nparts, e->row_nparts.data(), e->row_nparts.size() * sizeof(int));
+    up(e->d_sym_cta, e->sym_cta.data(), e->sym_cta.size() * sizeof(int));
     up(e->d_row_sys, e->row_sys.data(), e->row_sys.size() * sizeof(int));
     if (!rc) RG_CUDA_CHECK(cudaStreamSynchronize(e->st));
     e->graph_valid = false;
@@ -1172,7 +1237,9 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
     bool split_done = false;
     if (e->gravity_mode == RG_GRAVITY_MIXED && !plan.empty()) {
         // a later stage of the attempt needs only the coordinates split again: the step start's
-        // split wrote the masses and radii, which change only at events (after the attempt)
+        // split wrote the masses and radii, which change only at events (after the attempt).
+        // (Writing the split from the stage combination instead was slower: its 8-byte stores
+        // at a 32-byte stride cost the combination more than this kernel takes.)
         if (stage > 0 && !g.smax)
             rc = launch_split_coords(g.px, g.py, g.pz, e->cap, (SplitPos*)e->d_split, e->st);
         else
@@ -1228,6 +1295,12 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
                                         e->st);
                 e->n_kernels += 2;
             }
+            break;
+        case GROUP_DF_SYM:
+            rc = launch_grav_df_sym(g, e->d_sym_cta, (int)e->sym_cta.size() - 1, e->d_split, e->d_few_row0 + gr.off,
+                                    gr.max_src, e->d_terms, e->few_rows, e->few_pitch, e->d_row_sink, e->d_row_nparts,
+                                    e->d_sym_ticket, e->st);
+            e->n_kernels++;
             break;
         case GROUP_MIXED:
             if (!split_done) {
@@ -1641,6 +1714,7 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     chk(dalloc(&e->d_hill_set, 2 * (size_t)HILL_SET_CAP * ns));
     chk(dalloc(&e->d_hill_n, ns));
     chk(dalloc(&e->d_hill_which, ns));
+    chk(dalloc(&e->d_sym_ticket, ns));
     // the event log holds every record of one advance: 16 per body, at least 4096, at most
     // 2^18 (128 MiB); more records end the advance with RG_ERR_EVENT_OVERFLOW
     e->elog_cap = (unsigned int)std::min<int64_t>(1 << 18, std::max<int64_t>(4096, 16 * tot));
@@ -1762,6 +1836,7 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     if (!rc && cudaMemsetAsync(e->d_kerr, 0, sizeof(unsigned int), e->st) != cudaSuccess) chk(RG_ERR_CUDA);
     for (auto z : {std::make_pair((void*)e->d_hill_n, ns * sizeof(int)),
                    std::make_pair((void*)e->d_hill_which, ns * sizeof(int)),
+                   std::make_pair((void*)e->d_sym_ticket, ns * sizeof(unsigned int)),
                    std::make_pair((void*)e->d_elog_count, sizeof(unsigned int)),
                    std::make_pair((void*)e->d_elog_seq, ns * sizeof(unsigned int)),
                    std::make_pair((void*)e->d_flags, sizeof(unsigned int)),

@@ -45,18 +45,8 @@ struct SplitPos {
 
 // inactive bodies (id < 0, pp_disk.cu:242) get mass 0 here, so the pair loop needs no
 // per-pair activity test: their terms vanish.  Coordinates beyond 1e15 AU are clamped
-// there (a merged body is parked at 1e20 AU, pp_disk.cu:1184, and a hit-star merger stays
-// active with m = 0 until the next ejection check): |r|^2 then stays finite in FP32, so
-// the pair loop needs no clamp either, and such a body's zero mass gives a zero term.
-//
-__device__ __forceinline__ void split_coord(double v, float& hi, float& lo)
-{
-    split_bits(v, hi, lo);
-    if (fabsf(hi) > 1.0e15f) {
-        hi = copysignf(1.0e15f, hi);
-        lo = 0.0f;
-    }
-}
+// (split_coord, dfloat.cuh).
+static_assert(sizeof(SplitPos) == 4 * sizeof(float2), "SplitPos: float2 #0 x, #1 y, #2 z, #3 m");
 
 // |r_i - r_base| in FP32 from the split positions' leading parts (event screens)
 __device__ __forceinline__ float star_dist_f(const SplitPos& pi, const SplitPos& p0)
@@ -1015,6 +1005,230 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
     }
 }
 
+// Heavy-light pairs once for both directions.  A system whose SI block is a few heavy
+// bodies (star, giant planets: rows over every massive body) and whose NSI block takes the
+// row kernel over them (light bodies: rows over the SI bodies) has each (heavy h, light i)
+// pair in two rows.  The displacement, r^2, y = 1/r and y^3 are the same for both; this
+// kernel forms them once and both terms from them:
+//   i's row:  (y^3 m_h) (r_h - r_i)   -- grav_df_rowseq's term, bit for bit, in its source order
+//   h's row: -(y^3 m_i) (r_h - r_i)   -- summed over the thread's light bodies in compensated
+//                                        accumulators, then over the CTA
+// The light bodies of all such systems, end to end, are cut into one equal range per CTA (the
+// grid is a whole wave); a range is split into segments at system boundaries, and each
+// segment is one part of its system's heavy rows: partial[(comp * rows + row) * pitch +
+// part].  The segment with part 1 also forms the heavy-heavy pairs (grav_df_few's terms and
+// screens) into part 0.  The system's last segment to finish (a ticket per system, reset by
+// it) adds the parts in order into the heavy rows.  The close-pair FP64 displacement is taken
+// when either body's split positions would be too coarse for it (the row kernel's and the
+// few kernel's thresholds).
+struct DfSymArgs {
+    GravArgs g;             // tiles: the segments (Tile::part from 1)
+    const int* cta_seg;     // CTA c takes segments [cta_seg[c], cta_seg[c + 1])
+    const SplitPos* sp;
+    const int* tile_row0;   // per segment: its system's first heavy row
+    double* partial;
+    int rows;
+    long long pitch;
+    const int* row_sink;    // the heavy rows' bodies
+    const int* row_nparts;  // parts per heavy row: 1 + the system's segments
+    unsigned int* ticket;   // per system, zero between launches
+};
+
+template <bool SCREEN, int HMAX>
+__global__ void __launch_bounds__(256, DF_SYM_RESIDENT) grav_df_sym(DfSymArgs a)
+{
+    const GravArgs& g = a.g;
+    __shared__ SplitPos s_h[HMAX];
+    __shared__ float s_R[HMAX], s_rho[HMAX], s_close2[HMAX];
+    __shared__ double s_x[HMAX], s_y[HMAX], s_z[HMAX];
+    __shared__ int s_src[HMAX], s_sink[HMAX];
+    __shared__ DF s_red[8][3 * HMAX];
+    __shared__ DF s_hh[HMAX][HMAX][3];
+    __shared__ int s_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int sg = a.cta_seg[blockIdx.x]; sg < a.cta_seg[blockIdx.x + 1]; sg++) {
+        const Tile tile = g.tiles[sg];
+        if (g.sys_active && !g.sys_active[tile.sys]) continue;  // uniform over the CTA
+        const int nh = tile.src_end - tile.src_begin;          // <= HMAX (the launcher's choice)
+        SplitPos p0{};
+        float inv3M = 0.0f;
+        const float frad = SCREEN ? tile_frad_f(g, tile) : 0.0f;
+        if (SCREEN && g.hill) {
+            p0 = a.sp[tile.base];
+            inv3M = 1.0f / (3.0f * p0.zm.z);
+        }
+        __syncthreads();  // the previous segment's shared data are consumed
+        if ((int)threadIdx.x < nh) {
+            const int h = tile.src_begin + threadIdx.x;
+            const SplitPos ph = a.sp[h];
+            const int id = g.id[h];
+            s_h[threadIdx.x] = ph;
+            s_src[threadIdx.x] = 0 <= id;  // a source term (pp_disk.cu:246-247)
+            s_sink[threadIdx.x] = 0 < id;  // a sink's row (pp_disk.cu:235-236)
+            s_R[threadIdx.x] = SCREEN ? g.rf[h] : 0.0f;
+            s_rho[threadIdx.x] = (SCREEN && g.hill) ? star_dist_f(ph, p0) : 0.0f;
+            s_close2[threadIdx.x] = close_r2(ph);
+            s_x[threadIdx.x] = g.px[h];
+            s_y[threadIdx.x] = g.py[h];
+            s_z[threadIdx.x] = g.pz[h];
+        }
+        __syncthreads();
+        const int row0 = a.tile_row0[sg];
+        if (tile.part == 1) {  // part 0: the heavy-heavy pairs, as grav_df_few forms them
+            const int t = threadIdx.x;
+            if (t < nh * nh) {
+                const int hs = t / nh, hq = t % nh;  // sink, source
+                DF tx{0.0f, 0.0f}, ty{0.0f, 0.0f}, tz{0.0f, 0.0f};
+                if (hs != hq && s_sink[hs] && s_src[hq]) {
+                    float r2f;
+                    df_term(s_h[hs], s_h[hq], tx, ty, tz, r2f);
+                    if (r2f < s_close2[hs])
+                        df_term_fp64(s_x[hs], s_y[hs], s_z[hs], s_x[hq], s_y[hq], s_z[hq], s_h[hq].zm.z,
+                                     s_h[hq].zm.w, tx, ty, tz, r2f);
+                    if (SCREEN)
+                        df_screen(g, tile, tile.src_begin + hs, tile.src_begin + hq, r2f, s_R[hs], s_R[hq],
+                                  s_rho[hs], s_rho[hq], s_h[hs].zm.z, s_h[hq].zm.z, inv3M, frad);
+                }
+                s_hh[hs][hq][0] = tx;
+                s_hh[hs][hq][1] = ty;
+                s_hh[hs][hq][2] = tz;
+            }
+            __syncthreads();
+            if (t < 3 * nh) {
+                const int hs = t / 3, c = t % 3;
+                Acc2 v{0.0f, 0.0f};
+                for (int q = 0; q < nh; q++) acc_df(v, s_hh[hs][q][c]);
+                a.partial[((long long)c * a.rows + row0 + hs) * a.pitch] = f2d_bits(v.s) + f2d_bits(v.c);
+            }
+        }
+        Acc2 racc[HMAX][3];
+#pragma unroll
+        for (int h = 0; h < HMAX; h++)
+#pragma unroll
+            for (int c = 0; c < 3; c++) racc[h][c] = Acc2{0.0f, 0.0f};
+        // the next light body's record is loaded while the current one's pairs are formed
+        int i = tile.sink_begin + (int)threadIdx.x;
+        SplitPos pn{};
+        int idn = -1;
+        float Rn = 0.0f;
+        if (i < tile.sink_end) {
+            pn = a.sp[i];
+            idn = g.id[i];
+            if (SCREEN) Rn = g.rf[i];
+        }
+        for (; i < tile.sink_end; i += blockDim.x) {
+            const SplitPos pi = pn;
+            const int idi = idn;
+            const float Ri = Rn;
+            if (i + (int)blockDim.x < tile.sink_end) {
+                pn = a.sp[i + blockDim.x];
+                idn = g.id[i + blockDim.x];
+                if (SCREEN) Rn = g.rf[i + blockDim.x];
+            }
+            const bool sink_ok = 0 < idi, src_ok = 0 <= idi;
+            Acc2 ox{0.0f, 0.0f}, oy{0.0f, 0.0f}, oz{0.0f, 0.0f};
+            if (src_ok) {
+                const float rhoi = (SCREEN && g.hill) ? star_dist_f(pi, p0) : 0.0f;
+                const float close_i = close_r2(pi);
+                const DF mi{pi.zm.z, pi.zm.w};
+#pragma unroll
+                for (int h = 0; h < HMAX; h++) {
+                    if (h >= nh) continue;
+                    const bool own = sink_ok && s_src[h];
+                    const bool rev = s_sink[h] != 0;
+                    if (!(own || rev)) continue;
+                    const SplitPos ph = s_h[h];
+                    DF dx = df_diff(ph.xy.x, ph.xy.y, pi.xy.x, pi.xy.y);
+                    DF dy = df_diff(ph.xy.z, ph.xy.w, pi.xy.z, pi.xy.w);
+                    DF dz = df_diff(ph.zm.x, ph.zm.y, pi.zm.x, pi.zm.y);
+                    DF r2 = df_add_same_sign(df_add_same_sign(df_mul(dx, dx), df_mul(dy, dy)), df_mul(dz, dz));
+                    if (r2.hi < fmaxf(close_i, s_close2[h])) {  // the FP64 displacement (df_term_fp64)
+                        dx = split_df(__dadd_rn(s_x[h], -g.px[i]));
+                        dy = split_df(__dadd_rn(s_y[h], -g.py[i]));
+                        dz = split_df(__dadd_rn(s_z[h], -g.pz[i]));
+                        r2 = df_add_same_sign(df_add_same_sign(df_mul(dx, dx), df_mul(dy, dy)), df_mul(dz, dz));
+                    }
+                    if (!(r2.hi < 1.0e30f)) r2 = DF{1.0e30f, 0.0f};  // a merged body parked at 1e20 AU
+                    const float y0 = rsqrt_approx(r2.hi);
+                    const DF p = df_mul(r2, df_two_prod(y0, y0));
+                    const float hh = (1.0f - p.hi) - p.lo;
+                    const DF y = df_fast_sum(y0, 0.5f * y0 * hh);
+                    const DF y3 = df_mul(df_mul(y, y), y);
+                    if (own) {
+                        const DF w = df_mul(y3, DF{ph.zm.z, ph.zm.w});
+                        acc_df(ox, df_mul(w, dx));
+                        acc_df(oy, df_mul(w, dy));
+                        acc_df(oz, df_mul(w, dz));
+                        if (SCREEN)
+                            df_screen(g, tile, i, tile.src_begin + h, r2.hi, Ri, s_R[h], rhoi, s_rho[h], pi.zm.z,
+                                      ph.zm.z, inv3M, frad);
+                    }
+                    if (rev) {
+                        const DF w = df_mul(y3, mi);
+                        const DF tx = df_mul(w, dx), ty = df_mul(w, dy), tz = df_mul(w, dz);
+                        acc_df(racc[h][0], DF{-tx.hi, -tx.lo});
+                        acc_df(racc[h][1], DF{-ty.hi, -ty.lo});
+                        acc_df(racc[h][2], DF{-tz.hi, -tz.lo});
+                    }
+                }
+            }
+            if (g.acc_f2) {
+                const DF x = df_two_sum(ox.s, ox.c), y = df_two_sum(oy.s, oy.c), z = df_two_sum(oz.s, oz.c);
+                reinterpret_cast<float2*>(g.ax)[i] = make_float2(x.hi, x.lo);
+                reinterpret_cast<float2*>(g.ay)[i] = make_float2(y.hi, y.lo);
+                reinterpret_cast<float2*>(g.az)[i] = make_float2(z.hi, z.lo);
+            } else {
+                g.ax[i] = f2d_bits(ox.s) + f2d_bits(ox.c);
+                g.ay[i] = f2d_bits(oy.s) + f2d_bits(oy.c);
+                g.az[i] = f2d_bits(oz.s) + f2d_bits(oz.c);
+            }
+        }
+#pragma unroll
+        for (int h = 0; h < HMAX; h++) {
+            if (h < nh) {  // uniform over the CTA
+#pragma unroll
+                for (int c = 0; c < 3; c++) {
+                    Acc2 v = racc[h][c];
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) {
+                        const Acc2 o{__shfl_xor_sync(0xffffffffu, v.s, off), __shfl_xor_sync(0xffffffffu, v.c, off)};
+                        v = two_sum_merge(v, o);
+                    }
+                    if (lane == 0) s_red[warp][3 * h + c] = df_two_sum(v.s, v.c);
+                }
+            }
+        }
+        __syncthreads();
+        if ((int)threadIdx.x < 3 * nh) {
+            const int h = threadIdx.x / 3, c = threadIdx.x % 3;
+            DF v = s_red[0][threadIdx.x];
+            for (int w = 1; w < (int)(blockDim.x >> 5); w++) v = df_add(v, s_red[w][threadIdx.x]);
+            a.partial[((long long)c * a.rows + row0 + h) * a.pitch + tile.part] = df_to_double(v);
+        }
+        // the system's last segment adds its heavy rows' parts in order (no waiting: the
+        // others are done)
+        const int np = a.row_nparts[row0];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            s_last = atomicAdd(&a.ticket[tile.sys], 1u) == (unsigned int)(np - 2);  // np - 1 segments
+        }
+        __syncthreads();
+        if (s_last) {
+            __threadfence();
+            if (threadIdx.x == 0) a.ticket[tile.sys] = 0u;
+            if ((int)threadIdx.x < 3 * nh) {
+                const int h = threadIdx.x / 3, c = threadIdx.x % 3;
+                const double* P = a.partial + ((long long)c * a.rows + row0 + h) * a.pitch;
+                double v = 0.0;
+                for (int q = 0; q < np; q++) v += __ldcg(P + q);
+                double* out = c == 0 ? g.ax : (c == 1 ? g.ay : g.az);
+                store_acc(g, out, a.row_sink[row0 + h], v);
+            }
+        }
+    }
+}
+
 struct DfFinalArgs {
     int acc_f2;
     const double* partial;
@@ -1022,7 +1236,7 @@ struct DfFinalArgs {
     long long pitch;
     const int* row_sink;
     const int* row_nsrc;
-    const int* row_sys;  // nullptr for one disk
+    const int* row_sys;     // nullptr for one disk
     const int* sys_active;
     double *ax, *ay, *az;
     int chunk;
@@ -1090,6 +1304,30 @@ int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row
     DfFinalArgs f{g.acc_f2, partial, rows, group_row0, group_rows, pitch, row_sink, row_nsrc, row_sys, g.sys_active,
                   g.ax, g.ay, g.az, chunk};
     df_few_final<<<(3 * group_rows + 127) / 128, 128, 0, st>>>(f);
+    RG_CUDA_CHECK(cudaGetLastError());
+    return 0;
+}
+
+int launch_grav_df_sym(const GravArgs& g, const int* cta_seg, int n_cta, const void* split, const int* tile_row0,
+                       int max_heavy, double* partial, int rows, long long pitch, const int* row_sink,
+                       const int* row_nparts, unsigned int* ticket, cudaStream_t st)
+{
+    if (g.n_tiles <= 0 || n_cta <= 0) return 0;
+    if (max_heavy < 1 || max_heavy > DF_SYM_MAX_HEAVY) return set_error(RG_ERR_STATE, "symmetric tile: heavy bodies");
+    DfSymArgs b{g, cta_seg, (const SplitPos*)split, tile_row0, partial, rows, pitch, row_sink, row_nparts, ticket};
+    const bool screen = g.record || g.hill;
+#define RG_SYM(H)                                                    \
+    do {                                                             \
+        if (screen)                                                  \
+            grav_df_sym<true, H><<<n_cta, 256, 0, st>>>(b);          \
+        else                                                         \
+            grav_df_sym<false, H><<<n_cta, 256, 0, st>>>(b);         \
+    } while (0)
+    if (max_heavy <= 3)
+        RG_SYM(3);
+    else
+        RG_SYM(DF_SYM_MAX_HEAVY);
+#undef RG_SYM
     RG_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

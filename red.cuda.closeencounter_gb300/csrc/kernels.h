@@ -106,6 +106,20 @@ int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row
                        int chunk_hint,
                        double* partial, int rows, long long pitch, const int* row_sink, const int* row_nsrc,
                        const int* row_sys, int group_row0, int group_rows, cudaStream_t st);
+// heavy-light pairs once for both rows (grav_df_sym) and the heavy rows' sums: segments (the
+// tiles) of light bodies (sinks) against their system's SI bodies (sources, at most
+// DF_SYM_MAX_HEAVY), CTA c taking segments [cta_seg[c], cta_seg[c + 1]); Tile::part = the
+// segment's part of its heavy rows (1-based; part 1 also takes the heavy-heavy pairs),
+// tile_row0 = each segment's first heavy row, row_nparts = parts per heavy row (1 + the
+// system's segments), ticket = one counter per system, zero before the first launch
+constexpr int DF_SYM_MAX_HEAVY = 4;
+constexpr int DF_SYM_RESIDENT = 3;   // CTAs of 256 threads per SM (the kernel's launch bound)
+constexpr int DF_SYM_PASS = 256;             // light bodies per pass of a CTA (one per thread)
+constexpr double DF_SYM_SEGMENT_COST = 0.6;  // a segment's reduction and barriers, in passes
+int launch_grav_df_sym(const GravArgs& g, const int* cta_seg, int n_cta, const void* split, const int* tile_row0,
+                       int max_heavy, double* partial, int rows, long long pitch, const int* row_sink,
+                       const int* row_nparts, unsigned int* ticket, cudaStream_t st);
+
 int launch_star_distance(const double* x, const double* y, const double* z, const int* base_of, int n, double* rho,
                          cudaStream_t st);
 

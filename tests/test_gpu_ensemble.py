@@ -271,3 +271,40 @@ def test_mode_switch_keeps_the_first_stage_vector(gpulib):
         E1 = ens.energy(s)[0]
         assert np.isfinite(E1) and abs((E1 - E0[s]) / E0[s]) < 1e-10
         assert ens.stats(s)["status"] == T.SYS_RUNNING
+
+
+def test_mixed_heavy_light_pairs_match_fp64(gpulib):
+    """The mixed form evaluates each (heavy, light) pair once for both rows: the planetesimal's
+    row term and the star's or giant's row term come from one displacement and one y^3, and
+    the heavy rows add one part per tile of up to 2048 light bodies after the heavy-heavy part.
+    Over one accepted 0.01-day step (one attempt) from rest -- so that the velocity after the
+    step is the velocity change itself, to full precision -- every body's agrees with the FP64
+    form's to the mixed force tolerance, and the star's and the giants' to 1e-11, on disks of
+    one light tile and of several (5000 and 2049 planetesimals: tiles are balanced over the
+    ensemble, so their sizes differ)."""
+    disks = [bodies.config_disk("ensemble_member", seed=s, n=n) for s, n in ((1, 600), (2, 5000), (3, 2049))]
+    for d in disks:
+        for f in "xyz":
+            d.v[f][:] = 0.0
+    thr = bodies.thresholds(collision_factor=0.0)
+    dv, t_end = {}, {}
+    for mode in (T.GRAVITY_FP64, T.GRAVITY_MIXED):
+        ens = Ensemble(disks, thr)
+        ens.set_integrator(0.01, 1e-10)
+        ens.set_options(gravity_mode=mode)
+        v0 = [ens.state(s)[1] for s in range(len(disks))]
+        ens.advance(1.0, max_attempts=1)
+        out = []
+        for s in range(len(disks)):
+            assert ens.stats(s)["n_passed_step"] == 1
+            _, v1, _, _, t = ens.state(s)
+            out.append(np.stack([v1[f] - v0[s][f] for f in "xyz"], 1))
+            t_end[mode, s] = t
+        dv[mode] = out
+        ens.close()
+    for s, d in enumerate(disks):
+        assert t_end[T.GRAVITY_MIXED, s] == t_end[T.GRAVITY_FP64, s]
+        a_e, a_m = dv[T.GRAVITY_FP64][s], dv[T.GRAVITY_MIXED][s]
+        rel = np.linalg.norm(a_m - a_e, axis=1) / np.linalg.norm(a_e, axis=1)
+        print(f"disk {s} ({d.n_total} bodies): max rel {rel.max():.3e}, heavy rows {rel[:3].max():.3e}")
+        assert rel.max() < 1e-10 and rel[:3].max() < 1e-11
