@@ -769,6 +769,7 @@ struct rg_ens {
     int* d_type = nullptr;
     void* d_split = nullptr;
     float* d_rf = nullptr;  // FP32 radii of the mixed kernels' event screens
+    float2* d_mass_f2 = nullptr;  // the split masses (the symmetric kernel's later stages)
     unsigned int* d_smax = nullptr;  // the screens' maxima per disk (split_positions)
     int* d_screen_slot = nullptr;    // per body: its disk for a light body, -1 for a heavy one
     std::vector<int> screen_slot;
@@ -933,7 +934,7 @@ void free_all(rg_ens* e)
                     e->d_sym_ticket, e->d_sym_cta, e->d_terms, e->d_ev, e->d_ev_count, e->d_hill, e->d_hill_count, e->d_part, e->d_base_of, e->d_log,
                     e->d_log_count, e->d_feat, e->d_dt_last, e->d_ideal_last, e->d_hist, e->d_proposed, e->d_step_prop_rej,
                     e->d_prop_rej_steps, e->d_cool, e->d_nprop, e->d_nprop_acc, e->d_nfallback,
-                    e->d_kerr, e->d_rf, e->d_smax, e->d_screen_slot, e->d_prm,
+                    e->d_kerr, e->d_rf, e->d_mass_f2, e->d_smax, e->d_screen_slot, e->d_prm,
                     e->d_f_rad, e->d_base, e->d_ntot, e->d_nsi, e->d_hill_set, e->d_hill_n, e->d_hill_which,
                     e->d_elog, e->d_elog_count, e->d_elog_seq, e->d_flags, e->d_hit_slots, e->d_keep,
                     e->d_attempts, e->d_tiles_of, e->d_feat_red};
@@ -1235,9 +1236,14 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
     }
     const auto& plan = e->plan[e->gravity_mode == RG_GRAVITY_MIXED ? 1 : 0];
     bool split_done = false;
-    if (e->gravity_mode == RG_GRAVITY_MIXED && !plan.empty()) {
-        // a later stage of the attempt needs only the coordinates split again: the step start's
-        // split wrote the masses and radii, which change only at events (after the attempt).
+    // a later stage of the attempt needs only the coordinates split again: the step start's
+    // split wrote the masses and radii, which change only at events (after the attempt); when
+    // the symmetric kernel is the only one, it splits the coordinates itself (from the FP64
+    // positions and the step start's split masses)
+    bool sym_only = !plan.empty();
+    for (const auto& gr : plan) sym_only = sym_only && gr.kind == GROUP_DF_SYM;
+    const bool sym_splits = e->gravity_mode == RG_GRAVITY_MIXED && sym_only && stage > 0 && !g.smax;
+    if (e->gravity_mode == RG_GRAVITY_MIXED && !plan.empty() && !sym_splits) {
         // (Writing the split from the stage combination instead was slower: its 8-byte stores
         // at a 32-byte stride cost the combination more than this kernel takes.)
         if (stage > 0 && !g.smax)
@@ -1245,7 +1251,7 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
         else
             rc = launch_split_positions(g.px, g.py, g.pz, e->d_mass, e->d_id, e->d_base_of, e->d_screen_slot,
                                         e->d_radius, e->cap, (SplitPos*)e->d_split, e->d_rf,
-                                        g.smax ? e->d_smax : nullptr, g.hill != 0, e->st);
+                                        g.smax ? e->d_smax : nullptr, g.hill != 0, e->st, e->d_mass_f2);
         split_done = true;
         e->n_kernels++;
         if (rc) return rc;
@@ -1299,7 +1305,7 @@ int ens_gravity(rg_ens* e, const double* pos, const double* vel, double* acc, in
         case GROUP_DF_SYM:
             rc = launch_grav_df_sym(g, e->d_sym_cta, (int)e->sym_cta.size() - 1, e->d_split, e->d_few_row0 + gr.off,
                                     gr.max_src, e->d_terms, e->few_rows, e->few_pitch, e->d_row_sink, e->d_row_nparts,
-                                    e->d_sym_ticket, e->st);
+                                    e->d_sym_ticket, e->st, sym_splits ? e->d_mass_f2 : nullptr);
             e->n_kernels++;
             break;
         case GROUP_MIXED:
@@ -1668,6 +1674,7 @@ int create_impl(int n_sys, const rg_counts_t* counts, const rg_vec_t* r, const r
     chk(dalloc(&e->d_base_of, nt));
     chk(dalloc((char**)&e->d_split, SPLIT_POS_BYTES * nt));
     chk(dalloc(&e->d_rf, nt));
+    chk(dalloc(&e->d_mass_f2, nt));
     chk(dalloc(&e->d_smax, (size_t)SCREEN_MAX_WORDS * ns));
     chk(dalloc(&e->d_screen_slot, nt));
     chk(dalloc(&e->d_thr, 5 * ns));

@@ -67,7 +67,7 @@ __global__ void split_positions_kernel(const double* __restrict__ x, const doubl
                                        const int* __restrict__ id, const int* __restrict__ base_of,
                                        const int* __restrict__ screen_slot, const double* __restrict__ radius,
                                        int n, SplitPos* __restrict__ out, float* __restrict__ rf,
-                                       unsigned int* smax, bool hill)
+                                       unsigned int* smax, bool hill, float2* __restrict__ mass_f2)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     float rmax = 0.0f, mmax = 0.0f, dmax = 0.0f;
@@ -80,6 +80,7 @@ __global__ void split_positions_kernel(const double* __restrict__ x, const doubl
         sp.zm.z = sp.zm.w = 0.0f;
         if (id[i] >= 0) split_bits(m[i], sp.zm.z, sp.zm.w);
         out[i] = sp;
+        if (mass_f2) mass_f2[i] = make_float2(sp.zm.z, sp.zm.w);
         if (rf) {
             float rh, rl;
             split_bits(radius[i], rh, rl);
@@ -1021,6 +1022,18 @@ __global__ void __launch_bounds__(256, SMAX <= 4 ? 3 : 2) grav_df_few(DfFewArgs 
 // it) adds the parts in order into the heavy rows.  The close-pair FP64 displacement is taken
 // when either body's split positions would be too coarse for it (the row kernel's and the
 // few kernel's thresholds).
+// a body's split record from its FP64 coordinates and its split mass (split_positions_kernel's)
+__device__ __forceinline__ SplitPos split_record(double x, double y, double z, float2 m)
+{
+    SplitPos p;
+    split_coord(x, p.xy.x, p.xy.y);
+    split_coord(y, p.xy.z, p.xy.w);
+    split_coord(z, p.zm.x, p.zm.y);
+    p.zm.z = m.x;
+    p.zm.w = m.y;
+    return p;
+}
+
 struct DfSymArgs {
     GravArgs g;             // tiles: the segments (Tile::part from 1)
     const int* cta_seg;     // CTA c takes segments [cta_seg[c], cta_seg[c + 1])
@@ -1032,9 +1045,13 @@ struct DfSymArgs {
     const int* row_sink;    // the heavy rows' bodies
     const int* row_nparts;  // parts per heavy row: 1 + the system's segments
     unsigned int* ticket;   // per system, zero between launches
+    const float2* mass_f2;  // FROM64: the split masses; the coordinates are split here from FP64
 };
 
-template <bool SCREEN, int HMAX>
+// FROM64: the split records are formed here from the FP64 coordinates and mass_f2 (a later
+// stage of an attempt, whose coordinates the split records do not hold): 32 B read per light
+// body, where a separate split pass would read 24 and write 32 before this kernel's 32
+template <bool SCREEN, int HMAX, bool FROM64>
 __global__ void __launch_bounds__(256, DF_SYM_RESIDENT) grav_df_sym(DfSymArgs a)
 {
     const GravArgs& g = a.g;
@@ -1054,13 +1071,14 @@ __global__ void __launch_bounds__(256, DF_SYM_RESIDENT) grav_df_sym(DfSymArgs a)
         float inv3M = 0.0f;
         const float frad = SCREEN ? tile_frad_f(g, tile) : 0.0f;
         if (SCREEN && g.hill) {
-            p0 = a.sp[tile.base];
+            p0 = FROM64 ? split_record(g.px[tile.base], g.py[tile.base], g.pz[tile.base], a.mass_f2[tile.base])
+                        : a.sp[tile.base];
             inv3M = 1.0f / (3.0f * p0.zm.z);
         }
         __syncthreads();  // the previous segment's shared data are consumed
         if ((int)threadIdx.x < nh) {
             const int h = tile.src_begin + threadIdx.x;
-            const SplitPos ph = a.sp[h];
+            const SplitPos ph = FROM64 ? split_record(g.px[h], g.py[h], g.pz[h], a.mass_f2[h]) : a.sp[h];
             const int id = g.id[h];
             s_h[threadIdx.x] = ph;
             s_src[threadIdx.x] = 0 <= id;  // a source term (pp_disk.cu:246-247)
@@ -1109,22 +1127,28 @@ __global__ void __launch_bounds__(256, DF_SYM_RESIDENT) grav_df_sym(DfSymArgs a)
         // the next light body's record is loaded while the current one's pairs are formed
         int i = tile.sink_begin + (int)threadIdx.x;
         SplitPos pn{};
+        double xn = 0.0, yn = 0.0, zn = 0.0;
+        float2 mn{0.0f, 0.0f};
         int idn = -1;
         float Rn = 0.0f;
-        if (i < tile.sink_end) {
-            pn = a.sp[i];
-            idn = g.id[i];
-            if (SCREEN) Rn = g.rf[i];
-        }
+        auto fetch = [&](int j) {
+            if constexpr (FROM64) {
+                xn = g.px[j];
+                yn = g.py[j];
+                zn = g.pz[j];
+                mn = a.mass_f2[j];
+            } else {
+                pn = a.sp[j];
+            }
+            idn = g.id[j];
+            if (SCREEN) Rn = g.rf[j];
+        };
+        if (i < tile.sink_end) fetch(i);
         for (; i < tile.sink_end; i += blockDim.x) {
-            const SplitPos pi = pn;
+            const SplitPos pi = FROM64 ? split_record(xn, yn, zn, mn) : pn;
             const int idi = idn;
             const float Ri = Rn;
-            if (i + (int)blockDim.x < tile.sink_end) {
-                pn = a.sp[i + blockDim.x];
-                idn = g.id[i + blockDim.x];
-                if (SCREEN) Rn = g.rf[i + blockDim.x];
-            }
+            if (i + (int)blockDim.x < tile.sink_end) fetch(i + blockDim.x);
             const bool sink_ok = 0 < idi, src_ok = 0 <= idi;
             Acc2 ox{0.0f, 0.0f}, oy{0.0f, 0.0f}, oz{0.0f, 0.0f};
             if (src_ok) {
@@ -1310,24 +1334,33 @@ int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row
 
 int launch_grav_df_sym(const GravArgs& g, const int* cta_seg, int n_cta, const void* split, const int* tile_row0,
                        int max_heavy, double* partial, int rows, long long pitch, const int* row_sink,
-                       const int* row_nparts, unsigned int* ticket, cudaStream_t st)
+                       const int* row_nparts, unsigned int* ticket, cudaStream_t st, const float2* mass_f2)
 {
     if (g.n_tiles <= 0 || n_cta <= 0) return 0;
     if (max_heavy < 1 || max_heavy > DF_SYM_MAX_HEAVY) return set_error(RG_ERR_STATE, "symmetric tile: heavy bodies");
-    DfSymArgs b{g, cta_seg, (const SplitPos*)split, tile_row0, partial, rows, pitch, row_sink, row_nparts, ticket};
+    DfSymArgs b{g, cta_seg, (const SplitPos*)split, tile_row0, partial, rows, pitch, row_sink, row_nparts, ticket,
+                mass_f2};
     const bool screen = g.record || g.hill;
-#define RG_SYM(H)                                                    \
+#define RG_SYM2(H, F)                                                \
     do {                                                             \
         if (screen)                                                  \
-            grav_df_sym<true, H><<<n_cta, 256, 0, st>>>(b);          \
+            grav_df_sym<true, H, F><<<n_cta, 256, 0, st>>>(b);       \
         else                                                         \
-            grav_df_sym<false, H><<<n_cta, 256, 0, st>>>(b);         \
+            grav_df_sym<false, H, F><<<n_cta, 256, 0, st>>>(b);      \
+    } while (0)
+#define RG_SYM(H)               \
+    do {                        \
+        if (mass_f2)            \
+            RG_SYM2(H, true);   \
+        else                    \
+            RG_SYM2(H, false);  \
     } while (0)
     if (max_heavy <= 3)
         RG_SYM(3);
     else
         RG_SYM(DF_SYM_MAX_HEAVY);
 #undef RG_SYM
+#undef RG_SYM2
     RG_CUDA_CHECK(cudaGetLastError());
     return 0;
 }
@@ -1358,11 +1391,11 @@ int launch_split_coords(const double* x, const double* y, const double* z, int n
 
 int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id,
                            const int* base_of, const int* screen_slot, const double* radius, int n,
-                           SplitPos* out, float* rf, unsigned int* smax, bool hill, cudaStream_t st)
+                           SplitPos* out, float* rf, unsigned int* smax, bool hill, cudaStream_t st, float2* mass_f2)
 {
     if (n <= 0) return 0;
     split_positions_kernel<<<(n + 255) / 256, 256, 0, st>>>(x, y, z, m, id, base_of, screen_slot, radius, n, out,
-                                                            rf, smax, hill);
+                                                            rf, smax, hill, mass_f2);
     RG_CUDA_CHECK(cudaGetLastError());
     return 0;
 }

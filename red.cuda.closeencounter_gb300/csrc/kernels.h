@@ -91,7 +91,8 @@ constexpr size_t SPLIT_POS_BYTES = 32;  // per body
 int launch_split_coords(const double* x, const double* y, const double* z, int n, SplitPos* out, cudaStream_t st);
 int launch_split_positions(const double* x, const double* y, const double* z, const double* m, const int* id,
                            const int* base_of, const int* screen_slot, const double* radius, int n,
-                           SplitPos* out, float* rf, unsigned int* smax, bool hill, cudaStream_t st);
+                           SplitPos* out, float* rf, unsigned int* smax, bool hill, cudaStream_t st,
+                           float2* mass_f2 = nullptr);
 constexpr int SCREEN_MAX_WORDS = 4;  // GravArgs::smax per system: radius, mass, star distance, spare
 // hold: test hook -- no tile copies are issued, so the kernel's bounded waits run out
 int launch_grav_mixed_tiles(const GravArgs& g, const void* split, const int* heavy_end, float near_ratio,
@@ -111,14 +112,17 @@ int launch_grav_df_few(const GravArgs& g, const void* split, const int* tile_row
 // DF_SYM_MAX_HEAVY), CTA c taking segments [cta_seg[c], cta_seg[c + 1]); Tile::part = the
 // segment's part of its heavy rows (1-based; part 1 also takes the heavy-heavy pairs),
 // tile_row0 = each segment's first heavy row, row_nparts = parts per heavy row (1 + the
-// system's segments), ticket = one counter per system, zero before the first launch
+// system's segments), ticket = one counter per system, zero before the first launch; with
+// mass_f2 (the split masses, launch_split_positions) the kernel splits the FP64 coordinates
+// itself and reads no split records
 constexpr int DF_SYM_MAX_HEAVY = 4;
 constexpr int DF_SYM_RESIDENT = 3;   // CTAs of 256 threads per SM (the kernel's launch bound)
 constexpr int DF_SYM_PASS = 256;             // light bodies per pass of a CTA (one per thread)
 constexpr double DF_SYM_SEGMENT_COST = 0.6;  // a segment's reduction and barriers, in passes
 int launch_grav_df_sym(const GravArgs& g, const int* cta_seg, int n_cta, const void* split, const int* tile_row0,
                        int max_heavy, double* partial, int rows, long long pitch, const int* row_sink,
-                       const int* row_nparts, unsigned int* ticket, cudaStream_t st);
+                       const int* row_nparts, unsigned int* ticket, cudaStream_t st,
+                       const float2* mass_f2 = nullptr);
 
 int launch_star_distance(const double* x, const double* y, const double* z, const int* base_of, int n, double* rho,
                          cudaStream_t st);
