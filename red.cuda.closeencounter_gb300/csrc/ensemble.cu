@@ -470,6 +470,50 @@ __device__ __forceinline__ float to_f32(double v)
     return hi;
 }
 
+// the accepted disks' y_{n+1} into y (6 rows), with the ejection / hit-star screen of the new
+// positions (ens_eject_screen_kernel's tests) taken on the way: r^2 in FP32 from the
+// coordinates' leading parts first (relative error below 1e-6), the reference's FP64 test only
+// where that lies within 1e-5 of a threshold -- so the screen costs no FP64 work for bodies
+// far from both
+__global__ void ens_accept_kernel(const StageTile* tiles, const int* acc, const double* __restrict__ src,
+                                  double* __restrict__ dst, int stride, const int* id, const int* type,
+                                  const double* thr, int* ej)
+{
+    const StageTile t = tiles[blockIdx.x];
+    if (!acc[t.sys]) return;
+    const double* th = thr + 5 * t.sys;
+    const bool hit_on = 0.0 < th[0], ej_on = 0.0 < th[1];
+    const float hit_f = hit_on ? to_f32(th[3]) * (1.0f + 1e-5f) : 0.0f;
+    const float ej_f = ej_on ? to_f32(th[4]) * (1.0f - 1e-5f) : 0.0f;
+    // two bodies per thread and iteration, their six rows' loads first (memory latency)
+    constexpr int U = 2;
+    bool hit = false;
+    for (int i0 = t.b0 + threadIdx.x; i0 < t.b1; i0 += U * blockDim.x) {
+        double v[U][6];
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int i = min(i0 + u * (int)blockDim.x, t.b1 - 1);
+#pragma unroll
+            for (int r = 0; r < 6; r++) v[u][r] = __ldg(src + (long long)r * stride + i);
+        }
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+            const int i = i0 + u * (int)blockDim.x;
+            if (i >= t.b1) continue;
+#pragma unroll
+            for (int r = 0; r < 6; r++) dst[(long long)r * stride + i] = v[u][r];
+            if (!(hit_on || ej_on) || !(0 < id[i] && type[i] != 0)) continue;
+            const float xf = to_f32(v[u][0]), yf = to_f32(v[u][1]), zf = to_f32(v[u][2]);
+            const float r2f = xf * xf + yf * yf + zf * zf;
+            if (!((ej_on && !(r2f < ej_f)) || (hit_on && !(r2f > hit_f)))) continue;
+            const double x = v[u][0], yy = v[u][1], z = v[u][2];
+            const double r2 = x * x + yy * yy + z * z;  // pp_disk.cu:72-142, in FP64
+            if ((ej_on && th[4] < r2) || (hit_on && th[3] > r2)) hit = true;
+        }
+    }
+    if (hit) ej[t.sys] = 1;
+}
+
 // one body's contribution; si: the disk's first FEAT_MAX_SI SI bodies (positions relative to
 // body 0, masses, distance from body 0) in shared memory, ns of them in all (the rest are read
 // from the state rows), M = body 0's mass.  The body's values are loaded before any test, so
@@ -891,7 +935,10 @@ namespace {
 
 constexpr double GAUSS = 1.720209895e-2;
 constexpr double GAUSS2 = 2.959122082855911025e-4;
-constexpr int STAGE_TILE = 2048;
+// bodies per stage tile (one CTA of the per-element kernels): the tiles of a disk are equal but
+// its last, so smaller tiles spread the stage combinations' bytes more evenly over the SMs
+// (1024 against 2048: 0.93 against 1.03 ms of stage kernels per 256-disk attempt)
+constexpr int STAGE_TILE = 1024;
 constexpr int ENS_FEW_BLOCK = 32;
 constexpr int HILL_SET_CAP = 256;  // pairs inside their Hill spheres per disk
 constexpr int HIT_CAP = 64;        // hit-star records per disk and check
@@ -1530,10 +1577,8 @@ int record_attempt(rg_ens* e, bool in_graph)
     pr = prof_begin(e, 2);
     ens_controller_kernel<<<nb, 128, 0, e->st>>>(e->sys());
     RG_CUDA_CHECK(cudaGetLastError());
-    ens_copy_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_acc, e->d_yout, 0, e->d_y, 0, 6, e->cap);
-    RG_CUDA_CHECK(cudaGetLastError());
-    ens_eject_screen_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_acc, e->d_y, e->cap, e->d_id, e->d_type,
-                                                  e->d_thr, e->d_ej);
+    ens_accept_kernel<<<ns, 256, 0, e->st>>>(e->d_stiles, e->d_acc, e->d_yout, e->d_y, e->cap, e->d_id, e->d_type,
+                                             e->d_thr, e->d_ej);
     RG_CUDA_CHECK(cudaGetLastError());
     ens_finalize_kernel<<<nb, 128, 0, e->st>>>(e->sys());
     RG_CUDA_CHECK(cudaGetLastError());
@@ -1542,7 +1587,7 @@ int record_attempt(rg_ens* e, bool in_graph)
     if (!rc) rc = launch_ens_loop(loop_args(e, in_graph), e->st);
     prof_end(e, pr);
     if (rc) return rc;
-    e->n_kernels += e->gravity_mode == RG_GRAVITY_MIXED ? 6 : 7;  // (error norm,) controller ... loop
+    e->n_kernels += e->gravity_mode == RG_GRAVITY_MIXED ? 5 : 6;  // (error norm,) controller ... loop
     return RG_OK;
 }
 

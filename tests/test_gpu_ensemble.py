@@ -120,6 +120,44 @@ def test_ensemble_collisions_match_oracle(gpulib):
     assert all(int(e["event_name"]) != T.EVENT_COLLISION for e in ev[sysv == 1])  # R1 + R2: none
 
 
+def test_ensemble_ejection_and_hit_star_match_oracle(gpulib):
+    """The reference's ejection run (16 planetesimals on eccentric orbits, 4 test particles,
+    ejection beyond 3.2 AU: 11 ejections in 3 years) and a disk with two planetesimals let
+    fall towards the star from rest (hit-star inside 0.3 AU) as one ensemble: the screen of
+    each accepted state (taken in FP32 first, in FP64 near a threshold) finds the same bodies
+    at the same steps as the oracle's replay of each disk's step sizes, and the records and
+    the final states match it bit for bit."""
+    disk, params, _, _ = H.load_fixture("disk_eject_hit")
+    fall = bodies.make_disk(n_pl=16, seed=12, a_range=(1.0, 3.0))
+    for k in (5, 9):
+        for f in "xyz":
+            fall.v[f][k] = 0.0
+    thr = np.stack([H.thresholds_of(params)] * 2)
+    ens = Ensemble([disk, fall], thr)
+    ens.set_integrator(0.001, 1e-10)
+    ens.set_step_log(1 << 18)
+    ens.advance(params["length_yr"] * T.YEAR)
+    log = ens.step_log()
+    ev, sysv = ens.events()
+    for s, (d, kind) in enumerate(((disk, T.EVENT_EJECTION), (fall, T.EVENT_HIT_CENTRUM))):
+        o = pyoracle.OracleSystem(d, thr[s])
+        o.set_integrator(T.INT_RKF78, 0.001, True, 1e-10)
+        o.set_dt_replay(log[log["sys"] == s]["dt"])
+        o.advance(1e30, max_steps=ens.stats(s)["n_passed_step"])
+        eo, mine = o.events(), ev[sysv == s]
+        assert kind in {int(e["event_name"]) for e in eo}
+        assert len(mine) == len(eo)
+        for a, b in zip(mine, eo):
+            assert (a["event_name"], a["id1"], a["id2"]) == (b["event_name"], b["id1"], b["id2"])
+            assert H.same(a["t"], b["t"]) and H.same(a["d"], b["d"])
+        rg, vg, pg, mg, _ = ens.state(s)
+        ro, vo, po, mo, _ = o.state()
+        act_g, act_o = mg["id"] > 0, mo["id"] > 0
+        assert np.array_equal(mg["id"][act_g], mo["id"][act_o])
+        for f in "xyz":
+            assert H.same(rg[f][act_g], ro[f][act_o]) and H.same(vg[f][act_g], vo[f][act_o])
+
+
 def test_ensemble_mixed_and_energy(gpulib):
     disks = [bodies.config_disk("ensemble_member", seed=s, n=600) for s in (1, 2, 3)]
     ens = Ensemble(disks, bodies.thresholds(collision_factor=0.0))
