@@ -33,6 +33,7 @@
 #include "common.cuh"
 #include "dfloat.cuh"
 #include "kernels.h"
+#include "tma.cuh"
 
 namespace redgb {
 
@@ -479,60 +480,10 @@ __device__ __forceinline__ FlagTerm mixed_flag_term(const MixedArgs& a, const Ti
 // 8 KB copy of MX_T split positions), double-buffered: tile t + 2 is requested while tile t
 // is computed, each buffer's arrival is signalled on its own mbarrier (transaction bytes),
 // and one CTA barrier per tile releases the buffer for reuse.  Every wait on a copy is
-// bounded, by MX_WAIT_NS of the GPU's global timer (and, should the timer not advance, by
-// MX_WAIT_POLLS polls); a CTA whose copy does not arrive sets a.err, waits (again bounded)
+// bounded (tma.cuh: TMA_WAIT_NS of the GPU's global timer, or TMA_WAIT_POLLS polls should the
+// timer not advance); a CTA whose copy does not arrive sets a.err, waits (again bounded)
 // for the copies it issued, and returns.  `a.hold` (a test hook) issues no copies, so that
 // the waits run out and the host sees the error status.
-constexpr unsigned long long MX_WAIT_NS = 1000000000ull;  // one second
-constexpr unsigned MX_WAIT_POLLS = 1u << 28;
-
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned phase)
-{
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(phase)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ unsigned long long global_ns()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned phase)
-{
-    const unsigned long long t0 = global_ns();
-    for (unsigned k = 0; k < MX_WAIT_POLLS; k++) {
-        if (mbar_try_wait(bar, phase)) return true;
-        if ((k & 63u) == 63u && global_ns() - t0 > MX_WAIT_NS) return false;
-    }
-    return false;
-}
-
-// one thread: expect `bytes` on `bar` and start the bulk copy global -> shared
-__device__ __forceinline__ void tma_tile(void* dst, const void* src, unsigned bytes, unsigned long long* bar)
-{
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
 
 // dynamic shared memory of grav_mixed_kernel
 struct MixedSmem {
