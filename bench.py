@@ -447,7 +447,7 @@ def cpu_ensemble(seeds, years, hill, processes):
 
 
 def dense_ring_section(args):
-    """BASELINE config 4: 131 072 self-gravitating bodies in a narrow ring (a in [0.9, 1.1]
+    """The dense-ring stress workload: 131 072 self-gravitating bodies in a narrow ring (a in [0.9, 1.1]
     AU, e, i ~ R(0.002)) around a 1 Msun star plus a 3e-6 Msun embryo at 1 AU, masses
     log-uniform in [1e-11, 1e-9] Msun; RKF5 adaptive at tolerance 1e-9, collisions at R1 + R2,
     close encounters at 3 mutual Hill radii.  A bounded sample of the 10-year run: mixed
