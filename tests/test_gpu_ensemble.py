@@ -223,6 +223,35 @@ def test_ensemble_mixed_screen_cutoffs_keep_every_event(gpulib):
     assert out[T.GRAVITY_MIXED] == out[T.GRAVITY_FP64]
 
 
+def test_ensemble_heavy_light_events_match_fp64(gpulib):
+    """Disks of star, giants and planetesimals (the symmetric heavy-light kernel's plans: each
+    heavy-light pair screened once, in the planetesimal's row), with planetesimals placed
+    inside the giants' Hill spheres and two overlapping a giant: over one step the mixed
+    ensemble records the FP64 ensemble's close-encounter and collision records, pair for
+    pair."""
+    disks = []
+    for seed in (4, 5):
+        d = bodies.config_disk("ensemble_member", seed=seed, n=600)
+        offsets = [(0.05 * k, 0.03, 0.01) for k in range(1, 9)] + [(3e-4, 0.0, 0.0), (0.0, -2e-4, 1e-4)]
+        for k, off in enumerate(offsets):
+            g = 1 + k % 2
+            for f, c in zip("xyz", off):
+                d.r[f][3 + k] = d.r[f][g] + c
+        disks.append(d)
+    thr = bodies.thresholds(collision_factor=1.0)
+    out = {}
+    for mode in (T.GRAVITY_FP64, T.GRAVITY_MIXED):
+        ens = Ensemble(disks, thr)
+        ens.set_integrator(0.001, 1e-10)
+        ens.set_options(gravity_mode=mode, hill_factor=3.0)
+        ens.advance(0.0005)  # runs while t <= t_stop: one step of the first trial size
+        ev, sysv = ens.events()
+        out[mode] = [(int(s), int(e["event_name"]), int(e["id1"]), int(e["id2"])) for e, s in zip(ev, sysv)]
+    kinds = {k for _, k, _, _ in out[T.GRAVITY_FP64]}
+    assert {T.EVENT_CLOSE_ENCOUNTER, T.EVENT_COLLISION} <= kinds, out[T.GRAVITY_FP64]
+    assert out[T.GRAVITY_MIXED] == out[T.GRAVITY_FP64]
+
+
 def test_proposer_fallback_keeps_the_run_correct(gpulib):
     """A proposer that always asks for the largest step it may (twice the plain controller's):
     the embedded error estimate rejects its proposals, each disk falls back to the plain
