@@ -396,9 +396,10 @@ RG_API int rg_ens_kernel_count(rg_ens* ens, int64_t* n_kernels, int64_t* n_graph
  * shape of the current gravity mode (`reps` evaluations each, CUDA events on the ensemble's
  * stream) and keeps the fastest.  FP64 mode: sinks per pair-parallel CTA x the row-kernel
  * source limit -- every candidate sums in the reference's order, so results stay bit-exact;
- * mixed mode: sources per few-sink CTA (0 = automatic, 512, 1024, 2048; reported in
- * `mixed_chunks`) x the row-kernel limit.  The ensemble's state is not changed.  `out` (may be
- * NULL) receives the choice. */
+ * mixed mode: sources per few-sink CTA -- for disks of a few heavy bodies and many light
+ * ones, the light bodies per CTA of the symmetric heavy-light kernel, about, in whole waves
+ * (0 = automatic, about 2048; 512, 1024, 2048; reported in `mixed_chunks`) -- x the row-kernel
+ * limit.  The ensemble's state is not changed.  `out` (may be NULL) receives the choice. */
 RG_API int rg_ens_autotune(rg_ens* ens, int reps, rg_tune_t* out);
 
 /* ------------------------------------------------------------------ learned step proposer */

@@ -145,8 +145,9 @@ typedef struct rg_tune {
     int32_t pairpar_sinks;   /* FP64 mode: sinks per pair-parallel CTA (8, 12, 16, 18, 24, 32, 36) */
     int32_t rowseq_max_src;  /* blocks with at most this many sources use the row kernel         */
     int32_t mixed_chunks;    /* mixed mode: sources per grid.y chunk -- of the mixed kernel
-                                (rg_autotune) or the few-sink kernel (rg_ens_autotune); 0: chosen
-                                from the SM count                                               */
+                                (rg_autotune) or the few-sink kernel and the light bodies per
+                                CTA of the symmetric heavy-light kernel (rg_ens_autotune); 0:
+                                chosen from the SM count                                        */
     int32_t candidates;      /* configurations timed                                             */
     double  ms_per_eval;     /* the chosen configuration: CUDA-event time of one evaluation       */
     double  ms_before;       /* the configuration in place before tuning                         */
