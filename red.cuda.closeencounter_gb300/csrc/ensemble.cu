@@ -1058,9 +1058,10 @@ void build_gravity_plan(rg_ens* e)
     // mixed plan: a system whose SI block is a few heavy bodies (a few-sink block over every
     // massive body) and whose NSI block takes the row kernel over them evaluates the pairs
     // between the two blocks once, for both rows (grav_df_sym, the heavy-heavy pairs with
-    // them).  The light bodies of all such systems, end to end, are cut into equal ranges of
-    // about sym_chunk, one per CTA, their count whole waves of resident CTAs; a range's pieces
-    // in different systems are its segments, each one part of its system's heavy rows.
+    // them).  The light bodies of all such systems, end to end, are cut into ranges of equal
+    // cost (plan_tools.h), about sym_chunk bodies each, one per CTA, their count whole waves of
+    // resident CTAs; a range's pieces in different systems are its segments, each one part of
+    // its system's heavy rows.
     e->sym_chunk = e->few_chunk > 0 ? e->few_chunk : ENS_SYM_CHUNK;
     std::vector<char> sym(e->n_sys, 0);
     std::vector<Tile> sym_systems;
