@@ -39,6 +39,7 @@
 #include "host_tools.h"
 #include "kernels.h"
 #include "plan_tools.h"
+#include "tma.cuh"
 #include "rk_tables.h"
 #include "mlp.h"
 #include <cuda_bf16.h>
@@ -145,6 +146,7 @@ __device__ __forceinline__ double ens_combine_df_sum(const DF* w, const DF* k, d
 template <int FORM, int NTERM>
 __global__ void __launch_bounds__(256) ens_combine_df_kernel(EnsStageArgs a)
 {
+    pdl_wait();  // first: every CTA waits for the kernel before it (launch_stage may overlap them)
     const StageTile t = a.tiles[blockIdx.x];
     if (!a.active[t.sys]) return;
     const double dt = a.dt[t.sys];
@@ -1407,10 +1409,21 @@ int launch_stage(rg_ens* e, int form, int nterm, const int* stages, const double
     const int g = (int)e->stiles.size();
     if (g <= 0) return RG_OK;
     const bool df = e->gravity_mode == RG_GRAVITY_MIXED;  // double-float stage vectors
+    // the mixed form's combination may be scheduled while the gravity kernel before it
+    // finishes (programmatic dependent launch; the kernel waits before it reads anything)
+    cudaLaunchAttribute pdl[1];
+    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)g);
+    cfg.blockDim = dim3(256);
+    cfg.stream = e->st;
+    cfg.attrs = pdl;
+    cfg.numAttrs = 1;
 #define RG_ENS(F, T)                                                     \
     do {                                                                 \
         if (df)                                                          \
-            ens_combine_df_kernel<F, T><<<g, 256, 0, e->st>>>(a);        \
+            RG_CUDA_CHECK(cudaLaunchKernelEx(&cfg, ens_combine_df_kernel<F, T>, a)); \
         else                                                             \
             ens_combine_kernel<F, T><<<g, 256, 0, e->st>>>(a);           \
     } while (0)

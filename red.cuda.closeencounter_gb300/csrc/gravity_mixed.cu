@@ -1005,6 +1005,7 @@ struct DfSymArgs {
 template <bool SCREEN, int HMAX, bool FROM64>
 __global__ void __launch_bounds__(256, DF_SYM_RESIDENT) grav_df_sym(DfSymArgs a)
 {
+    pdl_wait();  // first: every CTA waits for the kernel before it (the launch may overlap them)
     const GravArgs& g = a.g;
     __shared__ SplitPos s_h[HMAX];
     __shared__ float s_R[HMAX], s_rho[HMAX], s_close2[HMAX];
@@ -1292,12 +1293,22 @@ int launch_grav_df_sym(const GravArgs& g, const int* cta_seg, int n_cta, const v
     DfSymArgs b{g, cta_seg, (const SplitPos*)split, tile_row0, partial, rows, pitch, row_sink, row_nparts, ticket,
                 mass_f2};
     const bool screen = g.record || g.hill;
-#define RG_SYM2(H, F)                                                \
-    do {                                                             \
-        if (screen)                                                  \
-            grav_df_sym<true, H, F><<<n_cta, 256, 0, st>>>(b);       \
-        else                                                         \
-            grav_df_sym<false, H, F><<<n_cta, 256, 0, st>>>(b);      \
+    // may be scheduled while the kernel before it finishes (programmatic dependent launch)
+    cudaLaunchAttribute pdl[1];
+    pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    pdl[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)n_cta);
+    cfg.blockDim = dim3(256);
+    cfg.stream = st;
+    cfg.attrs = pdl;
+    cfg.numAttrs = 1;
+#define RG_SYM2(H, F)                                                                   \
+    do {                                                                                \
+        if (screen)                                                                     \
+            RG_CUDA_CHECK(cudaLaunchKernelEx(&cfg, grav_df_sym<true, H, F>, b));        \
+        else                                                                            \
+            RG_CUDA_CHECK(cudaLaunchKernelEx(&cfg, grav_df_sym<false, H, F>, b));       \
     } while (0)
 #define RG_SYM(H)               \
     do {                        \

@@ -1,4 +1,5 @@
-// tma.cuh -- bulk copies global -> shared (cp.async.bulk) completed on mbarriers, with
+// tma.cuh -- asynchronous-execution helpers: bulk copies global -> shared (cp.async.bulk)
+// completed on mbarriers, and the wait of a programmatically dependent launch.  Bulk copies have
 // bounded waits: a wait gives up after TMA_WAIT_NS of the GPU's global timer (or, should the
 // timer not advance, after TMA_WAIT_POLLS polls) and returns false, so that a kernel whose
 // copy does not arrive can report an error status instead of spinning.
@@ -73,5 +74,11 @@ __device__ __forceinline__ void bulk_copy(void* dst, const void* src, unsigned b
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
 }
+
+// Programmatic dependent launch: a kernel launched with the programmatic-serialisation
+// attribute may be scheduled while the kernel before it on the stream finishes its last CTAs;
+// it must not read what that kernel writes before this wait (which returns at once for a
+// kernel launched without the attribute).
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 }  // namespace redgb
