@@ -329,22 +329,19 @@ __device__ __forceinline__ double rn_div(double a, double b)
 // addition of the serial loop.  The first term that breaks this is added by lane 0 on the
 // FP64 pipe; after a pass that took at least SERIAL_GOOD_PASS terms another pass follows,
 // otherwise lane 0 adds the rest of the round in order (one active lane: the FP64 pipe's cost
-// of a one-lane addition is small, its latency is what the serial loop pays).  One term is
-// enough (measured on GB300 over thresholds of 1 to 12: a 256-disk FP64 ensemble attempt
-// 12.0 ms at 1, 13.2 at 2, 16.0 at 8): a pass costs less than the serial additions it saves
-// as soon as it takes a term.
+// of a one-lane addition is small, its latency is what the serial loop pays).
 //
 // A running sum that keeps leaving its binade (a component hovering about zero, where the
-// terms cancel) makes every pass fail at its first term; after such a round the next
-// `backoff` rounds are serial, the backoff going 0, 1, 2, 4, 8 while rounds keep failing that
-// way and back to 0 after a round whose passes all took terms.  SerialSumState holds that per
-// chain; it starts as {0, 0}.
+// terms cancel) makes every pass short; after such a round the next `backoff` rounds are
+// serial, the backoff going 0, 1, 2, 4, 8 while rounds keep failing that way and back to 0
+// after a round whose passes were all long.  SerialSumState holds that per chain; it starts
+// as {0, 0}.
 struct SerialSumState {
     int skip;     // serial rounds still to do
     int backoff;  // serial rounds after the next poor round
 };
 
-constexpr int SERIAL_GOOD_PASS = 1;
+constexpr int SERIAL_GOOD_PASS = 8;
 
 // lane 0 adds T[from..m) in order; every lane returns the result
 __device__ __forceinline__ double serial_tail(double acc, const double* T, int from, int m)

@@ -59,7 +59,7 @@ static double round_emulated(double acc, const double* t, int m, State& st, long
             *fast += stop - pos;
         }
         if (stop >= m) break;
-        if (stop - pos < 1) {  // SERIAL_GOOD_PASS
+        if (stop - pos < 8) {  // SERIAL_GOOD_PASS
             st.skip = st.backoff;
             st.backoff = st.backoff ? (st.backoff * 2 < 8 ? st.backoff * 2 : 8) : 1;
             return tail(stop, m);
